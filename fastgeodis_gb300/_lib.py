@@ -1,0 +1,104 @@
+"""ctypes binding of the engine's C ABI (``include/fastgeodis_gb300.h``).
+
+The shared library ``fastgeodis_gb300/_fg.so`` is built in-tree by
+``fastgeodis_gb300/_build.py`` (``__graft_entry__.build()`` runs it).  There
+is no fallback: if the library is missing or does not load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_fg.so")
+
+FG_OK = 0
+FG_ERR_INVALID_ARGUMENT = 1
+FG_ERR_CUDA = 2
+FG_ERR_WORKSPACE = 3
+FG_ERR_TIMEOUT = 4
+FG_ERR_UNSUPPORTED = 5
+
+FG_OP_PLAIN = 0
+FG_OP_SIGNED = 1
+FG_OP_GSF = 2
+
+# every symbol include/fastgeodis_gb300.h declares
+EXPORTED = (
+    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_profile_begin", "fg_profile_end",
+    "fg_workspace_bytes", "fg_workspace_status",
+    "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
+    "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
+    "fg_GSF2d", "fg_GSF3d",
+)
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    """A non-argument failure reported by the engine (CUDA error, timeout...)."""
+
+
+def load():
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"fastgeodis_gb300 engine library not found at {LIB_PATH}; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` or "
+            "`python fastgeodis_gb300/_build.py`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i, f, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.fg_abi_version.restype = i
+    L.fg_last_error.restype = ctypes.c_char_p
+    L.fg_workspace_bytes.argtypes = [i, i, i, i, i]
+    L.fg_workspace_bytes.restype = sz
+    L.fg_profile_begin.argtypes = []
+    L.fg_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_double)]
+    L.fg_set_tuning.argtypes = [i, i]
+    L.fg_set_tuning.restype = i
+    L.fg_workspace_status.argtypes = [vp, vp]
+    L.fg_workspace_status.restype = i
+    L.fg_generalised_geodesic2d.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp, sz, vp]
+    L.fg_signed_generalised_geodesic2d.argtypes = L.fg_generalised_geodesic2d.argtypes
+    L.fg_generalised_geodesic3d.argtypes = [vp, i, i, i, i, vp, i, fp, vp, f, f, f, i, vp, sz, vp]
+    L.fg_signed_generalised_geodesic3d.argtypes = L.fg_generalised_geodesic3d.argtypes
+    L.fg_GSF2d.argtypes = [vp, i, i, i, vp, i, f, f, f, i, vp, vp, sz, vp]
+    L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
+    for name in EXPORTED:
+        if name not in ("fg_last_error",):
+            getattr(L, name).restype = getattr(L, name).restype or i
+    if L.fg_abi_version() != 1:
+        raise ImportError("fastgeodis_gb300 engine ABI mismatch")
+    _lib = L
+    return L
+
+
+def profile_begin() -> None:
+    check(load().fg_profile_begin())
+
+
+def profile_end():
+    """Returns (summed pass-kernel ms, launches, voxel-passes) since profile_begin()."""
+    ms, n, vp = ctypes.c_double(), ctypes.c_int(), ctypes.c_double()
+    check(load().fg_profile_end(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(vp)))
+    return ms.value, n.value, vp.value
+
+
+def last_error() -> str:
+    msg = load().fg_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int) -> None:
+    """Map an engine status code onto the reference's exception types."""
+    if rc == FG_OK:
+        return
+    msg = last_error()
+    if rc == FG_ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    raise EngineError(f"fastgeodis_gb300 engine error {rc}: {msg}")

@@ -1,0 +1,135 @@
+/*
+ * fastgeodis_gb300 -- C ABI of the GB300 generalised geodesic distance engine.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*, a cudaStream_t), launches on that stream and returns
+ * without synchronising.  Tensors are float32, contiguous, in the reference's
+ * layout without the batch dimension (which the reference requires to be 1):
+ *   image  [C][H][W]      or [C][D][H][W]
+ *   mask   [Cm][H][W]     or [Cm][D][H][W]
+ *   out    [Cm][H][W]     or [Cm][D][H][W]   (allocated by the caller)
+ * As in the reference, every mask channel is scaled by v and only channel 0
+ * is swept.  Inputs are never modified.
+ *
+ * Arithmetic follows the reference's CPU path operation by operation, in
+ * float32 without contraction, so results are bit-identical to it.
+ *
+ * Scratch: each call needs a caller-provided device workspace of at least
+ * fg_workspace_bytes(...) bytes (256-byte aligned).  The library allocates
+ * no device memory.  A workspace may be reused by calls that are ordered on
+ * one stream; calls that may run concurrently need separate workspaces.
+ *
+ * Return value: FG_OK or an FG_ERR_* code; fg_last_error() gives a message
+ * (thread-local).  Kernels never trap: a bounded wait that expires records
+ * FG_ERR_TIMEOUT in the workspace, readable with fg_workspace_status().
+ */
+#ifndef FASTGEODIS_GB300_H
+#define FASTGEODIS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FG_API __attribute__((visibility("default")))
+#else
+#define FG_API
+#endif
+
+#define FG_ABI_VERSION 1
+
+#define FG_OK 0
+#define FG_ERR_INVALID_ARGUMENT 1 /* shape, size or pointer problem (the reference's std::invalid_argument) */
+#define FG_ERR_CUDA 2             /* a CUDA runtime call failed */
+#define FG_ERR_WORKSPACE 3        /* workspace missing or too small */
+#define FG_ERR_TIMEOUT 4          /* a bounded inter-CTA wait expired (recorded on the device) */
+#define FG_ERR_UNSUPPORTED 5      /* size beyond what this build plans for */
+
+/* Operation codes for fg_workspace_bytes. */
+#define FG_OP_PLAIN 0
+#define FG_OP_SIGNED 1
+#define FG_OP_GSF 2
+
+FG_API int fg_abi_version(void);
+FG_API const char *fg_last_error(void);
+
+/* Bytes of workspace needed by one call of the given operation on a volume
+ * of D*H*W voxels (D = 1 for 2D) with C image channels. */
+FG_API size_t fg_workspace_bytes(int op, int C, int D, int H, int W);
+
+/* Planner limits (no counterpart in the reference, which has no planner):
+ * the largest cross-section region, in cells, one CTA may own, and the most
+ * tiles one pass may use.  0 restores the default.  Results do not depend on
+ * these values; they exist to tune and to exercise multi-tile plans. */
+FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
+
+/* Event timing of the sweep kernels (no counterpart in the reference):
+ * between fg_profile_begin() and fg_profile_end(), every pass launch is
+ * bracketed by CUDA events on its stream.  fg_profile_end synchronises those
+ * events and returns the summed kernel time in ms, the number of launches and
+ * the voxel-passes (cells x maps updated) they performed.  Not for use inside
+ * CUDA graph capture. */
+FG_API int fg_profile_begin(void);
+FG_API int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_passes);
+
+/* Reads (and clears) the device status word of a workspace after
+ * synchronising `stream`: FG_OK, or FG_ERR_TIMEOUT if a kernel gave up. */
+FG_API int fg_workspace_status(void *workspace, void *stream);
+
+/* Replaces FastGeodis.generalised_geodesic2d
+ * (reference: FastGeodis/__init__.py:37-65 -> FastGeodis/fastgeodis.cpp:44-90
+ *  -> FastGeodis/fastgeodis_cuda.cu:278-318).
+ * l_grad = lamb, l_eucl = 1 - lamb, both already narrowed to float. */
+FG_API int fg_generalised_geodesic2d(const float *image, int C, int H, int W,
+                              const float *mask, int Cm, float *out, float v,
+                              float l_grad, float l_eucl, int iterations,
+                              void *workspace, size_t workspace_bytes,
+                              void *stream);
+
+/* Replaces FastGeodis.generalised_geodesic3d
+ * (reference: FastGeodis/__init__.py:68-98 -> FastGeodis/fastgeodis.cpp:92-146
+ *  -> FastGeodis/fastgeodis_cuda.cu:587-656).  spacing: 3 floats (host). */
+FG_API int fg_generalised_geodesic3d(const float *image, int C, int D, int H, int W,
+                              const float *mask, int Cm, const float *spacing,
+                              float *out, float v, float l_grad, float l_eucl,
+                              int iterations, void *workspace,
+                              size_t workspace_bytes, void *stream);
+
+/* Replaces FastGeodis.signed_generalised_geodesic2d: D(mask) - D(1 - mask)
+ * (reference: FastGeodis/__init__.py:101-130 -> FastGeodis/fastgeodis.cpp:241-249). */
+FG_API int fg_signed_generalised_geodesic2d(const float *image, int C, int H, int W,
+                                     const float *mask, int Cm, float *out,
+                                     float v, float l_grad, float l_eucl,
+                                     int iterations, void *workspace,
+                                     size_t workspace_bytes, void *stream);
+
+/* Replaces FastGeodis.signed_generalised_geodesic3d
+ * (reference: FastGeodis/__init__.py:133-162 -> FastGeodis/fastgeodis.cpp:251-258). */
+FG_API int fg_signed_generalised_geodesic3d(const float *image, int C, int D, int H,
+                                     int W, const float *mask, int Cm,
+                                     const float *spacing, float *out, float v,
+                                     float l_grad, float l_eucl, int iterations,
+                                     void *workspace, size_t workspace_bytes,
+                                     void *stream);
+
+/* Replaces FastGeodis.GSF2d (reference: FastGeodis/__init__.py:526-553 ->
+ * FastGeodis/fastgeodis.cpp:319-330).  lambda as float; 1 - lambda is formed
+ * in float inside, as the reference does. */
+FG_API int fg_GSF2d(const float *image, int C, int H, int W, const float *mask,
+             int Cm, float theta, float v, float lambda, int iterations,
+             float *out, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Replaces FastGeodis.GSF3d (reference: FastGeodis/__init__.py:556-585 ->
+ * FastGeodis/fastgeodis.cpp:332-343). */
+FG_API int fg_GSF3d(const float *image, int C, int D, int H, int W, const float *mask,
+             int Cm, float theta, const float *spacing, float v, float lambda,
+             int iterations, float *out, void *workspace,
+             size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTGEODIS_GB300_H */

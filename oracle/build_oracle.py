@@ -1,0 +1,132 @@
+"""Build recipes for the CPU oracle (test infrastructure only).
+
+Two artefacts are produced here; neither is part of the shipped product:
+
+* ``oracle/_build/libfg_oracle.so`` -- the plain-C restatement of FastGeodis'
+  raster scan (``oracle/fg_oracle.c``), compiled with ``gcc`` and OpenMP.  It
+  runs on any host (x86 container or the Arm GPU host) and is the parity
+  checker and the timed CPU baseline.
+* ``oracle/_ref/fastgeodis_ref_cpu*.so`` -- the reference's own CPU sources
+  (``FastGeodis/*.cpp`` of masadcv/FastGeodis 1.0.5), compiled file by file with
+  ``g++`` against the installed torch headers, without running the reference's
+  ``setup.py``.  It only exists where the reference source tree is mounted and
+  is used to generate the committed golden vectors under ``tests/golden/``.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+may load these libraries.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import sysconfig
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+PORT_SRC = os.path.join(HERE, "fg_oracle.c")
+PORT_LIB = os.path.join(BUILD_DIR, "libfg_oracle.so")
+REF_MODULE = "fastgeodis_ref_cpu"
+DEFAULT_REF_ROOT = os.environ.get("FG_REFERENCE_ROOT", "/root/reference")
+
+
+def _newer(target: str, *sources: str) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_port(force: bool = False, verbose: bool = False) -> str:
+    """Compile the C restatement.  ``-ffp-contract=off`` keeps every float
+    operation separately rounded on aarch64 as well, which is how the
+    reference's x86-64 build (no ``-march``, so no FMA) evaluates them."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and _newer(PORT_LIB, PORT_SRC):
+        return PORT_LIB
+    cmd = [
+        "gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp",
+        "-ffp-contract=off", "-fno-fast-math", "-fsigned-char",
+        PORT_SRC, "-o", PORT_LIB + ".tmp", "-lm",
+    ]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(PORT_LIB + ".tmp", PORT_LIB)
+    return PORT_LIB
+
+
+def reference_module_path() -> str:
+    return os.path.join(REF_DIR, REF_MODULE + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_reference(ref_root: str = DEFAULT_REF_ROOT, force: bool = False,
+                    verbose: bool = False) -> str | None:
+    """Compile the reference's CPU path (all of ``FastGeodis/*.cpp``; the
+    pybind module in ``fastgeodis.cpp`` references every backend) into a
+    Python extension module under ``oracle/_ref``.  Returns None when the
+    reference tree is absent (for example on the GPU host)."""
+    src_dir = os.path.join(ref_root, "FastGeodis")
+    if not os.path.isdir(src_dir):
+        return None
+    import torch
+    from torch.utils import cpp_extension
+
+    out = reference_module_path()
+    sources = sorted(
+        os.path.join(src_dir, f) for f in os.listdir(src_dir) if f.endswith(".cpp")
+    )
+    if not force and _newer(out, *sources):
+        return out
+    os.makedirs(REF_DIR, exist_ok=True)
+    abi = int(torch._C._GLIBCXX_USE_CXX11_ABI)
+    inc = [f"-I{p}" for p in cpp_extension.include_paths()]
+    inc += [f"-I{sysconfig.get_paths()['include']}", f"-I{src_dir}",
+            f"-I{os.path.join(ref_root, 'dependency')}"]
+    defs = ["-DTORCH_API_INCLUDE_EXTENSION_H", f"-DTORCH_EXTENSION_NAME={REF_MODULE}",
+            f"-D_GLIBCXX_USE_CXX11_ABI={abi}", "-DAT_PARALLEL_OPENMP=1"]
+    flags = ["-O2", "-g0", "-std=c++17", "-fPIC", "-fopenmp"]
+    objs = []
+
+    def compile_one(src: str) -> str:
+        obj = os.path.join(REF_DIR, os.path.basename(src) + ".o")
+        cmd = ["g++", *flags, *defs, *inc, "-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.check_call(cmd)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(compile_one, sources))
+    lib_dir = os.path.join(os.path.dirname(torch.__file__), "lib")
+    link = ["g++", "-shared", "-fopenmp", *objs, "-o", out + ".tmp",
+            f"-L{lib_dir}", "-lc10", "-ltorch", "-ltorch_cpu", "-ltorch_python",
+            f"-Wl,-rpath,{lib_dir}"]
+    if verbose:
+        print(" ".join(link))
+    subprocess.check_call(link)
+    os.replace(out + ".tmp", out)
+    for o in objs:
+        os.remove(o)
+    return out
+
+
+def load_reference():
+    """Import the compiled reference CPU module (None if it was not built)."""
+    path = reference_module_path()
+    if not os.path.exists(path):
+        return None
+    import importlib.util
+    import torch  # noqa: F401  (loads libtorch before the extension)
+
+    spec = importlib.util.spec_from_file_location(REF_MODULE, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+if __name__ == "__main__":
+    print(build_port(force="--force" in sys.argv, verbose=True))
+    print(build_reference(force="--force" in sys.argv, verbose=True))
