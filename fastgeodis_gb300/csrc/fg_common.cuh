@@ -1,0 +1,69 @@
+// Shared declarations of the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fastgeodis_gb300.h"
+
+namespace fgi {
+
+constexpr int kThreads = 512;            // largest CTA; one thread per run of 4 cells
+constexpr int kMaxRegion = kThreads * 4; // cells of one CTA's region (tile + halo)
+constexpr int kMaxMaps = 2;              // distance maps updated by one launch (they share the image)
+constexpr int kMaxChannels = 4;          // image channels held in registers
+constexpr int kMaxTiles = 2048;          // progress flags in a workspace
+constexpr unsigned kSpinLimit = 1u << 23; // flag polls (each an L2 round trip, ~0.3-1 us) before FG_ERR_TIMEOUT
+
+// Arithmetic of one candidate.  GENERAL is the reference expression
+// (D + l_eucl*ld) + l_grad*L1.  EUCLID (l_grad == 0) and GEO (l_eucl == 0 and
+// l_grad == 1) drop a term that is exactly +0 or a factor that is exactly 1
+// for finite inputs, so they return the same bits with less work.
+enum Mode { MODE_GENERAL = 0, MODE_EUCLID = 1, MODE_GEO = 2 };
+
+// One directional pass ("sweep") over a layout whose innermost dimension is
+// cross-section dimension 2 (stride 1).  Cross-section dimension 1 exists
+// for volumes only (CROSS == 2).  The distance maps are read in that layout
+// and written either in place or, for the pass that changes layout, in a
+// layout whose innermost dimension is the swept one ("transposed write").
+struct PassArgs {
+  const float *img;               // image in the read layout, channel 0
+  long long img_cs;               // elements between image channels
+  int C;                          // image channels
+  const float *dsrc[kMaxMaps];    // distance maps, read layout
+  float *ddst[kMaxMaps];          // distance maps, write layout
+  float lg[kMaxMaps];             // l_grad per map
+  float e[kMaxMaps][9];           // l_eucl * ld[n] per map and neighbour n = 3*(d1+1) + (d2+1)
+  int L, dir;                     // steps; +1 forward, -1 backward
+  long long s_str, st1;           // read layout strides of a step and of cross dimension 1
+  long long ws_str, wst1, wst2;   // write layout strides (step, cross 1, cross 2)
+  int N1, N2;                     // cross-section extents
+  int T1, T2, K1, K2;             // tile extents and halo widths
+  int tiles1, tiles2;
+  int S;                          // steps per chunk: halo hand-off and transposed-flush period
+  int B2;                         // floats per buffer row (4-cell left apron, runs of 4, right apron)
+  int rowf;                       // floats per buffer position (all rows), multiple of 32
+  int vec;                        // runs may use 16-byte global loads and stores
+  unsigned *flags;                // per-tile progress (chunks completed)
+  unsigned flag_base;
+  int *status;                    // FG_ERR_TIMEOUT if a bounded wait expired
+};
+
+struct LaunchCfg {
+  int tiles;
+  int threads;
+  size_t smem;
+};
+
+// Shared-memory bytes of a pass kernel for a region of R1 x R2 cells.
+size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2, int *rowf,
+                       int *nown_max);
+
+// Launchers (one translation unit per cross-section rank).
+int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
+int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
+
+// Host error reporting shared by the units.
+int set_error(int code, const char *msg);
+
+}  // namespace fgi

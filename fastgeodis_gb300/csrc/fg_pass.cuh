@@ -1,0 +1,388 @@
+// The sweep kernel: one directional pass of the raster scan over one tile of
+// the cross-section per CTA.
+//
+//   D[t][x] = min(D[t][x], min_n D[t-1][x+n] + l_eucl*ld[n] + l_grad*L1(I[t][x], I[t-1][x+n]))
+//   (reference: FastGeodis/fastgeodis_cpu.cpp:53-162 and :203-340)
+//
+// Design (this build's own):
+//   * A CTA owns a tile of the cross-section plus a halo of K cells per side
+//     and walks every step of the pass.  Each thread owns a run of 4
+//     consecutive cells along the innermost cross dimension.
+//   * A thread's own inputs of a step (old distance and image values) are
+//     loaded straight into registers P steps ahead (16-byte loads where the
+//     layout allows).  Shared memory only holds the rows its neighbours read:
+//     the previous step's distances and image values.  One barrier per step.
+//   * With several tiles, the halo lets a CTA run S <= K steps on its own.
+//     Every S steps it replaces its halo cells of the last row by the exact
+//     values its neighbours published (per-tile progress flags,
+//     release/acquire, bounded waits).  Halo cells are never written back.
+//   * Layout: the swept axis is never the contiguous one in the read layout.
+//     The pass that hands over to a sweep along the contiguous axis writes
+//     its result transposed (step innermost), through an S-row shared ring
+//     flushed as S-element segments.
+//   * Arithmetic: float32, every operation rounded on its own, in the
+//     reference CPU order; fminf ignores NaN, so cells outside the image
+//     (held as NaN) never contribute a candidate, as in the reference.
+#pragma once
+
+#include "fg_common.cuh"
+
+namespace fgi {
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_status(const int *p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// Global loads pinned where they are written (asm volatile), so that the
+// prefetch of step t+P is issued at step t and not moved next to its use.
+__device__ __forceinline__ float4 ldg4_pinned(const float *p) {
+  float4 v;
+  asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];\n" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float4 ldg4_nc_pinned(const float *p) {
+  float4 v;
+  asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];\n" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ldg_pinned(const float *p) {
+  float v;
+  asm volatile("ld.global.f32 %0, [%1];\n" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ldg_nc_pinned(const float *p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];\n" : "=f"(v) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ float f4get(const float4 &v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ void f4set(float4 &v, int i, float x) {
+  if (i == 0) v.x = x;
+  else if (i == 1) v.y = x;
+  else if (i == 2) v.z = x;
+  else v.w = x;
+}
+
+// channels held in registers and the prefetch depth of a kernel variant
+__host__ __device__ constexpr int pass_nch(int ct, int mode) {
+  return mode == MODE_EUCLID ? 0 : (ct == 0 ? kMaxChannels : ct);
+}
+__host__ __device__ constexpr int pass_depth(int nch, int m) { return (nch + m <= 2) ? 8 : ((nch + m <= 4) ? 4 : 2); }
+
+template <int CROSS, int CT, int M, int MODE, bool WT>
+__global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) {
+  constexpr bool USE_IMG = MODE != MODE_EUCLID;
+  constexpr int NCH = pass_nch(CT, MODE);
+  constexpr int NCHR = NCH > 0 ? NCH : 1;
+  constexpr int P = pass_depth(NCH, M);
+  constexpr int A1 = CROSS == 2 ? 1 : 0;  // apron row above the region
+  constexpr int NR = CROSS == 2 ? 3 : 1;  // stencil rows
+  extern __shared__ __align__(16) float sm[];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int NT = blockDim.x, nwarps = NT >> 5;
+  const int C = USE_IMG ? (CT == 0 ? a.C : CT) : 0;
+  const int L = a.L, S = a.S;
+  const int SR = WT ? S : 2;  // distance rows kept in shared memory
+  const int tile = blockIdx.x;
+  const int ti1 = tile / a.tiles2, ti2 = tile - ti1 * a.tiles2;
+  const int R1 = CROSS == 2 ? a.T1 + 2 * a.K1 : 1, R2 = a.T2 + 2 * a.K2;
+  const int B2 = a.B2, rowf = a.rowf;
+  const int rs1 = CROSS == 2 ? ti1 * a.T1 - a.K1 : 0, rs2 = ti2 * a.T2 - a.K2;
+  const int o1lo = CROSS == 2 ? a.K1 : 0;
+  const int o1hi = CROSS == 2 ? a.K1 + min(a.T1, a.N1 - ti1 * a.T1) : 1;
+  const int o2lo = a.K2, o2hi = a.K2 + min(a.T2, a.N2 - ti2 * a.T2);
+  const float qnan = __int_as_float(0x7fffffff);
+
+  float *dring = sm;                   // [SR][M][rowf] distances of the last SR steps
+  float *iring = sm + SR * M * rowf;   // [2][NCH][rowf] image values of the last two steps
+  int2 *otab = reinterpret_cast<int2 *>(iring + 2 * NCH * rowf);  // own cells (transposed flush)
+
+  // --- set-up ---
+  for (int i = tid; i < (SR * M + 2 * NCH) * rowf; i += NT) sm[i] = qnan;
+  int nown = 0;
+  if (WT) {
+    const int O1 = o1hi - o1lo, O2 = o2hi - o2lo;
+    nown = O1 * O2;
+    for (int i = tid; i < nown; i += NT) {
+      int o1 = o1lo + i / O2, o2 = o2lo + i % O2;
+      long long g = (long long)(rs1 + o1) * a.wst1 + (long long)(rs2 + o2) * a.wst2;
+      otab[i] = make_int2((o1 + A1) * B2 + 4 + o2, (int)g);
+    }
+  }
+  const int rpr = (R2 + 3) >> 2;
+  const int r1 = tid / rpr, u = tid - (tid / rpr) * rpr;
+  const int g1 = rs1 + r1, g20 = rs2 + 4 * u;
+  const int cb = (r1 + A1) * B2 + 4 + 4 * u;
+  unsigned valid = 0, own = 0;
+  if (r1 < R1) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      int r2 = 4 * u + i, g2 = g20 + i;
+      bool in = r2 < R2 && g1 >= 0 && g1 < a.N1 && g2 >= 0 && g2 < a.N2;
+      if (in) valid |= 1u << i;
+      if (in && r1 >= o1lo && r1 < o1hi && r2 >= o2lo && r2 < o2hi) own |= 1u << i;
+    }
+  }
+  const bool active = valid != 0;
+  const bool full = valid == 0xFu && a.vec;
+  const unsigned halo = valid & ~own;
+  const long long roff = (long long)g1 * a.st1 + g20;                             // read layout
+  const long long woff = (long long)g1 * a.wst1 + (long long)g20 * a.wst2;       // write layout
+  int nbr = -1;  // neighbour tile polled by this thread
+  if (tid < 8) {
+    int d1, d2;
+    if (CROSS == 2) {
+      int k = tid < 4 ? tid : tid + 1;
+      d1 = k / 3 - 1;
+      d2 = k % 3 - 1;
+    } else {
+      d1 = 0;
+      d2 = tid == 0 ? -1 : 1;
+    }
+    int n1 = ti1 + d1, n2 = ti2 + d2;
+    if ((CROSS == 2 || tid < 2) && n1 >= 0 && n1 < a.tiles1 && n2 >= 0 && n2 < a.tiles2) nbr = n1 * a.tiles2 + n2;
+  }
+  const bool has_nb = a.tiles1 * a.tiles2 > 1;
+  __syncthreads();
+
+  auto pos = [&](int t) -> long long { return a.dir > 0 ? (long long)t : (long long)(L - 1 - t); };
+
+  float4 rd[P][M];
+  float4 ri[P][NCHR];
+  auto load_step = [&](int t, int k) {
+    const long long so = pos(t) * a.s_str + roff;
+    if (full) {
+#pragma unroll
+      for (int m = 0; m < M; m++) rd[k][m] = ldg4_pinned(a.dsrc[m] + so);
+#pragma unroll
+      for (int c = 0; c < NCH; c++)
+        if (c < C) ri[k][c] = ldg4_nc_pinned(a.img + c * a.img_cs + so);
+    } else {
+#pragma unroll
+      for (int m = 0; m < M; m++) {
+        rd[k][m] = make_float4(qnan, qnan, qnan, qnan);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          if (valid & (1u << i)) f4set(rd[k][m], i, ldg_pinned(a.dsrc[m] + so + i));
+      }
+#pragma unroll
+      for (int c = 0; c < NCH; c++) {
+        ri[k][c] = make_float4(qnan, qnan, qnan, qnan);
+        if (c < C) {
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+            if (valid & (1u << i)) f4set(ri[k][c], i, ldg_nc_pinned(a.img + c * a.img_cs + so + i));
+        }
+      }
+    }
+  };
+
+  auto wait_neighbours = [&](unsigned target) {
+    if (nbr >= 0) {
+      unsigned spins = 0;
+      while ((int)(ld_acquire(a.flags + nbr) - target) < 0) {
+        if (++spins > kSpinLimit || ((spins & 1023u) == 0 && ld_status(a.status) != 0)) {
+          atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
+          break;
+        }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+  };
+
+#pragma unroll
+  for (int k = 0; k < P; k++)
+    if (k < L && active) load_step(k, k);
+
+  for (int tb = 0; tb < L; tb += P) {
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+      const int t = tb + k;
+      if (t >= L) break;
+      // exact halo values of the previous row from the neighbour tiles
+      if (has_nb && t > 0 && t % S == 0) {
+        wait_neighbours(a.flag_base + (unsigned)(t / S));
+        if (halo) {
+          const long long so = pos(t - 1) * a.ws_str + woff;
+          float *pr = dring + ((t - 1) % SR) * M * rowf + cb;
+#pragma unroll
+          for (int m = 0; m < M; m++)
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              if (halo & (1u << i)) pr[m * rowf + i] = __ldcg(a.ddst[m] + so + i * a.wst2);
+        }
+        __syncthreads();
+      }
+      if (active) {
+        float4 out[M];
+        if (t == 0) {
+#pragma unroll
+          for (int m = 0; m < M; m++) out[m] = rd[k][m];
+        } else {
+          const float *dp0 = dring + ((t - 1) % SR) * M * rowf;
+          const float *ip0 = iring + ((t - 1) & 1) * NCH * rowf;
+          float best[M][4];
+#pragma unroll
+          for (int m = 0; m < M; m++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) best[m][i] = f4get(rd[k][m], i);
+#pragma unroll
+          for (int r = 0; r < NR; r++) {
+            const int d1 = CROSS == 2 ? r - 1 : 0;
+            const int pc = cb + d1 * B2;
+            float ip[NCHR][6];
+#pragma unroll
+            for (int c = 0; c < NCH; c++) {
+              if (c < C) {
+                const float *q = ip0 + c * rowf + pc;
+                float4 v = *reinterpret_cast<const float4 *>(q);
+                ip[c][0] = q[-1], ip[c][1] = v.x, ip[c][2] = v.y, ip[c][3] = v.z, ip[c][4] = v.w, ip[c][5] = q[4];
+              }
+            }
+            float dp[M][6];
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+              const float *q = dp0 + m * rowf + pc;
+              float4 v = *reinterpret_cast<const float4 *>(q);
+              dp[m][0] = q[-1], dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = q[4];
+            }
+#pragma unroll
+            for (int d2 = -1; d2 <= 1; d2++) {
+              const int n = CROSS == 2 ? (d1 + 1) * 3 + (d2 + 1) : d2 + 1;
+#pragma unroll
+              for (int i = 0; i < 4; i++) {
+                float l1 = 0.0f;
+                if (USE_IMG) {
+                  if (CT == 1) {
+                    l1 = fabsf(__fsub_rn(f4get(ri[k][0], i), ip[0][i + 1 + d2]));
+                  } else {
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                      if (c < C) l1 = __fadd_rn(l1, fabsf(__fsub_rn(f4get(ri[k][c], i), ip[c][i + 1 + d2])));
+                  }
+                }
+#pragma unroll
+                for (int m = 0; m < M; m++) {
+                  float cand;
+                  if (MODE == MODE_GENERAL)
+                    cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], l1));
+                  else if (MODE == MODE_EUCLID)
+                    cand = __fadd_rn(dp[m][i + 1 + d2], a.e[m][n]);
+                  else
+                    cand = __fadd_rn(dp[m][i + 1 + d2], l1);
+                  best[m][i] = fminf(best[m][i], cand);
+                }
+              }
+            }
+          }
+#pragma unroll
+          for (int m = 0; m < M; m++) {
+            // cells outside the image or the region stay NaN
+            out[m].x = (valid & 1u) ? best[m][0] : qnan;
+            out[m].y = (valid & 2u) ? best[m][1] : qnan;
+            out[m].z = (valid & 4u) ? best[m][2] : qnan;
+            out[m].w = (valid & 8u) ? best[m][3] : qnan;
+          }
+        }
+        float *dc = dring + (t % SR) * M * rowf + cb;
+#pragma unroll
+        for (int m = 0; m < M; m++) *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
+        float *ic = iring + (t & 1) * NCH * rowf + cb;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+          if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = ri[k][c];
+        if (!WT && t > 0 && own) {
+          const long long so = pos(t) * a.ws_str + woff;
+#pragma unroll
+          for (int m = 0; m < M; m++) {
+            if (own == 0xFu && a.vec) {
+              *reinterpret_cast<float4 *>(a.ddst[m] + so) = out[m];
+            } else {
+#pragma unroll
+              for (int i = 0; i < 4; i++)
+                if (own & (1u << i)) a.ddst[m][so + i * a.wst2] = f4get(out[m], i);
+            }
+          }
+        }
+        if (t + P < L) load_step(t + P, k);
+      }
+      __syncthreads();
+      const bool chunk_end = (t + 1) % S == 0 || t == L - 1;
+      if (WT && chunk_end) {
+        // transposed write-back of the chunk's own cells: S consecutive
+        // positions of one cell are contiguous in the write layout
+        const int t0 = t - t % S, Sn = t - t0 + 1;
+        const int cpw = 32 / S, j = lane % S;
+        if (j < Sn) {
+          const long long so = pos(t0 + j) * a.ws_str;
+          const float *src = dring + j * M * rowf;
+#pragma unroll
+          for (int m = 0; m < M; m++)
+            for (int i = warp * cpw + lane / S; i < nown; i += nwarps * cpw) {
+              int2 e = otab[i];
+              a.ddst[m][so + e.y] = src[m * rowf + e.x];
+            }
+        }
+        __syncthreads();
+      }
+      if (has_nb && chunk_end && tid == 0) {
+        __threadfence();
+        st_release(a.flags + tile, a.flag_base + (unsigned)(t / S) + 1u);
+      }
+    }
+  }
+}
+
+template <int CROSS, int CT, int M, int MODE, bool WT>
+int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
+  auto fn = fg_pass_kernel<CROSS, CT, M, MODE, WT>;
+  static unsigned long long configured = 0;  // bit per device (set under the engine's launch lock)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 64 && !(configured & (1ull << dev))) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+    configured |= 1ull << dev;
+  }
+  void *args[] = {const_cast<PassArgs *>(&a)};
+  if (c.tiles > 1)
+    e = cudaLaunchCooperativeKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
+  else
+    e = cudaLaunchKernel((const void *)fn, dim3(1), dim3(c.threads), args, c.smem, s);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  return FG_OK;
+}
+
+template <int CROSS, int M, bool WT>
+int launch_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStream_t s) {
+  const bool one = a.C == 1;
+  if (mode == MODE_EUCLID) return launch_variant<CROSS, 1, M, MODE_EUCLID, WT>(a, c, s);
+  if (mode == MODE_GEO)
+    return one ? launch_variant<CROSS, 1, M, MODE_GEO, WT>(a, c, s) : launch_variant<CROSS, 0, M, MODE_GEO, WT>(a, c, s);
+  return one ? launch_variant<CROSS, 1, M, MODE_GENERAL, WT>(a, c, s)
+             : launch_variant<CROSS, 0, M, MODE_GENERAL, WT>(a, c, s);
+}
+
+template <int CROSS>
+int launch_cross(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
+  if (M == 1) return wt ? launch_mode<CROSS, 1, true>(a, c, mode, s) : launch_mode<CROSS, 1, false>(a, c, mode, s);
+  if (M == 2) return wt ? launch_mode<CROSS, 2, true>(a, c, mode, s) : launch_mode<CROSS, 2, false>(a, c, mode, s);
+  return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
+}
+
+}  // namespace fgi
