@@ -29,7 +29,7 @@ EXPORTED = (
     "fg_workspace_bytes", "fg_workspace_status",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
-    "fg_GSF2d", "fg_GSF3d",
+    "fg_GSF2d", "fg_GSF3d", "fg_generalised_geodesic2d_noalloc",
 )
 
 _lib = None
@@ -68,6 +68,7 @@ def load():
     L.fg_generalised_geodesic3d.argtypes = [vp, i, i, i, i, vp, i, fp, vp, f, f, f, i, vp, sz, vp]
     L.fg_signed_generalised_geodesic3d.argtypes = L.fg_generalised_geodesic3d.argtypes
     L.fg_GSF2d.argtypes = [vp, i, i, i, vp, i, f, f, f, i, vp, vp, sz, vp]
+    L.fg_generalised_geodesic2d_noalloc.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp]
     L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
     for name in EXPORTED:
         if name not in ("fg_last_error",):

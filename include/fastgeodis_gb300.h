@@ -128,6 +128,25 @@ FG_API int fg_GSF3d(const float *image, int C, int D, int H, int W, const float 
              int iterations, float *out, void *workspace,
              size_t workspace_bytes, void *stream);
 
+/* Allocation-free variant of fg_generalised_geodesic2d (no counterpart in
+ * the reference).  For callers that cannot allocate device memory when they
+ * need the transform -- code running inside a framework that owns the
+ * allocator and forbids allocation during execution, or C callers without a
+ * device allocator.  It takes no workspace: its scratch is a fixed 16 MiB
+ * device array inside this library, held by every GPU that loads the library
+ * until the process exits.  Limit: (C + 1) * H * W * 4 bytes plus about 9 KiB
+ * must fit in 16 MiB (for example C = 1 up to about 2 million pixels);
+ * larger sizes return FG_ERR_UNSUPPORTED.  All calls share the array: calls
+ * whose GPU work overlaps race and give wrong results, so order them on one
+ * stream.  The first call on a device looks up the array's address there
+ * and should come before any stream capture.  Allocates nothing (no
+ * cudaMalloc / cudaFree); results are bit-identical to
+ * fg_generalised_geodesic2d. */
+FG_API int fg_generalised_geodesic2d_noalloc(const float *image, int C, int H, int W,
+                                             const float *mask, int Cm, float *out, float v,
+                                             float l_grad, float l_eucl, int iterations,
+                                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif
