@@ -615,13 +615,16 @@ namespace fgi {
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2o, int *rowfo,
                        int *nown_max) {
   const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
+  const int depth = (nch + M <= 2) ? 8 : ((nch + M <= 4) ? 4 : 2);  // pass_depth in fg_pass.cuh
   const int B1 = cross == 2 ? R1 + 2 : 1, B2 = ((R2 + 3) & ~3) + 8;
   const int rowf = (B1 * B2 + 3) & ~3;
   const int SR = wt ? S : 2;
+  const int nt = std::max(32, (R1 * ((R2 + 3) / 4) + 31) / 32 * 32);
   *B2o = B2;
   *rowfo = rowf;
   *nown_max = R1 * R2;
-  return (size_t)(SR * M + 2 * nch) * rowf * 4 + (wt ? (size_t)R1 * R2 * 8 : 0) + 64;
+  return (size_t)(SR * M + 2 * nch) * rowf * 4 + (size_t)depth * (M + nch) * nt * 16 +
+         (wt ? (size_t)R1 * R2 * 8 : 0) + 64;
 }
 
 }  // namespace fgi

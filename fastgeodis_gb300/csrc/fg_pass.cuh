@@ -75,27 +75,42 @@ __device__ __forceinline__ void f4set(float4 &v, int i, float x) {
   else v.w = x;
 }
 
-// channels held in registers and the prefetch depth of a kernel variant
+// channels staged per step and the prefetch depth (steps) of a kernel variant
 __host__ __device__ constexpr int pass_nch(int ct, int mode) {
   return mode == MODE_EUCLID ? 0 : (ct == 0 ? kMaxChannels : ct);
 }
 __host__ __device__ constexpr int pass_depth(int nch, int m) { return (nch + m <= 2) ? 8 : ((nch + m <= 4) ? 4 : 2); }
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 template <int CROSS, int CT, int M, int MODE, bool WT>
 __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) {
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
-  constexpr int P = pass_depth(NCH, M);
-  constexpr int A1 = CROSS == 2 ? 1 : 0;  // apron row above the region
-  constexpr int NR = CROSS == 2 ? 3 : 1;  // stencil rows
+  constexpr int P = pass_depth(NCH, M);  // steps of own inputs in flight (power of 2)
+  constexpr int AR = M + NCH;            // arrays staged per step
+  constexpr int A1 = CROSS == 2 ? 1 : 0; // apron row above the region
+  constexpr int NR = CROSS == 2 ? 3 : 1; // stencil rows
   extern __shared__ __align__(16) float sm[];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NT = blockDim.x, nwarps = NT >> 5;
   const int C = USE_IMG ? (CT == 0 ? a.C : CT) : 0;
-  const int L = a.L, S = a.S;
-  const int SR = WT ? S : 2;  // distance rows kept in shared memory
+  const int L = a.L, S = a.S, lgS = __ffs(S) - 1;  // S is a power of two
+  const int SR = WT ? S : 2;                        // distance rows kept in shared memory
   const int tile = blockIdx.x;
   const int ti1 = tile / a.tiles2, ti2 = tile - ti1 * a.tiles2;
   const int R1 = CROSS == 2 ? a.T1 + 2 * a.K1 : 1, R2 = a.T2 + 2 * a.K2;
@@ -106,12 +121,13 @@ __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) 
   const int o2lo = a.K2, o2hi = a.K2 + min(a.T2, a.N2 - ti2 * a.T2);
   const float qnan = __int_as_float(0x7fffffff);
 
-  float *dring = sm;                   // [SR][M][rowf] distances of the last SR steps
-  float *iring = sm + SR * M * rowf;   // [2][NCH][rowf] image values of the last two steps
-  int2 *otab = reinterpret_cast<int2 *>(iring + 2 * NCH * rowf);  // own cells (transposed flush)
+  float *dring = sm;                                            // [SR][M][rowf] distances, last SR steps
+  float *iring = sm + SR * M * rowf;                            // [2][NCH][rowf] image values, last 2 steps
+  float4 *oring = reinterpret_cast<float4 *>(iring + 2 * NCH * rowf);  // [P][AR][NT] own inputs in flight
+  int2 *otab = reinterpret_cast<int2 *>(oring + P * AR * NT);  // own cells (transposed flush)
 
   // --- set-up ---
-  for (int i = tid; i < (SR * M + 2 * NCH) * rowf; i += NT) sm[i] = qnan;
+  for (int i = tid; i < (SR * M + 2 * NCH) * rowf + P * AR * NT * 4; i += NT) sm[i] = qnan;
   int nown = 0;
   if (WT) {
     const int O1 = o1hi - o1lo, O2 = o2hi - o2lo;
@@ -139,8 +155,6 @@ __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) 
   const bool active = valid != 0;
   const bool full = valid == 0xFu && a.vec;
   const unsigned halo = valid & ~own;
-  const long long roff = (long long)g1 * a.st1 + g20;                             // read layout
-  const long long woff = (long long)g1 * a.wst1 + (long long)g20 * a.wst2;       // write layout
   int nbr = -1;  // neighbour tile polled by this thread
   if (tid < 8) {
     int d1, d2;
@@ -158,36 +172,39 @@ __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) 
   const bool has_nb = a.tiles1 * a.tiles2 > 1;
   __syncthreads();
 
-  auto pos = [&](int t) -> long long { return a.dir > 0 ? (long long)t : (long long)(L - 1 - t); };
+  // running offsets: read layout of the next step to prefetch, write layout of the current step
+  const long long rstep = a.dir > 0 ? a.s_str : -a.s_str;
+  const long long wstep = a.dir > 0 ? a.ws_str : -a.ws_str;
+  const long long r0 = (a.dir > 0 ? 0 : (long long)(L - 1) * a.s_str) + (long long)g1 * a.st1 + g20;
+  const long long w0 = (a.dir > 0 ? 0 : (long long)(L - 1) * a.ws_str) + (long long)g1 * a.wst1 + (long long)g20 * a.wst2;
+  long long rnext = r0;  // read offset of the next step to stage
+  long long wcur = w0;   // write offset of the current step
 
-  float4 rd[P][M];
-  float4 ri[P][NCHR];
-  auto load_step = [&](int t, int k) {
-    const long long so = pos(t) * a.s_str + roff;
-    if (full) {
+  // stage the own inputs of the next step into ring slot `slot` (one commit group per step)
+  auto stage = [&](int slot) {
+    if (active) {
+      float4 *dst = oring + slot * AR * NT + tid;
+      if (full) {
 #pragma unroll
-      for (int m = 0; m < M; m++) rd[k][m] = ldg4_pinned(a.dsrc[m] + so);
+        for (int m = 0; m < M; m++) cp_async16(dst + m * NT, a.dsrc[m] + rnext);
 #pragma unroll
-      for (int c = 0; c < NCH; c++)
-        if (c < C) ri[k][c] = ldg4_nc_pinned(a.img + c * a.img_cs + so);
-    } else {
+        for (int c = 0; c < NCH; c++)
+          if (c < C) cp_async16(dst + (M + c) * NT, a.img + c * a.img_cs + rnext);
+      } else {
 #pragma unroll
-      for (int m = 0; m < M; m++) {
-        rd[k][m] = make_float4(qnan, qnan, qnan, qnan);
+        for (int i = 0; i < 4; i++) {
+          if (valid & (1u << i)) {
 #pragma unroll
-        for (int i = 0; i < 4; i++)
-          if (valid & (1u << i)) f4set(rd[k][m], i, ldg_pinned(a.dsrc[m] + so + i));
-      }
+            for (int m = 0; m < M; m++) cp_async4(reinterpret_cast<float *>(dst + m * NT) + i, a.dsrc[m] + rnext + i);
 #pragma unroll
-      for (int c = 0; c < NCH; c++) {
-        ri[k][c] = make_float4(qnan, qnan, qnan, qnan);
-        if (c < C) {
-#pragma unroll
-          for (int i = 0; i < 4; i++)
-            if (valid & (1u << i)) f4set(ri[k][c], i, ldg_nc_pinned(a.img + c * a.img_cs + so + i));
+            for (int c = 0; c < NCH; c++)
+              if (c < C) cp_async4(reinterpret_cast<float *>(dst + (M + c) * NT) + i, a.img + c * a.img_cs + rnext + i);
+          }
         }
       }
     }
+    cp_async_commit();
+    rnext += rstep;
   };
 
   auto wait_neighbours = [&](unsigned target) {
@@ -205,146 +222,154 @@ __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) 
   };
 
 #pragma unroll
-  for (int k = 0; k < P; k++)
-    if (k < L && active) load_step(k, k);
+  for (int k = 0; k < P; k++) {
+    if (k < L) stage(k);
+    else cp_async_commit();
+  }
 
-  for (int tb = 0; tb < L; tb += P) {
+  for (int t = 0; t < L; t++) {
+    const int slot = t & (P - 1);
+    // exact halo values of the previous row from the neighbour tiles
+    if (has_nb && t > 0 && (t & (S - 1)) == 0) {
+      wait_neighbours(a.flag_base + (unsigned)(t >> lgS));
+      if (halo) {
+        const long long so = wcur - wstep;  // write offset of step t-1
+        float *pr = dring + ((t - 1) & (SR - 1)) * M * rowf + cb;
 #pragma unroll
-    for (int k = 0; k < P; k++) {
-      const int t = tb + k;
-      if (t >= L) break;
-      // exact halo values of the previous row from the neighbour tiles
-      if (has_nb && t > 0 && t % S == 0) {
-        wait_neighbours(a.flag_base + (unsigned)(t / S));
-        if (halo) {
-          const long long so = pos(t - 1) * a.ws_str + woff;
-          float *pr = dring + ((t - 1) % SR) * M * rowf + cb;
+        for (int m = 0; m < M; m++)
 #pragma unroll
-          for (int m = 0; m < M; m++)
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-              if (halo & (1u << i)) pr[m * rowf + i] = __ldcg(a.ddst[m] + so + i * a.wst2);
-        }
-        __syncthreads();
-      }
-      if (active) {
-        float4 out[M];
-        if (t == 0) {
-#pragma unroll
-          for (int m = 0; m < M; m++) out[m] = rd[k][m];
-        } else {
-          const float *dp0 = dring + ((t - 1) % SR) * M * rowf;
-          const float *ip0 = iring + ((t - 1) & 1) * NCH * rowf;
-          float best[M][4];
-#pragma unroll
-          for (int m = 0; m < M; m++)
-#pragma unroll
-            for (int i = 0; i < 4; i++) best[m][i] = f4get(rd[k][m], i);
-#pragma unroll
-          for (int r = 0; r < NR; r++) {
-            const int d1 = CROSS == 2 ? r - 1 : 0;
-            const int pc = cb + d1 * B2;
-            float ip[NCHR][6];
-#pragma unroll
-            for (int c = 0; c < NCH; c++) {
-              if (c < C) {
-                const float *q = ip0 + c * rowf + pc;
-                float4 v = *reinterpret_cast<const float4 *>(q);
-                ip[c][0] = q[-1], ip[c][1] = v.x, ip[c][2] = v.y, ip[c][3] = v.z, ip[c][4] = v.w, ip[c][5] = q[4];
-              }
-            }
-            float dp[M][6];
-#pragma unroll
-            for (int m = 0; m < M; m++) {
-              const float *q = dp0 + m * rowf + pc;
-              float4 v = *reinterpret_cast<const float4 *>(q);
-              dp[m][0] = q[-1], dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = q[4];
-            }
-#pragma unroll
-            for (int d2 = -1; d2 <= 1; d2++) {
-              const int n = CROSS == 2 ? (d1 + 1) * 3 + (d2 + 1) : d2 + 1;
-#pragma unroll
-              for (int i = 0; i < 4; i++) {
-                float l1 = 0.0f;
-                if (USE_IMG) {
-                  if (CT == 1) {
-                    l1 = fabsf(__fsub_rn(f4get(ri[k][0], i), ip[0][i + 1 + d2]));
-                  } else {
-#pragma unroll
-                    for (int c = 0; c < NCH; c++)
-                      if (c < C) l1 = __fadd_rn(l1, fabsf(__fsub_rn(f4get(ri[k][c], i), ip[c][i + 1 + d2])));
-                  }
-                }
-#pragma unroll
-                for (int m = 0; m < M; m++) {
-                  float cand;
-                  if (MODE == MODE_GENERAL)
-                    cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], l1));
-                  else if (MODE == MODE_EUCLID)
-                    cand = __fadd_rn(dp[m][i + 1 + d2], a.e[m][n]);
-                  else
-                    cand = __fadd_rn(dp[m][i + 1 + d2], l1);
-                  best[m][i] = fminf(best[m][i], cand);
-                }
-              }
-            }
-          }
-#pragma unroll
-          for (int m = 0; m < M; m++) {
-            // cells outside the image or the region stay NaN
-            out[m].x = (valid & 1u) ? best[m][0] : qnan;
-            out[m].y = (valid & 2u) ? best[m][1] : qnan;
-            out[m].z = (valid & 4u) ? best[m][2] : qnan;
-            out[m].w = (valid & 8u) ? best[m][3] : qnan;
-          }
-        }
-        float *dc = dring + (t % SR) * M * rowf + cb;
-#pragma unroll
-        for (int m = 0; m < M; m++) *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
-        float *ic = iring + (t & 1) * NCH * rowf + cb;
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-          if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = ri[k][c];
-        if (!WT && t > 0 && own) {
-          const long long so = pos(t) * a.ws_str + woff;
-#pragma unroll
-          for (int m = 0; m < M; m++) {
-            if (own == 0xFu && a.vec) {
-              *reinterpret_cast<float4 *>(a.ddst[m] + so) = out[m];
-            } else {
-#pragma unroll
-              for (int i = 0; i < 4; i++)
-                if (own & (1u << i)) a.ddst[m][so + i * a.wst2] = f4get(out[m], i);
-            }
-          }
-        }
-        if (t + P < L) load_step(t + P, k);
+          for (int i = 0; i < 4; i++)
+            if (halo & (1u << i)) pr[m * rowf + i] = __ldcg(a.ddst[m] + so + i * a.wst2);
       }
       __syncthreads();
-      const bool chunk_end = (t + 1) % S == 0 || t == L - 1;
-      if (WT && chunk_end) {
-        // transposed write-back of the chunk's own cells: S consecutive
-        // positions of one cell are contiguous in the write layout
-        const int t0 = t - t % S, Sn = t - t0 + 1;
-        const int cpw = 32 / S, j = lane % S;
-        if (j < Sn) {
-          const long long so = pos(t0 + j) * a.ws_str;
-          const float *src = dring + j * M * rowf;
+    }
+    cp_async_wait<P - 1>();  // this thread's inputs of step t have landed
+    if (active) {
+      const float4 *mine = oring + slot * AR * NT + tid;
+      float4 dold[M], icur[NCHR];
 #pragma unroll
-          for (int m = 0; m < M; m++)
-            for (int i = warp * cpw + lane / S; i < nown; i += nwarps * cpw) {
-              int2 e = otab[i];
-              a.ddst[m][so + e.y] = src[m * rowf + e.x];
+      for (int m = 0; m < M; m++) dold[m] = mine[m * NT];
+#pragma unroll
+      for (int c = 0; c < NCH; c++) icur[c] = mine[(M + c) * NT];
+      float4 out[M];
+      if (t == 0) {
+#pragma unroll
+        for (int m = 0; m < M; m++) out[m] = dold[m];
+      } else {
+        const float *dp0 = dring + ((t - 1) & (SR - 1)) * M * rowf;
+        const float *ip0 = iring + ((t - 1) & 1) * NCH * rowf;
+        float best[M][4];
+#pragma unroll
+        for (int m = 0; m < M; m++)
+#pragma unroll
+          for (int i = 0; i < 4; i++) best[m][i] = f4get(dold[m], i);
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+          const int d1 = CROSS == 2 ? r - 1 : 0;
+          const int pc = cb + d1 * B2;
+          float ip[NCHR][6];
+#pragma unroll
+          for (int c = 0; c < NCH; c++) {
+            if (c < C) {
+              const float *q = ip0 + c * rowf + pc;
+              float4 v = *reinterpret_cast<const float4 *>(q);
+              ip[c][0] = q[-1], ip[c][1] = v.x, ip[c][2] = v.y, ip[c][3] = v.z, ip[c][4] = v.w, ip[c][5] = q[4];
             }
+          }
+          float dp[M][6];
+#pragma unroll
+          for (int m = 0; m < M; m++) {
+            const float *q = dp0 + m * rowf + pc;
+            float4 v = *reinterpret_cast<const float4 *>(q);
+            dp[m][0] = q[-1], dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = q[4];
+          }
+#pragma unroll
+          for (int d2 = -1; d2 <= 1; d2++) {
+            const int n = CROSS == 2 ? (d1 + 1) * 3 + (d2 + 1) : d2 + 1;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+              float l1 = 0.0f;
+              if (USE_IMG) {
+                if (CT == 1) {
+                  l1 = fabsf(__fsub_rn(f4get(icur[0], i), ip[0][i + 1 + d2]));
+                } else {
+#pragma unroll
+                  for (int c = 0; c < NCH; c++)
+                    if (c < C) l1 = __fadd_rn(l1, fabsf(__fsub_rn(f4get(icur[c], i), ip[c][i + 1 + d2])));
+                }
+              }
+#pragma unroll
+              for (int m = 0; m < M; m++) {
+                float cand;
+                if (MODE == MODE_GENERAL)
+                  cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], l1));
+                else if (MODE == MODE_EUCLID)
+                  cand = __fadd_rn(dp[m][i + 1 + d2], a.e[m][n]);
+                else
+                  cand = __fadd_rn(dp[m][i + 1 + d2], l1);
+                best[m][i] = fminf(best[m][i], cand);
+              }
+            }
+          }
         }
-        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+          // cells outside the image or the region stay NaN
+          out[m].x = (valid & 1u) ? best[m][0] : qnan;
+          out[m].y = (valid & 2u) ? best[m][1] : qnan;
+          out[m].z = (valid & 4u) ? best[m][2] : qnan;
+          out[m].w = (valid & 8u) ? best[m][3] : qnan;
+        }
       }
-      if (has_nb && chunk_end && tid == 0) {
-        __threadfence();
-        st_release(a.flags + tile, a.flag_base + (unsigned)(t / S) + 1u);
+      float *dc = dring + (t & (SR - 1)) * M * rowf + cb;
+#pragma unroll
+      for (int m = 0; m < M; m++) *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
+      float *ic = iring + (t & 1) * NCH * rowf + cb;
+#pragma unroll
+      for (int c = 0; c < NCH; c++)
+        if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = icur[c];
+      if (!WT && t > 0 && own) {
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+          if (own == 0xFu && a.vec) {
+            *reinterpret_cast<float4 *>(a.ddst[m] + wcur) = out[m];
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              if (own & (1u << i)) a.ddst[m][wcur + i * a.wst2] = f4get(out[m], i);
+          }
+        }
       }
     }
+    // the slot's values are consumed (they are in registers): refill it with step t+P
+    if (t + P < L) stage(slot);
+    else cp_async_commit();
+    wcur += wstep;
+    __syncthreads();
+    const bool chunk_end = ((t + 1) & (S - 1)) == 0 || t == L - 1;
+    if (WT && chunk_end) {
+      // transposed write-back of the chunk's own cells: S consecutive
+      // positions of one cell are contiguous in the write layout
+      const int t0 = t & ~(S - 1), Sn = t - t0 + 1;
+      const int cpw = 32 / S, j = lane & (S - 1);
+      if (j < Sn) {
+        const long long so = (a.dir > 0 ? (long long)(t0 + j) : (long long)(L - 1 - t0 - j)) * a.ws_str;
+        const float *src = dring + j * M * rowf;
+#pragma unroll
+        for (int m = 0; m < M; m++)
+          for (int i = warp * cpw + (lane >> lgS); i < nown; i += nwarps * cpw) {
+            int2 e = otab[i];
+            a.ddst[m][so + e.y] = src[m * rowf + e.x];
+          }
+      }
+      __syncthreads();
+    }
+    if (has_nb && chunk_end && tid == 0) {
+      __threadfence();
+      st_release(a.flags + tile, a.flag_base + (unsigned)(t >> lgS) + 1u);
+    }
   }
+  cp_async_wait<0>();
 }
 
 template <int CROSS, int CT, int M, int MODE, bool WT>
