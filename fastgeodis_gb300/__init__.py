@@ -30,6 +30,9 @@ from . import _lib
 __version__ = "1.0.5"  # API level of the FastGeodis release this mirrors
 
 __all__ = [
+    "GeodesicBatch2d",
+    "generalised_geodesic2d_batch",
+    "signed_generalised_geodesic2d_batch",
     "generalised_geodesic2d",
     "generalised_geodesic3d",
     "signed_generalised_geodesic2d",
@@ -258,3 +261,6 @@ def GSF3d(image: torch.Tensor, softmask: torch.Tensor, theta: float, spacing: Li
           iter: int):
     r"""Geodesic symmetric filtering of a 3D soft mask."""
     return _run("gsf3d", image, softmask, v, lamb, iter, spacing=spacing, theta=theta)
+
+
+from .batch import GeodesicBatch2d, generalised_geodesic2d_batch, signed_generalised_geodesic2d_batch  # noqa: E402

@@ -29,7 +29,8 @@ EXPORTED = (
     "fg_workspace_bytes", "fg_workspace_status",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
-    "fg_GSF2d", "fg_GSF3d", "fg_generalised_geodesic2d_noalloc",
+    "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
+    "fg_generalised_geodesic2d_noalloc",
 )
 
 _lib = None
@@ -69,6 +70,9 @@ def load():
     L.fg_signed_generalised_geodesic3d.argtypes = L.fg_generalised_geodesic3d.argtypes
     L.fg_GSF2d.argtypes = [vp, i, i, i, vp, i, f, f, f, i, vp, vp, sz, vp]
     L.fg_generalised_geodesic2d_noalloc.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp]
+    L.fg_batch2d_smem_bytes.argtypes = [i, i, i]
+    L.fg_batch2d_smem_bytes.restype = sz
+    L.fg_batch_geodesic2d.argtypes = [vp, i, i, i, i, i, vp, vp, vp]
     L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
     for name in EXPORTED:
         if name not in ("fg_last_error",):

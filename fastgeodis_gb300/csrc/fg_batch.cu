@@ -1,0 +1,198 @@
+// Batched 2D transforms: many images of uneven size (and channel count) in
+// one persistent launch.
+//
+// Each CTA repeatedly claims the next image from a work queue (an atomic
+// counter; the caller orders the images largest first) and runs that image's
+// whole transform by itself: transposed image copy, initial distances, every
+// pass of every iteration (through pass_body, one tile covering the whole
+// cross-section), and for the signed form the final subtraction.  No CTA
+// ever waits for another, so any number of images and any grid size is safe,
+// and the launch can be captured in a CUDA graph (memset of the counter +
+// one kernel).  Each image's arithmetic is exactly that of the per-call path:
+// results are bit-identical, alone or in a batch.
+
+#include <math.h>
+
+#include <algorithm>
+
+#include "fg_pass.cuh"
+
+namespace fgi {
+namespace {
+
+constexpr int kBatchS = 8;  // steps per transposed flush
+
+__device__ void batch_prologue(const fg_batch2d_item &it, bool is_signed, float *sm) {
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
+  const int H = it.H, W = it.W;
+  const long long P = (long long)H * W;
+  // image [C][H][W] -> [C][W][H], 32x32 tiles through shared memory, one per warp
+  float *tb = sm + warp * 32 * 33;
+  const int th = (H + 31) / 32, tw = (W + 31) / 32;
+  for (int job = warp; job < it.C * th * tw; job += nwarps) {
+    const int c = job / (th * tw), r = job - c * th * tw, h0 = (r / tw) * 32, w0 = (r % tw) * 32;
+    const float *src = it.image + c * P;
+    float *dst = it.image_t + c * P;
+    for (int y = 0; y < 32; y++) {
+      int h = h0 + y, w = w0 + lane;
+      if (h < H && w < W) tb[y * 33 + lane] = src[(long long)h * W + w];
+    }
+    __syncwarp();
+    for (int y = 0; y < 32; y++) {
+      int w = w0 + y, h = h0 + lane;
+      if (h < H && w < W) dst[(long long)w * H + h] = tb[lane * 33 + y];
+    }
+    __syncwarp();
+  }
+  // initial distances v*M (and v*(1-M) for the signed form)
+  for (long long i = tid; i < P; i += NT) {
+    const float m = it.mask[i];
+    it.out[i] = __fmul_rn(it.v, m);
+    if (is_signed) it.d2[i] = __fmul_rn(it.v, __fsub_rn(1.0f, m));
+  }
+}
+
+// arguments of pass `k` (0: along H forward, 1: along H backward writing
+// [W][H], 2: along W forward, 3: along W backward writing [H][W])
+__device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, float r2, int *status, PassArgs *pa) {
+  PassArgs a;
+  const int H = it.H, W = it.W;
+  const bool alongW = k >= 2, back = (k & 1) != 0;
+  const long long P = (long long)H * W;
+  a.img = alongW ? it.image_t : it.image;
+  a.img_cs = P;
+  a.C = it.C;
+  float *r[2] = {it.out, it.d2}, *t[2] = {it.t1, it.t2};
+  const float ld[3] = {r2, 1.0f, r2};
+  for (int m = 0; m < kMaxMaps; m++) {
+    const int mm = m < M ? m : 0;
+    a.dsrc[m] = alongW ? t[mm] : r[mm];
+    a.ddst[m] = (k == 1) ? t[mm] : ((k == 3) ? r[mm] : const_cast<float *>(a.dsrc[m]));
+    a.lg[m] = it.l_grad;
+    for (int n = 0; n < 9; n++) a.e[m][n] = n < 3 ? __fmul_rn(it.l_eucl, ld[n]) : 0.0f;
+  }
+  a.L = alongW ? W : H;
+  a.dir = back ? -1 : 1;
+  a.s_str = alongW ? H : W;
+  a.st1 = 0;
+  const int N2 = alongW ? H : W;
+  if (k == 1) {
+    a.ws_str = 1, a.wst1 = 0, a.wst2 = H;
+  } else if (k == 3) {
+    a.ws_str = 1, a.wst1 = 0, a.wst2 = W;
+  } else {
+    a.ws_str = a.s_str, a.wst1 = 0, a.wst2 = 1;
+  }
+  a.N1 = 1;
+  a.N2 = N2;
+  a.T1 = 1, a.T2 = N2, a.K1 = 0, a.K2 = 0, a.tiles1 = 1, a.tiles2 = 1;
+  a.S = kBatchS;
+  a.B2 = ((N2 + 3) & ~3) + 8;
+  a.rowf = a.B2;
+  bool vec = (H % 4 == 0) && (W % 4 == 0);
+  const void *ptrs[6] = {a.img, it.out, it.t1, M > 1 ? it.d2 : it.out, M > 1 ? it.t2 : it.t1, it.image_t};
+  for (int i = 0; i < 6; i++) vec = vec && ((reinterpret_cast<uintptr_t>(ptrs[i]) & 15) == 0);
+  a.vec = vec ? 1 : 0;
+  a.flags = nullptr;
+  a.flag_base = 0;
+  a.status = status;
+  *pa = a;
+}
+
+template <int CT, int M>
+__global__ void __launch_bounds__(kThreads, 1)
+    fg_batch2d_kernel(const fg_batch2d_item *items, int n, int iterations, float r2, int *counter, int *status) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int s_item;
+  __shared__ PassArgs s_args;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int i = s_item;
+    if (i >= n) break;
+    const fg_batch2d_item it = items[i];
+    if ((long long)it.H * it.W > 0) {
+      batch_prologue(it, M == 2, sm);
+      __threadfence();
+      __syncthreads();
+      for (int iter = 0; iter < iterations; iter++) {
+        for (int k = 0; k < 4; k++) {
+          const int L = k >= 2 ? it.W : it.H;
+          const bool wt = k & 1;
+          if (L <= 1 && !wt) continue;
+          if (threadIdx.x == 0) batch_pass_args(it, M, k, r2, status, &s_args);
+          __syncthreads();
+          if (wt)
+            pass_body<1, CT, M, MODE_GENERAL, true>(s_args, 0, sm);
+          else
+            pass_body<1, CT, M, MODE_GENERAL, false>(s_args, 0, sm);
+          __threadfence();
+          __syncthreads();
+        }
+      }
+      if (M == 2) {
+        const long long P = (long long)it.H * it.W;
+        for (long long p = threadIdx.x; p < P; p += blockDim.x) it.out[p] = __fsub_rn(it.out[p], it.d2[p]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int CT, int M>
+int launch_batch(const fg_batch2d_item *items, int n, int iterations, int max_extent, int *counter, int *status,
+                 size_t smem, int grid, cudaStream_t s) {
+  auto fn = fg_batch2d_kernel<CT, M>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
+  fn<<<grid, kThreads, smem, s>>>(items, n, iterations, r2, counter, status);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  (void)max_extent;
+  return FG_OK;
+}
+
+}  // namespace
+}  // namespace fgi
+
+extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed) {
+  using namespace fgi;
+  if (max_C < 1 || max_extent < 1) return 0;
+  const int M = is_signed ? 2 : 1;
+  const int nch = pass_nch(max_C == 1 ? 1 : 0, MODE_GENERAL);
+  const int depth = pass_depth(nch, M);
+  const int rowf = ((max_extent + 3) & ~3) + 8;  // one row: 4-cell apron, runs of 4, apron
+  // the largest pass: a transposed-writing one (kBatchS distance rows) over the longest side
+  const size_t pass = (size_t)(kBatchS * M + 2 * nch) * rowf * 4 + (size_t)depth * (M + nch) * kThreads * 16 +
+                      (size_t)max_extent * 8 + 64;
+  const size_t transpose = (size_t)(kThreads / 32) * 32 * 33 * 4;
+  return std::max(pass, transpose);
+}
+
+extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
+                                          int is_signed, int iterations, int *counter, int *status, void *stream) {
+  using namespace fgi;
+  if (n < 0 || (n > 0 && (!items || !counter || !status)))
+    return set_error(FG_ERR_INVALID_ARGUMENT, "batch: null descriptor, counter or status pointer");
+  if (max_C < 1 || max_C > kMaxChannels)
+    return set_error(FG_ERR_UNSUPPORTED, "batch: images need 1 to 4 channels");
+  if (max_extent > 4 * kThreads)
+    return set_error(FG_ERR_UNSUPPORTED, "batch: image sides up to 2048 are supported (one CTA sweeps a whole row)");
+  if (n == 0) return FG_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = fg_batch2d_smem_bytes(max_C, max_extent, is_signed);
+  if (smem > 227 * 1024) return set_error(FG_ERR_UNSUPPORTED, "batch: shared memory plan too large");
+  const int grid = std::max(1, std::min(n, sms));
+  const int its = std::max(iterations, 0);
+  if (max_C == 1)
+    return is_signed ? launch_batch<1, 2>(items, n, its, max_extent, counter, status, smem, grid, s)
+                     : launch_batch<1, 1>(items, n, its, max_extent, counter, status, smem, grid, s);
+  return is_signed ? launch_batch<0, 2>(items, n, its, max_extent, counter, status, smem, grid, s)
+                   : launch_batch<0, 1>(items, n, its, max_extent, counter, status, smem, grid, s);
+}

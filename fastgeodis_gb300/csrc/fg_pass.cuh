@@ -95,8 +95,12 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// The body of one pass over tile `tile`, shared by the per-pass kernel and the
+// batched kernel.  `ar` may live in parameter or shared memory; it is copied
+// into registers first so the step loop never reloads its fields.
 template <int CROSS, int CT, int M, int MODE, bool WT>
-__global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) {
+__device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, float *sm) {
+  const PassArgs a = ar;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
@@ -104,14 +108,12 @@ __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) 
   constexpr int AR = M + NCH;            // arrays staged per step
   constexpr int A1 = CROSS == 2 ? 1 : 0; // apron row above the region
   constexpr int NR = CROSS == 2 ? 3 : 1; // stencil rows
-  extern __shared__ __align__(16) float sm[];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NT = blockDim.x, nwarps = NT >> 5;
   const int C = USE_IMG ? (CT == 0 ? a.C : CT) : 0;
   const int L = a.L, S = a.S, lgS = __ffs(S) - 1;  // S is a power of two
   const int SR = WT ? S : 2;                        // distance rows kept in shared memory
-  const int tile = blockIdx.x;
   const int ti1 = tile / a.tiles2, ti2 = tile - ti1 * a.tiles2;
   const int R1 = CROSS == 2 ? a.T1 + 2 * a.K1 : 1, R2 = a.T2 + 2 * a.K2;
   const int B2 = a.B2, rowf = a.rowf;
@@ -370,6 +372,12 @@ __global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) 
     }
   }
   cp_async_wait<0>();
+}
+
+template <int CROSS, int CT, int M, int MODE, bool WT>
+__global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  pass_body<CROSS, CT, M, MODE, WT>(a, blockIdx.x, sm);
 }
 
 template <int CROSS, int CT, int M, int MODE, bool WT>

@@ -128,6 +128,36 @@ FG_API int fg_GSF3d(const float *image, int C, int D, int H, int W, const float 
              int iterations, float *out, void *workspace,
              size_t workspace_bytes, void *stream);
 
+/* One image of a batched 2D transform (see fg_batch_geodesic2d).  All
+ * pointers are device pointers; float32, contiguous.  The scratch buffers
+ * belong to the caller and must not overlap between items. */
+typedef struct fg_batch2d_item {
+  const float *image; /* [C][H][W] */
+  const float *mask;  /* [H][W] soft mask (one channel) */
+  float *out;         /* [H][W] result: D(mask), or D(mask) - D(1 - mask) when signed */
+  float *image_t;     /* scratch [C][W][H] */
+  float *d2;          /* scratch [H][W] (signed only) */
+  float *t1;          /* scratch [W][H] */
+  float *t2;          /* scratch [W][H] (signed only) */
+  int C, H, W, reserved0;
+  float v, l_grad, l_eucl, reserved1;
+} fg_batch2d_item;
+
+/* Batched generalised_geodesic2d / signed_generalised_geodesic2d over n
+ * images of any sizes up to 2048 per side and 1-4 channels, in one
+ * persistent launch: each CTA takes the next image from a work queue and
+ * runs its whole transform (no counterpart in the reference, which takes one
+ * image per call; per image the results are bit-identical to
+ * fg_generalised_geodesic2d / fg_signed_generalised_geodesic2d).
+ * `items`: device array of n descriptors, ideally ordered largest first;
+ * max_C / max_extent: the largest channel count and side among them;
+ * `counter`, `status`: device ints (the counter is reset by the call).
+ * Capturable in a CUDA graph. */
+FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed);
+FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
+                               int is_signed, int iterations, int *counter, int *status,
+                               void *stream);
+
 /* Allocation-free variant of fg_generalised_geodesic2d (no counterpart in
  * the reference).  For callers that cannot allocate device memory when they
  * need the transform -- code running inside a framework that owns the
