@@ -20,7 +20,6 @@
 namespace fgi {
 namespace {
 
-constexpr int kBatchS = 8;  // steps per transposed flush
 
 __device__ void batch_prologue(const fg_batch2d_item &it, bool is_signed, float *sm) {
   const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
@@ -54,7 +53,8 @@ __device__ void batch_prologue(const fg_batch2d_item &it, bool is_signed, float 
 
 // arguments of pass `k` (0: along H forward, 1: along H backward writing
 // [W][H], 2: along W forward, 3: along W backward writing [H][W])
-__device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, float r2, int *status, PassArgs *pa) {
+__device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, float r2, int *status,
+                                PassArgs *pa) {
   PassArgs a;
   const int H = it.H, W = it.W;
   const bool alongW = k >= 2, back = (k & 1) != 0;
@@ -86,7 +86,7 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, float r
   a.N1 = 1;
   a.N2 = N2;
   a.T1 = 1, a.T2 = N2, a.K1 = 0, a.K2 = 0, a.tiles1 = 1, a.tiles2 = 1;
-  a.S = kBatchS;
+  a.S = S;
   a.B2 = ((N2 + 3) & ~3) + 8;
   a.rowf = a.B2;
   bool vec = (H % 4 == 0) && (W % 4 == 0);
@@ -101,7 +101,8 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, float r
 
 template <int CT, int M>
 __global__ void __launch_bounds__(kThreads, 1)
-    fg_batch2d_kernel(const fg_batch2d_item *items, int n, int iterations, float r2, int *counter, int *status) {
+    fg_batch2d_kernel(const fg_batch2d_item *items, int n, int iterations, int S, float r2, int *counter,
+                      int *status) {
   extern __shared__ __align__(16) float sm[];
   __shared__ int s_item;
   __shared__ PassArgs s_args;
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int L = k >= 2 ? it.W : it.H;
           const bool wt = k & 1;
           if (L <= 1 && !wt) continue;
-          if (threadIdx.x == 0) batch_pass_args(it, M, k, r2, status, &s_args);
+          if (threadIdx.x == 0) batch_pass_args(it, M, k, S, r2, status, &s_args);
           __syncthreads();
           if (wt)
             pass_body<1, CT, M, MODE_GENERAL, true>(s_args, 0, sm);
@@ -140,34 +141,45 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 template <int CT, int M>
-int launch_batch(const fg_batch2d_item *items, int n, int iterations, int max_extent, int *counter, int *status,
+int launch_batch(const fg_batch2d_item *items, int n, int iterations, int S, int *counter, int *status,
                  size_t smem, int grid, cudaStream_t s) {
   auto fn = fg_batch2d_kernel<CT, M>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
-  fn<<<grid, kThreads, smem, s>>>(items, n, iterations, r2, counter, status);
+  fn<<<grid, kThreads, smem, s>>>(items, n, iterations, S, r2, counter, status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  (void)max_extent;
   return FG_OK;
 }
 
 }  // namespace
 }  // namespace fgi
 
-extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed) {
-  using namespace fgi;
-  if (max_C < 1 || max_extent < 1) return 0;
+namespace fgi {
+namespace {
+// shared memory of the batched kernel with S steps per transposed flush
+size_t batch_smem(int max_C, int max_extent, int is_signed, int S) {
   const int M = is_signed ? 2 : 1;
   const int nch = pass_nch(max_C == 1 ? 1 : 0, MODE_GENERAL);
   const int depth = pass_depth(nch, M);
   const int rowf = ((max_extent + 3) & ~3) + 8;  // one row: 4-cell apron, runs of 4, apron
-  // the largest pass: a transposed-writing one (kBatchS distance rows) over the longest side
-  const size_t pass = (size_t)(kBatchS * M + 2 * nch) * rowf * 4 + (size_t)depth * (M + nch) * kThreads * 16 +
+  // the largest pass: a transposed-writing one (S distance rows) over the longest side
+  const size_t pass = (size_t)(S * M + 2 * max_C) * rowf * 4 + (size_t)depth * (M + max_C) * kThreads * 16 +
                       (size_t)max_extent * 8 + 64;
   const size_t transpose = (size_t)(kThreads / 32) * 32 * 33 * 4;
   return std::max(pass, transpose);
+}
+constexpr size_t kBatchSmemLimit = 227 * 1024;
+int batch_flush_steps(int max_C, int max_extent, int is_signed) {
+  return batch_smem(max_C, max_extent, is_signed, 8) <= kBatchSmemLimit ? 8 : 4;
+}
+}  // namespace
+}  // namespace fgi
+
+extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed) {
+  if (max_C < 1 || max_extent < 1) return 0;
+  return fgi::batch_smem(max_C, max_extent, is_signed, fgi::batch_flush_steps(max_C, max_extent, is_signed));
 }
 
 extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
@@ -186,13 +198,14 @@ extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, i
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = fg_batch2d_smem_bytes(max_C, max_extent, is_signed);
-  if (smem > 227 * 1024) return set_error(FG_ERR_UNSUPPORTED, "batch: shared memory plan too large");
+  const int S = batch_flush_steps(max_C, max_extent, is_signed);
+  const size_t smem = batch_smem(max_C, max_extent, is_signed, S);
+  if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "batch: shared memory plan too large");
   const int grid = std::max(1, std::min(n, sms));
   const int its = std::max(iterations, 0);
   if (max_C == 1)
-    return is_signed ? launch_batch<1, 2>(items, n, its, max_extent, counter, status, smem, grid, s)
-                     : launch_batch<1, 1>(items, n, its, max_extent, counter, status, smem, grid, s);
-  return is_signed ? launch_batch<0, 2>(items, n, its, max_extent, counter, status, smem, grid, s)
-                   : launch_batch<0, 1>(items, n, its, max_extent, counter, status, smem, grid, s);
+    return is_signed ? launch_batch<1, 2>(items, n, its, S, counter, status, smem, grid, s)
+                     : launch_batch<1, 1>(items, n, its, S, counter, status, smem, grid, s);
+  return is_signed ? launch_batch<0, 2>(items, n, its, S, counter, status, smem, grid, s)
+                   : launch_batch<0, 1>(items, n, its, S, counter, status, smem, grid, s);
 }

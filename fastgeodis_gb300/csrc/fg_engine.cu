@@ -614,8 +614,9 @@ namespace fgi {
 
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2o, int *rowfo,
                        int *nown_max) {
-  const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
-  const int depth = (nch + M <= 2) ? 8 : ((nch + M <= 4) ? 4 : 2);  // pass_depth in fg_pass.cuh
+  const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);  // channels of the variant
+  const int depth = (nch + M <= 2) ? 8 : ((nch + M <= 4) ? 4 : 2);        // pass_depth in fg_pass.cuh
+  const int ci = mode == MODE_EUCLID ? 0 : C;                              // image arrays staged
   const int B1 = cross == 2 ? R1 + 2 : 1, B2 = ((R2 + 3) & ~3) + 8;
   const int rowf = (B1 * B2 + 3) & ~3;
   const int SR = wt ? S : 2;
@@ -623,7 +624,7 @@ size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1
   *B2o = B2;
   *rowfo = rowf;
   *nown_max = R1 * R2;
-  return (size_t)(SR * M + 2 * nch) * rowf * 4 + (size_t)depth * (M + nch) * nt * 16 +
+  return (size_t)(SR * M + 2 * ci) * rowf * 4 + (size_t)depth * (M + ci) * nt * 16 +
          (wt ? (size_t)R1 * R2 * 8 : 0) + 64;
 }
 

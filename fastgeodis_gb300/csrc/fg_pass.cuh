@@ -105,7 +105,6 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
   constexpr int P = pass_depth(NCH, M);  // steps of own inputs in flight (power of 2)
-  constexpr int AR = M + NCH;            // arrays staged per step
   constexpr int A1 = CROSS == 2 ? 1 : 0; // apron row above the region
   constexpr int NR = CROSS == 2 ? 3 : 1; // stencil rows
 
@@ -123,13 +122,14 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const int o2lo = a.K2, o2hi = a.K2 + min(a.T2, a.N2 - ti2 * a.T2);
   const float qnan = __int_as_float(0x7fffffff);
 
-  float *dring = sm;                                            // [SR][M][rowf] distances, last SR steps
-  float *iring = sm + SR * M * rowf;                            // [2][NCH][rowf] image values, last 2 steps
-  float4 *oring = reinterpret_cast<float4 *>(iring + 2 * NCH * rowf);  // [P][AR][NT] own inputs in flight
+  const int AR = M + C;                                        // arrays staged per step
+  float *dring = sm;                                           // [SR][M][rowf] distances, last SR steps
+  float *iring = sm + SR * M * rowf;                           // [2][C][rowf] image values, last 2 steps
+  float4 *oring = reinterpret_cast<float4 *>(iring + 2 * C * rowf);  // [P][AR][NT] own inputs in flight
   int2 *otab = reinterpret_cast<int2 *>(oring + P * AR * NT);  // own cells (transposed flush)
 
   // --- set-up ---
-  for (int i = tid; i < (SR * M + 2 * NCH) * rowf + P * AR * NT * 4; i += NT) sm[i] = qnan;
+  for (int i = tid; i < (SR * M + 2 * C) * rowf + P * AR * NT * 4; i += NT) sm[i] = qnan;
   int nown = 0;
   if (WT) {
     const int O1 = o1hi - o1lo, O2 = o2hi - o2lo;
@@ -252,14 +252,15 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
 #pragma unroll
       for (int m = 0; m < M; m++) dold[m] = mine[m * NT];
 #pragma unroll
-      for (int c = 0; c < NCH; c++) icur[c] = mine[(M + c) * NT];
+      for (int c = 0; c < NCH; c++)
+        if (c < C) icur[c] = mine[(M + c) * NT];  // the ring holds M + C arrays
       float4 out[M];
       if (t == 0) {
 #pragma unroll
         for (int m = 0; m < M; m++) out[m] = dold[m];
       } else {
         const float *dp0 = dring + ((t - 1) & (SR - 1)) * M * rowf;
-        const float *ip0 = iring + ((t - 1) & 1) * NCH * rowf;
+        const float *ip0 = iring + ((t - 1) & 1) * C * rowf;
         float best[M][4];
 #pragma unroll
         for (int m = 0; m < M; m++)
@@ -326,7 +327,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
       float *dc = dring + (t & (SR - 1)) * M * rowf + cb;
 #pragma unroll
       for (int m = 0; m < M; m++) *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
-      float *ic = iring + (t & 1) * NCH * rowf + cb;
+      float *ic = iring + (t & 1) * C * rowf + cb;
 #pragma unroll
       for (int c = 0; c < NCH; c++)
         if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = icur[c];
