@@ -448,6 +448,10 @@ def run_gpu_arm(args, w, rank, world):
     vp_step = voxel_passes(w)
     value = world * vp_step / (ms * 1e-3) / 1e9
 
+    if args.kernels_only:
+        if rank == 0:
+            print(json.dumps({"kernels_only": True, "ms_per_step": round(ms, 4), "pass_launches": pass_launches}))
+        return
     # end to end through the public API with host buffers (pinned), result read back each call
     h_img = torch.from_numpy(w["image"]).pin_memory()
     h_msk = torch.from_numpy(w["mask"]).pin_memory()
@@ -517,6 +521,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "c3"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sampling")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="run warm-up and timed GPU steps only (no end-to-end or CPU legs): for profiler captures")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
