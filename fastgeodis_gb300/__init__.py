@@ -30,6 +30,7 @@ from . import _lib
 __version__ = "1.0.5"  # API level of the FastGeodis release this mirrors
 
 __all__ = [
+    "generalised_geodesic2d_differentiable",
     "GeodesicBatch2d",
     "generalised_geodesic2d_batch",
     "signed_generalised_geodesic2d_batch",
@@ -264,3 +265,4 @@ def GSF3d(image: torch.Tensor, softmask: torch.Tensor, theta: float, spacing: Li
 
 
 from .batch import GeodesicBatch2d, generalised_geodesic2d_batch, signed_generalised_geodesic2d_batch  # noqa: E402
+from .autograd import generalised_geodesic2d_differentiable  # noqa: E402

@@ -30,6 +30,7 @@ EXPORTED = (
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
+    "fg_grad_geodesic2d_forward", "fg_grad_geodesic2d_backward",
     "fg_generalised_geodesic2d_noalloc",
 )
 
@@ -73,6 +74,8 @@ def load():
     L.fg_batch2d_smem_bytes.argtypes = [i, i, i]
     L.fg_batch2d_smem_bytes.restype = sz
     L.fg_batch_geodesic2d.argtypes = [vp, i, i, i, i, i, vp, vp, vp]
+    L.fg_grad_geodesic2d_forward.argtypes = [vp, i, i, i, i, vp, vp, vp]
+    L.fg_grad_geodesic2d_backward.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
     for name in EXPORTED:
         if name not in ("fg_last_error",):

@@ -96,6 +96,7 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, 
   a.flags = nullptr;
   a.flag_base = 0;
   a.status = status;
+  a.tape = nullptr;
   *pa = a;
 }
 
@@ -208,4 +209,260 @@ extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, i
                      : launch_batch<1, 1>(items, n, its, S, counter, status, smem, grid, s);
   return is_signed ? launch_batch<0, 2>(items, n, its, S, counter, status, smem, grid, s)
                    : launch_batch<0, 1>(items, n, its, S, counter, status, smem, grid, s);
+}
+
+// ---------------------------------------------------------------------------
+// differentiable 2D transform: forward with argmin tape, adjoint kernel
+// ---------------------------------------------------------------------------
+
+namespace fgi {
+namespace {
+
+__device__ fg_batch2d_item as_batch_item(const fg_grad2d_item &g) {
+  fg_batch2d_item b;
+  b.image = g.image, b.mask = g.mask, b.out = g.out, b.image_t = g.image_t;
+  b.d2 = nullptr, b.t1 = g.t1, b.t2 = nullptr;
+  b.C = g.C, b.H = g.H, b.W = g.W, b.reserved0 = 0;
+  b.v = g.v, b.l_grad = g.l_grad, b.l_eucl = g.l_eucl, b.reserved1 = 0.0f;
+  return b;
+}
+
+template <int CT>
+__global__ void __launch_bounds__(kThreads, 1)
+    fg_grad2d_forward_kernel(const fg_grad2d_item *items, int n, int iterations, int S, float r2, int *counter,
+                             int *status) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int s_item;
+  __shared__ PassArgs s_args;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int i = s_item;
+    if (i >= n) break;
+    const fg_grad2d_item g = items[i];
+    const fg_batch2d_item it = as_batch_item(g);
+    const long long P = (long long)it.H * it.W;
+    if (P > 0) {
+      batch_prologue(it, false, sm);
+      __threadfence();
+      __syncthreads();
+      for (int iter = 0; iter < iterations; iter++) {
+        for (int k = 0; k < 4; k++) {
+          const int L = k >= 2 ? it.W : it.H;
+          const bool wt = k & 1;
+          if (L <= 1 && !wt) continue;
+          if (threadIdx.x == 0) {
+            batch_pass_args(it, 1, k, S, r2, status, &s_args);
+            s_args.tape = g.tape + (long long)(iter * 4 + k) * P;
+          }
+          __syncthreads();
+          if (wt)
+            pass_body<1, CT, 1, MODE_GENERAL, true, true>(s_args, 0, sm);
+          else
+            pass_body<1, CT, 1, MODE_GENERAL, false, true>(s_args, 0, sm);
+          __threadfence();
+          __syncthreads();
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ float sgnf(float d) { return d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f); }
+
+// Adjoint of one pass of one image (one CTA).  The forward pass computed, for
+// t = 1..L-1 and every cell x, D[t][x] = min(Dold[t][x], D[t-1][x+k] + cost_k);
+// the tape holds which term won.  Walking t downwards, the gradient of a cell
+// either stays with Dold (the pass input) or moves to the predecessor
+// D[t-1][x+k] (and to the image through l_grad * |I - I'| of that step).
+template <int NCH>
+__device__ void adjoint_pass(const fg_grad2d_item &g, int k, int iter, int C, float *sm) {
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const int H = g.H, W = g.W;
+  const long long P = (long long)H * W;
+  const bool alongW = k >= 2;
+  const int dir = (k & 1) ? -1 : 1;
+  const int L = alongW ? W : H, N = alongW ? H : W;
+  const long long s_str = alongW ? H : W;                      // read layout: step stride (cross stride 1)
+  long long ws_str, wc;                                        // write layout
+  if (k == 1) ws_str = 1, wc = H;
+  else if (k == 3) ws_str = 1, wc = W;
+  else ws_str = s_str, wc = 1;
+  const float *Gout = (k == 0 || k == 3) ? g.g_r : g.g_t;
+  float *Gin = alongW ? g.g_t : g.g_r;
+  const float *I = alongW ? g.image_t : g.image;
+  float *gI = alongW ? g.gi_t : g.g_image;
+  const unsigned char *tape = g.tape + (long long)(iter * 4 + k) * P;
+  const float lg = g.l_grad;
+  float *gv = sm;                                   // [N] gradient handed to the previous row
+  int *cd = reinterpret_cast<int *>(sm + N);        // [N] tape code of the row
+  float *irow = sm + 2 * N;                         // [NCH][N] image values of the row
+  constexpr int J = 4;                              // cells per thread (N <= 4 * kThreads)
+  float racc[J], gip[J][NCH];
+#pragma unroll
+  for (int j = 0; j < J; j++) {
+    racc[j] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
+  }
+  auto pos = [&](int t) -> long long { return dir > 0 ? (long long)t : (long long)(L - 1 - t); };
+  for (int t = L - 1; t >= 0; t--) {
+    const long long s = pos(t), sp = t > 0 ? pos(t - 1) : 0;
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const int x = tid + j * NT;
+      if (x >= N) continue;
+      const float G = __fadd_rn(Gout[s * ws_str + x * wc], racc[j]);
+      const int code = t > 0 ? (int)tape[s * s_str + x] : 0;
+      float gself[NCH];
+#pragma unroll
+      for (int c = 0; c < NCH; c++) gself[c] = 0.0f;
+      if (code == kTapeSelf) {
+        Gin[s * s_str + x] = G;
+        gv[x] = 0.0f;
+      } else {
+        Gin[s * s_str + x] = 0.0f;
+        const int xp = x + code - 2;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+          if (c < C) {
+            const float d = __fsub_rn(I[c * P + s * s_str + x], I[c * P + sp * s_str + xp]);
+            gself[c] = __fmul_rn(__fmul_rn(G, lg), sgnf(d));
+          }
+        gv[x] = G;
+      }
+      cd[x] = code;
+#pragma unroll
+      for (int c = 0; c < NCH; c++)
+        if (c < C) {
+          const long long o = c * P + s * s_str + x;
+          irow[c * N + x] = I[o];
+          gI[o] = __fadd_rn(gI[o], __fadd_rn(gself[c], gip[j][c]));
+        }
+    }
+    __syncthreads();
+    if (t > 0) {
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        const int xq = tid + j * NT;  // cell of row t-1
+        racc[j] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
+        if (xq >= N) continue;
+#pragma unroll
+        for (int d = -1; d <= 1; d++) {
+          const int x = xq - d;  // a cell of row t whose step came from xq
+          if (x < 0 || x >= N || cd[x] != d + 2) continue;
+          const float gx = gv[x];
+          racc[j] = __fadd_rn(racc[j], gx);
+#pragma unroll
+          for (int c = 0; c < NCH; c++)
+            if (c < C) {
+              const float dd = __fsub_rn(irow[c * N + x], I[c * P + sp * s_str + xq]);
+              gip[j][c] = __fsub_rn(gip[j][c], __fmul_rn(__fmul_rn(gx, lg), sgnf(dd)));
+            }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int NCH>
+__global__ void __launch_bounds__(kThreads, 1)
+    fg_grad2d_backward_kernel(const fg_grad2d_item *items, int n, int iterations, int *counter) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int i = s_item;
+    if (i >= n) break;
+    const fg_grad2d_item g = items[i];
+    const int H = g.H, W = g.W, C = g.C;
+    const long long P = (long long)H * W;
+    if (P > 0) {
+      for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_r[p] = g.g_out[p];
+      for (long long p = threadIdx.x; p < C * P; p += blockDim.x) g.g_image[p] = 0.0f, g.gi_t[p] = 0.0f;
+      __threadfence();
+      __syncthreads();
+      for (int iter = iterations - 1; iter >= 0; iter--) {
+        for (int k = 3; k >= 0; k--) {
+          const int L = k >= 2 ? W : H;
+          if (L <= 1 && !(k & 1)) continue;  // the forward skipped this pass
+          adjoint_pass<NCH>(g, k, iter, C, sm);
+          __threadfence();
+          __syncthreads();
+        }
+      }
+      // dLoss/dmask = v * dLoss/dD0 ; dLoss/dimage = its original-layout part + the transposed part
+      for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_mask[p] = __fmul_rn(g.v, g.g_r[p]);
+      for (long long q = threadIdx.x; q < C * P; q += blockDim.x) {
+        const long long c = q / P, r = q - c * P, h = r / W, w = r - h * W;
+        g.g_image[q] = __fadd_rn(g.g_image[q], g.gi_t[c * P + w * H + h]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+}  // namespace fgi
+
+extern "C" FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                                 int iterations, int *counter, int *status, void *stream) {
+  using namespace fgi;
+  if (n < 0 || (n > 0 && (!items || !counter || !status)))
+    return set_error(FG_ERR_INVALID_ARGUMENT, "grad: null descriptor, counter or status pointer");
+  if (max_C < 1 || max_C > kMaxChannels) return set_error(FG_ERR_UNSUPPORTED, "grad: images need 1 to 4 channels");
+  if (max_extent > 4 * kThreads) return set_error(FG_ERR_UNSUPPORTED, "grad: image sides up to 2048 are supported");
+  if (n == 0) return FG_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int S = batch_flush_steps(max_C, max_extent, 0);
+  const size_t smem = batch_smem(max_C, max_extent, 0, S);
+  if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "grad: shared memory plan too large");
+  const int grid = std::max(1, std::min(n, sms));
+  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
+  auto launch = [&](auto fn) -> int {
+    cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
+    fn<<<grid, kThreads, smem, s>>>(items, n, std::max(iterations, 0), S, r2, counter, status);
+    e2 = cudaGetLastError();
+    return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
+  };
+  return max_C == 1 ? launch(fg_grad2d_forward_kernel<1>) : launch(fg_grad2d_forward_kernel<0>);
+}
+
+extern "C" FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                                  int iterations, int *counter, int *status, void *stream) {
+  using namespace fgi;
+  (void)status;
+  if (n < 0 || (n > 0 && (!items || !counter)))
+    return set_error(FG_ERR_INVALID_ARGUMENT, "grad: null descriptor or counter pointer");
+  if (max_C < 1 || max_C > kMaxChannels) return set_error(FG_ERR_UNSUPPORTED, "grad: images need 1 to 4 channels");
+  if (max_extent > 4 * kThreads) return set_error(FG_ERR_UNSUPPORTED, "grad: image sides up to 2048 are supported");
+  if (n == 0) return FG_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int nch = max_C == 1 ? 1 : kMaxChannels;
+  const size_t smem = (size_t)(2 + nch) * max_extent * 4 + 64;
+  const int grid = std::max(1, std::min(n, sms));
+  auto launch = [&](auto fn) -> int {
+    cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
+    fn<<<grid, kThreads, smem, s>>>(items, n, std::max(iterations, 0), counter);
+    e2 = cudaGetLastError();
+    return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
+  };
+  return max_C == 1 ? launch(fg_grad2d_backward_kernel<1>) : launch(fg_grad2d_backward_kernel<kMaxChannels>);
 }

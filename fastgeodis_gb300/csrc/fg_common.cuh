@@ -47,7 +47,12 @@ struct PassArgs {
   unsigned *flags;                // per-tile progress (chunks completed)
   unsigned flag_base;
   int *status;                    // FG_ERR_TIMEOUT if a bounded wait expired
+  unsigned char *tape;            // argmin tape of this pass, read layout, 1 byte per cell (TAPE variants)
 };
+
+// Argmin tape codes: 0 = the cell kept its old distance, 1 + n = it took the
+// candidate of neighbour n (n = 3*(d1+1) + (d2+1); 2D: n = d2+1).
+constexpr unsigned char kTapeSelf = 0;
 
 struct LaunchCfg {
   int tiles;

@@ -98,7 +98,7 @@ __device__ __forceinline__ void cp_async_wait() {
 // The body of one pass over tile `tile`, shared by the per-pass kernel and the
 // batched kernel.  `ar` may live in parameter or shared memory; it is copied
 // into registers first so the step loop never reloads its fields.
-template <int CROSS, int CT, int M, int MODE, bool WT>
+template <int CROSS, int CT, int M, int MODE, bool WT, bool TAPE = false>
 __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, float *sm) {
   const PassArgs a = ar;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
@@ -180,6 +180,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const long long r0 = (a.dir > 0 ? 0 : (long long)(L - 1) * a.s_str) + (long long)g1 * a.st1 + g20;
   const long long w0 = (a.dir > 0 ? 0 : (long long)(L - 1) * a.ws_str) + (long long)g1 * a.wst1 + (long long)g20 * a.wst2;
   long long rnext = r0;  // read offset of the next step to stage
+  long long rcur = r0;   // read offset of the current step
   long long wcur = w0;   // write offset of the current step
 
   // stage the own inputs of the next step into ring slot `slot` (one commit group per step)
@@ -262,6 +263,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         const float *dp0 = dring + ((t - 1) & (SR - 1)) * M * rowf;
         const float *ip0 = iring + ((t - 1) & 1) * C * rowf;
         float best[M][4];
+        unsigned code[4] = {kTapeSelf, kTapeSelf, kTapeSelf, kTapeSelf};  // TAPE: argmin of map 0
 #pragma unroll
         for (int m = 0; m < M; m++)
 #pragma unroll
@@ -310,9 +312,24 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
                   cand = __fadd_rn(dp[m][i + 1 + d2], a.e[m][n]);
                 else
                   cand = __fadd_rn(dp[m][i + 1 + d2], l1);
-                best[m][i] = fminf(best[m][i], cand);
+                if (TAPE && m == 0) {
+                  // same value as fminf for the non-NaN current distance of an in-image cell
+                  if (cand < best[m][i]) best[m][i] = cand, code[i] = 1 + n;
+                } else {
+                  best[m][i] = fminf(best[m][i], cand);
+                }
               }
             }
+          }
+        }
+        if (TAPE && own) {
+          unsigned char *tp = a.tape + rcur;  // the tape has the read layout, one byte per cell
+          if (own == 0xFu && a.vec) {
+            *reinterpret_cast<unsigned *>(tp) = code[0] | (code[1] << 8) | (code[2] << 16) | (code[3] << 24);
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              if (own & (1u << i)) tp[i] = (unsigned char)code[i];
           }
         }
 #pragma unroll
@@ -348,6 +365,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     if (t + P < L) stage(slot);
     else cp_async_commit();
     wcur += wstep;
+    rcur += rstep;
     __syncthreads();
     const bool chunk_end = ((t + 1) & (S - 1)) == 0 || t == L - 1;
     if (WT && chunk_end) {

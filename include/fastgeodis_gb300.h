@@ -158,6 +158,36 @@ FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, i
                                int is_signed, int iterations, int *counter, int *status,
                                void *stream);
 
+/* One image of a differentiable 2D transform (fg_grad_geodesic2d_forward /
+ * _backward; no counterpart in the reference, which is not differentiable).
+ * Device pointers, float32 unless noted, contiguous; scratch belongs to the
+ * caller and is shared by the forward and the backward of one image. */
+typedef struct fg_grad2d_item {
+  const float *image;   /* [C][H][W] */
+  const float *mask;    /* [H][W] soft mask */
+  float *out;           /* forward output D [H][W] */
+  float *image_t;       /* scratch [C][W][H] */
+  float *t1;            /* scratch [W][H] */
+  unsigned char *tape;  /* iterations * 4 * H * W bytes: argmin of every cell in every pass */
+  const float *g_out;   /* backward input dLoss/dD [H][W] */
+  float *g_image;       /* backward output dLoss/dimage [C][H][W] */
+  float *g_mask;        /* backward output dLoss/dmask [H][W] */
+  float *g_r;           /* scratch [H][W] */
+  float *g_t;           /* scratch [W][H] */
+  float *gi_t;          /* scratch [C][W][H] */
+  int C, H, W, reserved0;
+  float v, l_grad, l_eucl, reserved1;
+} fg_grad2d_item;
+
+/* Forward: D exactly as fg_generalised_geodesic2d, plus the argmin tape. */
+FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                      int iterations, int *counter, int *status, void *stream);
+/* Backward: routes dLoss/dD along the recorded argmins (the adjoint of every
+ * pass, last pass first) to dLoss/dmask (= v * dLoss/dD0) and dLoss/dimage
+ * (l_grad * sign(dI) of each step taken). */
+FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                       int iterations, int *counter, int *status, void *stream);
+
 /* Allocation-free variant of fg_generalised_geodesic2d (no counterpart in
  * the reference).  For callers that cannot allocate device memory when they
  * need the transform -- code running inside a framework that owns the
