@@ -206,6 +206,202 @@ def run_batch_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_grad_arm(args, rank, world):
+    """Differentiable geodesic2d: batch 16x1x512x512 smoothed noise, soft
+    mask sigmoid(smoothed Gaussian noise), lamb 0.75, iterations 2, v 10,
+    loss = sum(w * D) with w ~ U[0,1]; forward + backward timed, gradients
+    checked against float64 central finite differences (eps 1e-3) of the
+    oracle scan at 64 random voxels of the first image."""
+    import torch
+
+    import fastgeodis_gb300 as fg
+    from oracle import oracle
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(4)
+    B, H, W = 16, 512, 512
+    v, lamb, it = 10.0, 0.75, 2
+    img = np.stack([smooth_noise(rng, (H, W), 3.0, 0.0, 255.0) for _ in range(B)])[:, None]
+    msk = np.stack([1.0 / (1.0 + np.exp(-smooth_noise(rng, (H, W), 3.0, -6.0, 6.0) * 4.0)) for _ in range(B)])
+    msk = msk[:, None].astype(np.float32)
+    wts = rng.random((B, 1, H, W)).astype(np.float32)
+    ti = torch.from_numpy(img).cuda().requires_grad_(True)
+    tm = torch.from_numpy(msk).cuda().requires_grad_(True)
+    tw = torch.from_numpy(wts).cuda()
+    flush = torch.empty(FLUSH_BYTES // 4, device="cuda")
+
+    def step():
+        ti.grad = None
+        tm.grad = None
+        d = fg.generalised_geodesic2d_differentiable(ti, tm, v, lamb, it)
+        (d * tw).sum().backward()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local).start()
+    tot = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    clk = clocks.stop()
+    ms = tot / args.steps
+    gi = ti.grad[0, 0].cpu().numpy().astype(np.float64)
+    gm = tm.grad[0, 0].cpu().numpy().astype(np.float64)
+    if rank != 0:
+        return
+    # float64 finite differences of the same scan (oracle), first image
+    eps = 1e-3
+    w0 = wts[0, 0].astype(np.float64)
+    im0, m0 = img[0].astype(np.float64), msk[0].astype(np.float64)
+
+    def loss(im, m):
+        return float((oracle.geodesic2d_f64(im, m, v, lamb, it)[0] * w0).sum())
+
+    pts = [(int(rng.integers(0, H)), int(rng.integers(0, W))) for _ in range(64)]
+    agree_i = agree_m = 0
+    max_rel = 0.0
+    t0 = time.perf_counter()
+    for (y, x) in pts:
+        p, q = im0.copy(), im0.copy()
+        p[0, y, x] += eps
+        q[0, y, x] -= eps
+        fd_i = (loss(p, m0) - loss(q, m0)) / (2 * eps)
+        p, q = m0.copy(), m0.copy()
+        p[0, y, x] += eps
+        q[0, y, x] -= eps
+        fd_m = (loss(im0, p) - loss(im0, q)) / (2 * eps)
+        for fd, g, tag in ((fd_i, gi[y, x], "i"), (fd_m, gm[y, x], "m")):
+            rel = abs(fd - g) / max(1.0, abs(fd))
+            ok = rel <= 1e-2
+            if tag == "i":
+                agree_i += ok
+            else:
+                agree_m += ok
+            if ok:
+                max_rel = max(max_rel, rel)
+    fd_s = time.perf_counter() - t0
+    vp = float(B * H * W * 4 * it)  # forward voxel-passes; the adjoint walks the same passes once more
+    line = {
+        "metric": "differentiable generalised_geodesic2d forward+backward throughput",
+        "value": round(2 * vp / ms / 1e6, 4), "unit": "Gvoxel-passes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "16x1x512x512 smoothed noise [0,255], softmask sigmoid(smoothed noise), lamb 0.75, "
+                               "v 10, iterations 2, loss sum(w*D), w ~ U[0,1]; forward + backward per step",
+                   "grad_check": {"voxels": 64, "eps": 1e-3, "reference": "float64 central differences of the scan",
+                                  "image_agree": int(agree_i), "mask_agree": int(agree_m),
+                                  "tolerance": "1e-2 relative (1e-2 absolute below 1)",
+                                  "max_rel_err_agreeing": max_rel, "seconds": round(fd_s, 1)},
+                   "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)"},
+        "clocks": clk, "gpu_launches": 2,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serve_arm(args, rank, world):
+    """Served interactive stream: Poisson arrivals at 200 req/s; 70% 2D
+    (256^2-2048^2, 1-3 channels), 30% 3D (64^3-256^3, spacing U[0.5, 3] per
+    axis); 1-5 click seeds each; 10% of requests GSF (theta 0.5); v 1e10,
+    lamb 1.0, iterations 2.  Images live on the device (a pool of 12 2D and
+    6 3D images, registered once), masks are rasterised from the clicks on the
+    device.  The continuous-batching server (8 in flight, 4 streams, 16 GB
+    budget) is compared with the same arrivals served one at a time on one
+    stream (the plain per-call path)."""
+    import torch
+
+    from fastgeodis_gb300.serving import GeodesicServer, Request
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(11)
+    g = torch.Generator(device="cpu").manual_seed(11)
+    pool2d, pool3d = [], []
+    for _ in range(12):
+        H, W, C = int(rng.integers(256, 2049)), int(rng.integers(256, 2049)), int(rng.integers(1, 4))
+        pool2d.append(torch.rand((1, C, H, W), generator=g) * 255)
+    for _ in range(6):
+        n = [int(rng.integers(64, 257)) for _ in range(3)]
+        pool3d.append(torch.rand((1, 1) + tuple(n), generator=g))
+    n_req = args.requests
+    rate = 200.0
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    specs = []
+    for i in range(n_req):
+        is3d = rng.random() < 0.3
+        key = ("v", int(rng.integers(0, len(pool3d)))) if is3d else ("i", int(rng.integers(0, len(pool2d))))
+        img = pool3d[key[1]] if is3d else pool2d[key[1]]
+        shape = img.shape[2:]
+        clicks = [[int(rng.integers(0, s)) for s in shape] for _ in range(int(rng.integers(1, 6)))]
+        sp = [float(x) for x in rng.uniform(0.5, 3.0, 3)] if is3d else None
+        op = "gsf" if rng.random() < 0.1 else "plain"
+        cells = float(np.prod(shape))
+        vp = cells * (6 if is3d else 4) * 2 * (6 if op == "gsf" else 1)
+        specs.append((key, clicks, sp, op, vp))
+
+    def serve(max_inflight, streams):
+        srv = GeodesicServer(budget_bytes=16 << 30, max_inflight=max_inflight, streams=streams)
+        for i, t in enumerate(pool2d):
+            srv.register_image(("i", i), t)
+        for i, t in enumerate(pool3d):
+            srv.register_image(("v", i), t)
+        # warm-up: one request of every image (kernel variants, workspaces)
+        for key in [("i", i) for i in range(len(pool2d))] + [("v", i) for i in range(len(pool3d))]:
+            img = srv.executor.images[key]
+            srv.submit(Request(image_id=key, clicks=[[0] * (img.dim() - 2)], v=1e10, lamb=1.0,
+                               spacing=[1.0, 1.0, 1.0] if img.dim() == 5 else None))
+        srv.drain()
+        srv.scheduler.completed.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reqs = []
+        for (key, clicks, sp, op, vp), ta in zip(specs, arrivals):
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            reqs.append(srv.submit(Request(image_id=key, clicks=clicks, op=op, v=1e10, lamb=1.0, iterations=2,
+                                           spacing=sp, theta=0.5, radius=3)))
+        srv.drain(timeout=600)
+        wall = time.perf_counter() - t0
+        errs = [r.error for r in reqs if r.error is not None]
+        if errs:
+            raise errs[0]
+        pct = srv.scheduler.latency_percentiles((50, 99))
+        peak = srv.scheduler.peak_inflight
+        srv.close()
+        return pct, wall, peak
+
+    clocks = ClockSampler(local).start()
+    pct_b, wall_b, peak_b = serve(8, 4)
+    clk = clocks.stop()
+    pct_s, wall_s, _ = serve(1, 1)
+    vp_total = sum(s[4] for s in specs)
+    if rank != 0:
+        return
+    line = {
+        "metric": "served geodesic requests: throughput (p50/p99 latency in config)",
+        "value": round(n_req / wall_b, 2), "unit": "requests/s", "n_gpus": world, "steps": n_req,
+        "warmup": 18, "ms_per_step": round(wall_b / n_req * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n_req} requests, Poisson arrivals at 200/s, 70% 2D 256^2-2048^2 C 1-3, "
+                               "30% 3D 64^3-256^3 spacing U[0.5,3], 1-5 clicks (r=3), 10% GSF (theta 0.5), "
+                               "v 1e10, lamb 1, iterations 2",
+                   "server": "continuous batching, 8 in flight, 4 streams, 16 GB HBM budget",
+                   "p50_ms": round(pct_b["p50"], 3), "p99_ms": round(pct_b["p99"], 3),
+                   "peak_inflight": peak_b, "gvoxel_passes_per_s": round(vp_total / wall_b / 1e9, 3),
+                   "per_call_path": {"p50_ms": round(pct_s["p50"], 3), "p99_ms": round(pct_s["p99"], 3),
+                                     "requests_per_s": round(n_req / wall_s, 2)}},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def voxel_passes(w) -> float:
     n = float(np.prod(w["image"].shape[2:]))
     per = 6 if w["dims"] == 3 else 4
@@ -519,13 +715,26 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "c3", "c4", "c5"])
+    ap.add_argument("--requests", type=int, default=300, help="requests of the served stream (c5)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run warm-up and timed GPU steps only (no end-to-end or CPU legs): for profiler captures")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.workload == "c5":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no server"}))
+            return
+        run_serve_arm(args, rank, world)
+        return
+    if args.workload == "c4":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradient"}))
+            return
+        run_grad_arm(args, rank, world)
+        return
     if args.workload == "c3":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the uneven batch has no reference CPU arm here"}))
