@@ -25,7 +25,7 @@ FG_OP_GSF = 2
 
 # every symbol include/fastgeodis_gb300.h declares
 EXPORTED = (
-    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_profile_begin", "fg_profile_end",
+    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override", "fg_profile_begin", "fg_profile_end",
     "fg_workspace_bytes", "fg_workspace_status",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
@@ -62,6 +62,8 @@ def load():
     L.fg_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
                                  ctypes.POINTER(ctypes.c_double)]
     L.fg_set_tuning.argtypes = [i, i]
+    L.fg_plan_override.argtypes = [i, i, i, i, i, i]
+    L.fg_plan_override.restype = i
     L.fg_set_tuning.restype = i
     L.fg_workspace_status.argtypes = [vp, vp]
     L.fg_workspace_status.restype = i

@@ -53,7 +53,7 @@ __device__ void batch_prologue(const fg_batch2d_item &it, bool is_signed, float 
 
 // arguments of pass `k` (0: along H forward, 1: along H backward writing
 // [W][H], 2: along W forward, 3: along W backward writing [H][W])
-__device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, float r2, int *status,
+__device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, int depth, float r2, int *status,
                                 PassArgs *pa) {
   PassArgs a;
   const int H = it.H, W = it.W;
@@ -97,6 +97,7 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, 
   a.flag_base = 0;
   a.status = status;
   a.tape = nullptr;
+  a.P = depth;
   *pa = a;
 }
 
@@ -122,7 +123,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int L = k >= 2 ? it.W : it.H;
           const bool wt = k & 1;
           if (L <= 1 && !wt) continue;
-          if (threadIdx.x == 0) batch_pass_args(it, M, k, S, r2, status, &s_args);
+          if (threadIdx.x == 0)
+            batch_pass_args(it, M, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), M), r2, status, &s_args);
           __syncthreads();
           if (wt)
             pass_body<1, CT, M, MODE_GENERAL, true>(s_args, 0, sm);
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const bool wt = k & 1;
           if (L <= 1 && !wt) continue;
           if (threadIdx.x == 0) {
-            batch_pass_args(it, 1, k, S, r2, status, &s_args);
+            batch_pass_args(it, 1, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), 1), r2, status, &s_args);
             s_args.tape = g.tape + (long long)(iter * 4 + k) * P;
           }
           __syncthreads();

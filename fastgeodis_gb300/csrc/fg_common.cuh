@@ -44,6 +44,7 @@ struct PassArgs {
   int B2;                         // floats per buffer row (4-cell left apron, runs of 4, right apron)
   int rowf;                       // floats per buffer position (all rows), multiple of 32
   int vec;                        // runs may use 16-byte global loads and stores
+  int P;                          // steps of own inputs staged ahead (2, 4 or 8)
   unsigned *flags;                // per-tile progress (chunks completed)
   unsigned flag_base;
   int *status;                    // FG_ERR_TIMEOUT if a bounded wait expired
@@ -62,7 +63,9 @@ struct LaunchCfg {
 
 // Shared-memory bytes of a pass kernel for a region of R1 x R2 cells.
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2, int *rowf,
-                       int *nown_max);
+                       int *nown_max, int depth);
+// largest staging depth a variant supports (registers hold none of it: it is shared memory)
+constexpr int max_pass_depth(int nch, int m) { return (nch + m <= 4) ? 8 : 2; }
 
 // Launchers (one translation unit per cross-section rank).
 int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);

@@ -184,7 +184,7 @@ DeviceInfo device_info() {
 }
 
 struct Plan {
-  int T1, T2, K1, K2, tiles1, tiles2, S, NT, B2, rowf;
+  int T1, T2, K1, K2, tiles1, tiles2, S, NT, B2, rowf, P;
   size_t smem;
 };
 
@@ -196,12 +196,17 @@ std::atomic<int> g_tune_tiles{0};            // cap on tiles per pass (0: the SM
 // hand-off of a multi-tile plan spread over the S steps of a chunk.
 constexpr double kStepLatency = 250.0, kCyclesPerRun = 1.2, kHandoff = 3000.0;
 
+// Plan overrides set by the autotuner (fg_plan_override): cross-section shape -> (S, T1, T2).
+std::mutex g_override_mu;
+std::map<std::tuple<int, int, int>, std::tuple<int, int, int>> g_overrides;
+std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older cache entries are stale
+
 bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int max_tiles, Plan *out) {
   static std::mutex mu;
-  static std::map<std::tuple<int, int, int, int, int, int, bool, int, int>, Plan> cache;
+  static std::map<std::tuple<int, int, int, int, int, int, bool, int, int, unsigned>, Plan> cache;
   const int max_region = g_tune_region.load();
   if (g_tune_tiles.load() > 0) max_tiles = std::min(max_tiles, g_tune_tiles.load());
-  auto key = std::make_tuple(cross, N1, N2, C, M, mode, wt, max_tiles, max_region);
+  auto key = std::make_tuple(cross, N1, N2, C, M, mode, wt, max_tiles, max_region, g_plan_epoch.load());
   {
     std::lock_guard<std::mutex> g(mu);
     auto it = cache.find(key);
@@ -224,19 +229,40 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     int runs = R1 * ((R2 + 3) / 4);
     if (runs > kThreads) return -1;
     int B2, rowf, nown;
-    size_t sm = pass_smem_bytes(cross, C, M, mode, wt, S, R1, R2, &B2, &rowf, &nown);
+    const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
+    // deepest staging that still leaves room for a second CTA on the SM (then
+    // concurrent transforms on other streams share its issue slots)
+    int depth = max_pass_depth(nch, M);
+    size_t sm = pass_smem_bytes(cross, C, M, mode, wt, S, R1, R2, &B2, &rowf, &nown, depth);
+    while (depth > 2 && sm > kSmemBudget / 2) {
+      depth /= 2;
+      sm = pass_smem_bytes(cross, C, M, mode, wt, S, R1, R2, &B2, &rowf, &nown, depth);
+    }
     (void)nown;
     if (sm > kSmemBudget) return -1;
     double cost = std::max(kStepLatency, kCyclesPerRun * runs) + (multi ? kHandoff / S : 0.0);
+    if (sm > kSmemBudget / 2) cost *= 1.05;
     if (!found || cost < best_cost - 1e-9) {
       int nt = std::max(32, std::min(kThreads, (runs + 31) / 32 * 32));
-      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, sm};
+      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm};
       best_cost = cost;
       found = true;
     }
     return 1;
   };
+  int ovS = 0, ovT1 = 0, ovT2 = 0;
+  {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    auto it = g_overrides.find(std::make_tuple(cross, N1, N2));
+    if (it != g_overrides.end()) std::tie(ovS, ovT1, ovT2) = it->second;
+  }
+  if (ovS > 0) {
+    const int T1 = cross == 2 ? std::min(ovT1, N1) : 1, T2 = std::min(ovT2, N2);
+    const int t1 = (N1 + T1 - 1) / T1, t2 = (N2 + T2 - 1) / T2;
+    if ((long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2);
+  }
   for (int S : {8, 4, 2, 1}) {
+    if (found) break;  // an override that fits wins
     if (cross == 1) {
       for (int tiles2 = 1; tiles2 <= max_tiles; tiles2++) {
         int T2 = (N2 + tiles2 - 1) / tiles2;
@@ -266,9 +292,9 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (debug)
       fprintf(stderr,
               "[fg plan] cross=%d N=%dx%d C=%d M=%d mode=%d wt=%d -> T=%dx%d K=%d,%d tiles=%dx%d S=%d NT=%d "
-              "smem=%zu cost=%.0f\n",
+              "P=%d smem=%zu cost=%.0f\n",
               cross, N1, N2, C, M, mode, (int)wt, best.T1, best.T2, best.K1, best.K2, best.tiles1, best.tiles2,
-              best.S, best.NT, best.smem, best_cost);
+              best.S, best.NT, best.P, best.smem, best_cost);
   }
   return found;
 }
@@ -509,6 +535,7 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
             vec = vec && (reinterpret_cast<uintptr_t>(a.dsrc[m]) & 15) == 0 &&
                   (reinterpret_cast<uintptr_t>(a.ddst[m]) & 15) == 0;
           a.vec = vec ? 1 : 0;
+          a.P = p.P;
           a.flags = w.flags;
           a.flag_base = (*launch_counter) << 16;
           a.status = w.status;
@@ -613,10 +640,8 @@ int geom3d(int C, int D, int H, int W, const float *spacing, Geometry *g) {
 namespace fgi {
 
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2o, int *rowfo,
-                       int *nown_max) {
-  const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);  // channels of the variant
-  const int depth = (nch + M <= 2) ? 8 : ((nch + M <= 4) ? 4 : 2);        // pass_depth in fg_pass.cuh
-  const int ci = mode == MODE_EUCLID ? 0 : C;                              // image arrays staged
+                       int *nown_max, int depth) {
+  const int ci = mode == MODE_EUCLID ? 0 : C;  // image arrays staged
   const int B1 = cross == 2 ? R1 + 2 : 1, B2 = ((R2 + 3) & ~3) + 8;
   const int rowf = (B1 * B2 + 3) & ~3;
   const int SR = wt ? S : 2;
@@ -671,6 +696,21 @@ int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_passes) {
   ps.ev.clear();
   ps.vp.clear();
   return rc;
+}
+
+int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2) {
+  if (cross < 1 || cross > 2 || N1 < 1 || N2 < 1) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad shape");
+  std::lock_guard<std::mutex> g(g_override_mu);
+  auto key = std::make_tuple(cross, N1, N2);
+  if (S == 0) {
+    g_overrides.erase(key);
+  } else {
+    if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
+    if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
+    g_overrides[key] = std::make_tuple(S, T1, T2);
+  }
+  g_plan_epoch.fetch_add(1);
+  return FG_OK;
 }
 
 int fg_set_tuning(int max_region_cells, int max_tiles) {

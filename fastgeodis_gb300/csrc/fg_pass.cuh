@@ -79,7 +79,7 @@ __device__ __forceinline__ void f4set(float4 &v, int i, float x) {
 __host__ __device__ constexpr int pass_nch(int ct, int mode) {
   return mode == MODE_EUCLID ? 0 : (ct == 0 ? kMaxChannels : ct);
 }
-__host__ __device__ constexpr int pass_depth(int nch, int m) { return (nch + m <= 2) ? 8 : ((nch + m <= 4) ? 4 : 2); }
+__host__ __device__ constexpr int pass_depth(int nch, int m) { return (nch + m <= 4) ? 4 : 2; }
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
   unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -104,7 +104,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
-  constexpr int P = pass_depth(NCH, M);  // steps of own inputs in flight (power of 2)
+  const int P = a.P;                     // steps of own inputs in flight (power of 2)
   constexpr int A1 = CROSS == 2 ? 1 : 0; // apron row above the region
   constexpr int NR = CROSS == 2 ? 3 : 1; // stencil rows
 
@@ -224,7 +224,6 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     __syncthreads();
   };
 
-#pragma unroll
   for (int k = 0; k < P; k++) {
     if (k < L) stage(k);
     else cp_async_commit();
@@ -246,7 +245,10 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
       }
       __syncthreads();
     }
-    cp_async_wait<P - 1>();  // this thread's inputs of step t have landed
+    // this thread's inputs of step t have landed (P - 1 younger groups may still be in flight)
+    if (P == 8) cp_async_wait<7>();
+    else if (P == 4) cp_async_wait<3>();
+    else cp_async_wait<1>();
     if (active) {
       const float4 *mine = oring + slot * AR * NT + tid;
       float4 dold[M], icur[NCHR];

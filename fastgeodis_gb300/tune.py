@@ -1,0 +1,170 @@
+"""Autotuner: picks each pass's tiling by measurement instead of by the model.
+
+The engine plans every pass (tile extents T1 x T2 of the cross-section, halo
+hand-off every S steps) from a cost model of one step.  `autotune` replaces the
+model's choice by timing: for each distinct pass cross-section of a transform
+it tries candidate plans, runs the whole transform on seeded synthetic data of
+that shape with each candidate, reads the pass-kernel time from the engine's
+event hooks (fg_profile_begin / fg_profile_end) and pins the fastest plan with
+``fg_plan_override``.  Cross-sections are tuned one after another with the
+others held fixed, so differences in the total are the tuned pass's own.
+
+Every plan computes the same bits; only the time changes.  Pinned plans hold
+for the process (all shapes with that cross-section) until `clear`.
+"""
+from __future__ import annotations
+
+import json
+import math
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import torch
+
+from . import _lib
+
+# Limits of one tile's region, as the engine checks them (fg_common.cuh):
+# at most kMaxRegion cells and kThreads runs of 4 cells.
+MAX_REGION = 2048
+MAX_RUNS = 512
+
+Key = Tuple[int, int, int]        # (cross, N1, N2)
+Choice = Tuple[int, int, int]     # (S, T1, T2)
+
+
+def _ceil(a: int, b: int) -> int:
+    return -(-a // b)
+
+
+def candidates(cross: int, N1: int, N2: int, sms: int, steps=(4, 8), max_per_step: int = 24) -> List[Choice]:
+    """Valid plans for a cross-section: for each tile count along N2 the
+    smallest tile height T1 that keeps every tile co-resident on `sms` SMs."""
+    out: List[Choice] = []
+    for S in steps:
+        seen_T2 = set()
+        n = 0
+        for t2 in range(1, N2 + 1):
+            T2 = _ceil(N2, t2)
+            if t2 > 1:
+                T2 = (T2 + 3) // 4 * 4  # runs of 4 cells must not straddle tiles
+            if T2 in seen_T2 or _ceil(N2, T2) > sms:
+                continue
+            seen_T2.add(T2)
+            tt2 = _ceil(N2, T2)
+            K2 = S if tt2 > 1 else 0
+            if tt2 > 1 and T2 < K2:
+                break
+            if cross == 1:
+                T1, K1 = 1, 0
+            else:
+                T1 = next((c for c in range(1, N1 + 1) if _ceil(N1, c) * tt2 <= sms), None)
+                if T1 is None:
+                    continue
+                K1 = S if _ceil(N1, T1) > 1 else 0
+                if K1 and T1 < K1:
+                    T1 = min(K1, N1)
+                    K1 = S if _ceil(N1, T1) > 1 else 0
+            R1 = T1 + 2 * K1 if cross == 2 else 1
+            R2 = T2 + 2 * K2
+            if R1 * R2 > MAX_REGION or R1 * _ceil(R2, 4) > MAX_RUNS:
+                continue
+            out.append((S, T1, T2))
+            n += 1
+            if n >= max_per_step:
+                break
+    return out
+
+
+def pass_keys(shape: Sequence[int]) -> List[Key]:
+    """Distinct (cross, N1, N2) cross-sections of a transform's passes."""
+    if len(shape) == 2:
+        H, W = (int(s) for s in shape)
+        keys = [(1, 1, W), (1, 1, H)]       # along H over [H][W], along W over [W][H]
+    elif len(shape) == 3:
+        D, H, W = (int(s) for s in shape)
+        keys = [(2, H, W), (2, D, W), (2, D, H)]  # along D, H, W
+    else:
+        raise ValueError("shape must be (H, W) or (D, H, W)")
+    return list(dict.fromkeys(keys))
+
+
+def pin(choices: Dict[Key, Choice]) -> None:
+    L = _lib.load()
+    for (cross, N1, N2), (S, T1, T2) in choices.items():
+        _lib.check(L.fg_plan_override(cross, N1, N2, S, T1, T2))
+
+
+def clear(shape: Sequence[int]) -> None:
+    """Unpin the plans of a shape's cross-sections (the cost model decides again)."""
+    L = _lib.load()
+    for cross, N1, N2 in pass_keys(shape):
+        _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0))
+
+
+def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing=(1.0, 1.0, 1.0),
+             iterations: int = 1, repeats: int = 3, device=None, max_per_step: int = 24,
+             verbose: bool = False) -> Dict[Key, Tuple[int, int, int, float]]:
+    """Measure candidate plans for a 2D (H, W) or 3D (D, H, W) transform of
+    `channels` image channels and pin the fastest for each cross-section.
+
+    Returns {(cross, N1, N2): (S, T1, T2, best pass-kernel ms of a transform)}.
+    The model's own plan competes as the unpinned entry (S = 0)."""
+    import fastgeodis_gb300 as fg
+
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    shape = tuple(int(s) for s in shape)
+    L = _lib.load()
+    g = torch.Generator(device="cpu").manual_seed(0)
+    img = torch.rand((1, channels) + shape, generator=g).to(dev)
+    msk = torch.ones((1, 1) + shape, device=dev)
+    msk.view(-1)[msk.numel() // 2] = 0.0
+    if len(shape) == 2:
+        run = lambda: fg.generalised_geodesic2d(img, msk, 1e10, lamb, iterations)
+    else:
+        run = lambda: fg.generalised_geodesic3d(img, msk, list(spacing), 1e10, lamb, iterations)
+
+    def measure() -> float:
+        run()  # first launch of a plan sets up its kernel attributes
+        torch.cuda.synchronize(dev)
+        best = math.inf
+        for _ in range(repeats):
+            _lib.profile_begin()
+            run()
+            ms, _, _ = _lib.profile_end()
+            best = min(best, ms)
+        return best
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    result = {}
+    with torch.cuda.device(dev):
+        for key in pass_keys(shape):
+            cross, N1, N2 = key
+            _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0))
+            best_c, best_t = (0, 0, 0), measure()
+            if verbose:
+                print(f"[tune] {key} model plan: {best_t:.3f} ms")
+            for c in candidates(cross, N1, N2, sms, max_per_step=max_per_step):
+                _lib.check(L.fg_plan_override(cross, N1, N2, *c))
+                t = measure()
+                if verbose:
+                    print(f"[tune] {key} S={c[0]} T={c[1]}x{c[2]}: {t:.3f} ms")
+                if t < best_t:
+                    best_c, best_t = c, t
+            _lib.check(L.fg_plan_override(cross, N1, N2, *best_c))
+            result[key] = best_c + (best_t,)
+    return result
+
+
+def save(result: Dict[Key, Tuple], path: str) -> None:
+    """Write tuned plans as JSON ({"cross,N1,N2": [S, T1, T2, ms]})."""
+    with open(path, "w") as f:
+        json.dump({",".join(map(str, k)): list(v) for k, v in result.items()}, f, indent=1)
+
+
+def load(path: str, apply: bool = True) -> Dict[Key, Tuple]:
+    """Read plans written by `save` and (by default) pin them."""
+    with open(path) as f:
+        raw = json.load(f)
+    result = {tuple(int(x) for x in k.split(",")): tuple(v) for k, v in raw.items()}
+    if apply:
+        pin({k: tuple(int(x) for x in v[:3]) for k, v in result.items() if int(v[0]) > 0})
+    return result

@@ -65,6 +65,14 @@ FG_API size_t fg_workspace_bytes(int op, int C, int D, int H, int W);
  * these values; they exist to tune and to exercise multi-tile plans. */
 FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 
+/* Plan override (no counterpart in the reference): for passes whose
+ * cross-section is N1 x N2 (cross = 1 for 2D images, N1 = 1; cross = 2 for
+ * volumes), use tiles of T1 x T2 cells with S steps per halo hand-off
+ * (S in {1,2,4,8}, halo S).  S = 0 removes the override.  Used by the
+ * autotuner (fastgeodis_gb300.tune); results do not depend on it.  A plan
+ * that does not fit the device falls back to the planner's choice. */
+FG_API int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2);
+
 /* Event timing of the sweep kernels (no counterpart in the reference):
  * between fg_profile_begin() and fg_profile_end(), every pass launch is
  * bracketed by CUDA events on its stream.  fg_profile_end synchronises those

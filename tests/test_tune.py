@@ -1,0 +1,117 @@
+"""Autotuner: candidate plans respect the engine's tiling rules (CPU), pinned
+plans round-trip through the C ABI and JSON (CPU), and tuned transforms give
+the same bits as the oracle (GPU)."""
+import numpy as np
+import pytest
+import torch
+
+from fastgeodis_gb300 import _lib, tune
+
+
+@pytest.mark.parametrize("cross,N1,N2", [(1, 1, 5), (1, 1, 300), (1, 1, 2048), (2, 7, 9), (2, 128, 256),
+                                         (2, 256, 256), (2, 40, 600), (2, 2048, 8)])
+@pytest.mark.parametrize("sms", [152, 8])
+def test_candidates_follow_the_tiling_rules(cross, N1, N2, sms):
+    cands = tune.candidates(cross, N1, N2, sms)
+    if cross == 1 or N1 * N2 <= sms * 512:
+        assert cands, "a cross-section that fits the SMs has a plan"
+    assert len(set(cands)) == len(cands)
+    for S, T1, T2 in cands:
+        assert S in (4, 8)
+        t1, t2 = -(-N1 // T1), -(-N2 // T2)
+        assert t1 * t2 <= sms
+        assert 1 <= T2 <= N2 and 1 <= T1 <= max(N1, 1)
+        if cross == 1:
+            assert T1 == 1
+        K1 = S if cross == 2 and t1 > 1 else 0
+        K2 = S if t2 > 1 else 0
+        if t2 > 1:
+            assert T2 % 4 == 0 and T2 >= K2
+        if t1 > 1:
+            assert T1 >= K1
+        R1 = T1 + 2 * K1 if cross == 2 else 1
+        R2 = T2 + 2 * K2
+        assert R1 * R2 <= tune.MAX_REGION and R1 * (-(-R2 // 4)) <= tune.MAX_RUNS
+
+
+def test_pass_keys():
+    assert tune.pass_keys((5, 7)) == [(1, 1, 7), (1, 1, 5)]
+    assert tune.pass_keys((6, 6)) == [(1, 1, 6)]
+    assert tune.pass_keys((3, 4, 5)) == [(2, 4, 5), (2, 3, 5), (2, 3, 4)]
+    assert tune.pass_keys((8, 8, 8)) == [(2, 8, 8)]
+    with pytest.raises(ValueError):
+        tune.pass_keys((1, 2, 3, 4))
+
+
+def test_override_validation_and_round_trip(tmp_path):
+    L = _lib.load()
+    assert L.fg_plan_override(2, 64, 64, 3, 8, 8) == _lib.FG_ERR_INVALID_ARGUMENT  # S not a power of two <= 8
+    assert L.fg_plan_override(2, 64, 64, 4, 8, 6) == _lib.FG_ERR_INVALID_ARGUMENT  # T2 not a multiple of 4
+    assert L.fg_plan_override(3, 64, 64, 4, 8, 8) == _lib.FG_ERR_INVALID_ARGUMENT
+    res = {(2, 64, 64): (4, 8, 16, 0.5), (1, 1, 100): (8, 1, 52, 0.25), (2, 9, 9): (0, 0, 0, 0.1)}
+    path = str(tmp_path / "plans.json")
+    tune.save(res, path)
+    back = tune.load(path)
+    assert back == res
+    tune.clear((64, 64, 64))
+    tune.clear((100, 100))
+
+
+def _case(shape, C, seed):
+    rng = np.random.default_rng(seed)
+    img = rng.random((C,) + tuple(shape)).astype(np.float32)
+    m = np.ones((1,) + tuple(shape), np.float32)
+    for _ in range(3):
+        m[(0,) + tuple(int(rng.integers(0, n)) for n in shape)] = 0
+    return img, m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,C", [((300, 517), 1), ((40, 72, 64), 2), ((24, 24, 24), 1)])
+def test_every_candidate_plan_gives_the_oracle_bits(shape, C):
+    import fastgeodis_gb300 as fg
+    from golden_cases import bits_equal
+    from oracle import oracle
+
+    img, m = _case(shape, C, 11)
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    if len(shape) == 2:
+        want = oracle.geodesic2d(img, m, 1e10, 0.6, 2)
+        run = lambda: fg.generalised_geodesic2d(ti, tm, 1e10, 0.6, 2)
+    else:
+        sp = [1.5, 0.8, 1.1]
+        want = oracle.geodesic3d(img, m, sp, 1e10, 0.6, 2)
+        run = lambda: fg.generalised_geodesic3d(ti, tm, sp, 1e10, 0.6, 2)
+    L = _lib.load()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    try:
+        for key in tune.pass_keys(shape):
+            for c in tune.candidates(*key, sms):
+                _lib.check(L.fg_plan_override(*key, *c))
+                got = run()[0].cpu().numpy()
+                assert bits_equal(got, want), (key, c, np.abs(got - want).max())
+            _lib.check(L.fg_plan_override(*key, 0, 0, 0))
+        fg.check_status()
+    finally:
+        tune.clear(shape)
+
+
+@pytest.mark.gpu
+def test_autotune_pins_plans_and_keeps_results():
+    import fastgeodis_gb300 as fg
+    from golden_cases import bits_equal
+    from oracle import oracle
+
+    shape = (36, 80, 96)
+    try:
+        res = tune.autotune(shape, channels=1, lamb=0.5, iterations=1, repeats=2, max_per_step=6)
+        assert set(res) == set(tune.pass_keys(shape))
+        for S, T1, T2, ms in res.values():
+            assert ms > 0 and S in (0, 4, 8)
+        img, m = _case(shape, 1, 5)
+        got = fg.generalised_geodesic3d(torch.from_numpy(img)[None].cuda(), torch.from_numpy(m)[None].cuda(),
+                                        [1.0, 1.0, 1.0], 1e10, 0.5, 2)[0].cpu().numpy()
+        assert bits_equal(got, oracle.geodesic3d(img, m, [1.0, 1.0, 1.0], 1e10, 0.5, 2))
+        fg.check_status()
+    finally:
+        tune.clear(shape)
