@@ -25,7 +25,8 @@ FG_OP_GSF = 2
 
 # every symbol include/fastgeodis_gb300.h declares
 EXPORTED = (
-    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override", "fg_profile_begin", "fg_profile_end",
+    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override",
+    "fg_profile_begin", "fg_profile_end", "fg_profile_launch_times",
     "fg_workspace_bytes", "fg_workspace_status",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
@@ -61,6 +62,8 @@ def load():
     L.fg_profile_begin.argtypes = []
     L.fg_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
                                  ctypes.POINTER(ctypes.c_double)]
+    L.fg_profile_launch_times.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), i,
+                                          ctypes.POINTER(ctypes.c_int)]
     L.fg_set_tuning.argtypes = [i, i]
     L.fg_plan_override.argtypes = [i, i, i, i, i, i]
     L.fg_plan_override.restype = i
@@ -97,6 +100,17 @@ def profile_end():
     ms, n, vp = ctypes.c_double(), ctypes.c_int(), ctypes.c_double()
     check(load().fg_profile_end(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(vp)))
     return ms.value, n.value, vp.value
+
+
+def profile_launch_times():
+    """[(ms, steps)] of every pass launch of the window closed by profile_end()."""
+    L = load()
+    n = ctypes.c_int()
+    check(L.fg_profile_launch_times(None, None, 0, ctypes.byref(n)))
+    ms = (ctypes.c_float * max(1, n.value))()
+    st = (ctypes.c_int * max(1, n.value))()
+    check(L.fg_profile_launch_times(ms, st, n.value, ctypes.byref(n)))
+    return [(float(ms[i]), int(st[i])) for i in range(n.value)]
 
 
 def last_error() -> str:

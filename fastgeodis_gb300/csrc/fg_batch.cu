@@ -93,8 +93,8 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, 
   const void *ptrs[6] = {a.img, it.out, it.t1, M > 1 ? it.d2 : it.out, M > 1 ? it.t2 : it.t1, it.image_t};
   for (int i = 0; i < 6; i++) vec = vec && ((reinterpret_cast<uintptr_t>(ptrs[i]) & 15) == 0);
   a.vec = vec ? 1 : 0;
-  a.flags = nullptr;
-  a.flag_base = 0;
+  a.xch = nullptr;  // one tile per image: no halo exchange
+  a.epoch_base = 0;
   a.status = status;
   a.tape = nullptr;
   a.P = depth;

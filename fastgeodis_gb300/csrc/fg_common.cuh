@@ -12,8 +12,8 @@ constexpr int kThreads = 512;            // largest CTA; one thread per run of 4
 constexpr int kMaxRegion = kThreads * 4; // cells of one CTA's region (tile + halo)
 constexpr int kMaxMaps = 2;              // distance maps updated by one launch (they share the image)
 constexpr int kMaxChannels = 4;          // image channels held in registers
-constexpr int kMaxTiles = 2048;          // progress flags in a workspace
-constexpr unsigned kSpinLimit = 1u << 23; // flag polls (each an L2 round trip, ~0.3-1 us) before FG_ERR_TIMEOUT
+constexpr int kMaxTiles = 2048;          // tiles of one pass (all co-resident)
+constexpr unsigned kSpinLimit = 1u << 23; // polls of one halo word (each an L2 round trip, ~0.3-1 us) before FG_ERR_TIMEOUT
 
 // Arithmetic of one candidate.  GENERAL is the reference expression
 // (D + l_eucl*ld) + l_grad*L1.  EUCLID (l_grad == 0) and GEO (l_eucl == 0 and
@@ -45,8 +45,13 @@ struct PassArgs {
   int rowf;                       // floats per buffer position (all rows), multiple of 32
   int vec;                        // runs may use 16-byte global loads and stores
   int P;                          // steps of own inputs staged ahead (2, 4 or 8)
-  unsigned *flags;                // per-tile progress (chunks completed)
-  unsigned flag_base;
+  // Halo exchange between tiles: 64-bit words [2 parities][kMaxMaps][N1*N2],
+  // each a cell's distance bits (low half) and the epoch of the chunk whose
+  // last row it holds (high half).  One aligned 64-bit access carries both,
+  // so a reader that sees the epoch it wants also sees the value.  Chunk c
+  // (steps [c*S, (c+1)*S)) publishes epoch epoch_base + c + 1 at parity (c+1) & 1.
+  unsigned long long *xch;
+  unsigned epoch_base;
   int *status;                    // FG_ERR_TIMEOUT if a bounded wait expired
   unsigned char *tape;            // argmin tape of this pass, read layout, 1 byte per cell (TAPE variants)
 };

@@ -53,7 +53,6 @@ using namespace fgi;
 
 constexpr size_t kSmemBudget = 227 * 1024 - 1024;
 constexpr size_t kWsHeader = 256;  // status word and spare
-constexpr size_t kWsFlags = kMaxTiles * sizeof(unsigned);
 
 int fail(int code, const std::string &msg) { return set_error(code, msg.c_str()); }
 
@@ -305,32 +304,49 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
 
 struct Workspace {
   int *status;
-  unsigned *flags;
+  unsigned long long *xch;  // halo exchange words (PassArgs::xch)
+  size_t xch_bytes;
   char *base;
   size_t map_stride;  // floats between maps
 };
 
 size_t map_bytes(long long P) { return ((size_t)P * 4 + 255) & ~(size_t)255; }
 
+// Largest pass cross-section of a transform.  With D == 1 the sweep along D
+// has one step and no tiles, so a 2D image and a one-slice volume both need
+// max(H, W).
+long long max_cross_cells(int D, int H, int W) {
+  if (D <= 1) return std::max(H, W);
+  return std::max({(long long)H * W, (long long)D * W, (long long)D * H});
+}
+
+// exchange words: 2 parities x kMaxMaps maps x the largest cross-section
+size_t xch_bytes(int D, int H, int W) {
+  return ((size_t)2 * kMaxMaps * max_cross_cells(D, H, W) * 8 + 255) & ~(size_t)255;
+}
+
 // extra maps in the original layout (beyond `out`), maps in the transposed
 // layout, and the transposed image copy
 int extra_maps(int op) { return op == FG_OP_PLAIN ? 0 : (op == FG_OP_SIGNED ? 1 : 4); }
 int t_maps(int op) { return op == FG_OP_PLAIN ? 1 : (op == FG_OP_SIGNED ? 2 : 4); }
 
-size_t workspace_bytes(int op, int C, long long P) {
-  return kWsHeader + kWsFlags + (size_t)(extra_maps(op) + t_maps(op)) * map_bytes(P) + map_bytes(P * C);
+size_t workspace_bytes(int op, int C, int D, int H, int W) {
+  const long long P = (long long)D * H * W;
+  return kWsHeader + xch_bytes(D, H, W) + (size_t)(extra_maps(op) + t_maps(op)) * map_bytes(P) + map_bytes(P * C);
 }
 
-int bind_workspace(void *ws, size_t bytes, int op, int C, long long P, Workspace *w) {
+int bind_workspace(void *ws, size_t bytes, int op, int C, int D, int H, int W, Workspace *w) {
   if (ws == nullptr) return fail(FG_ERR_WORKSPACE, "workspace pointer is null");
   if ((reinterpret_cast<uintptr_t>(ws) & 255) != 0) return fail(FG_ERR_WORKSPACE, "workspace must be 256-byte aligned");
-  size_t need = workspace_bytes(op, C, P);
+  const long long P = (long long)D * H * W;
+  size_t need = workspace_bytes(op, C, D, H, W);
   if (bytes < need)
     return fail(FG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes, got " + std::to_string(bytes));
   char *base = static_cast<char *>(ws);
   w->status = reinterpret_cast<int *>(base);
-  w->flags = reinterpret_cast<unsigned *>(base + kWsHeader);
-  w->base = base + kWsHeader + kWsFlags;
+  w->xch = reinterpret_cast<unsigned long long *>(base + kWsHeader);
+  w->xch_bytes = xch_bytes(D, H, W);
+  w->base = base + kWsHeader + w->xch_bytes;
   w->map_stride = map_bytes(P) / 4;
   return FG_OK;
 }
@@ -361,6 +377,9 @@ struct ProfileState {
   bool on = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
   std::vector<long long> vp;  // cells x maps updated by each recorded launch
+  std::vector<int> steps;     // pass length of each recorded launch
+  std::vector<float> last_ms; // per-launch times of the last closed window
+  std::vector<int> last_steps;
 };
 ProfileState &profile() {
   static ProfileState p;
@@ -392,6 +411,7 @@ int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bo
     std::lock_guard<std::mutex> g(ps.mu);
     ps.ev.emplace_back(e0, e1);
     ps.vp.push_back((long long)a.L * a.N1 * a.N2 * M);
+    ps.steps.push_back(a.L);
   }
   return FG_OK;
 }
@@ -480,8 +500,8 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
         const bool to_r = A.transposed && dir < 0;
         const bool wt = to_t || to_r;
         if (A.L <= 1 && !wt) continue;
-        if (*launch_counter >= 0xFFFFu) {  // progress values would wrap: start a fresh flag epoch
-          FG_CUDA(cudaMemsetAsync(w.flags, 0, kWsFlags, s));
+        if (*launch_counter >= 0xFFFFu) {  // epochs would repeat: clear the exchange words
+          FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
           *launch_counter = 0;
         }
         for (int m0 = 0; m0 < ms.M; m0 += kMaxMaps) {
@@ -536,8 +556,8 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
                   (reinterpret_cast<uintptr_t>(a.ddst[m]) & 15) == 0;
           a.vec = vec ? 1 : 0;
           a.P = p.P;
-          a.flags = w.flags;
-          a.flag_base = (*launch_counter) << 16;
+          a.xch = w.xch;
+          a.epoch_base = (*launch_counter) << 16;  // chunk epochs of this launch: base + 1 ... base + L/S
           a.status = w.status;
           (*launch_counter)++;
           int rc = launch_pass(a, p, cross, M, mode, wt, s);
@@ -566,7 +586,7 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   if (rc != FG_OK) return rc;
   if (g.P == 0) return FG_OK;
   Workspace w;
-  rc = bind_workspace(ws, ws_bytes, op, g.C, g.P, &w);
+  rc = bind_workspace(ws, ws_bytes, op, g.C, g.is3d ? g.D : 1, g.H, g.W, &w);
   if (rc != FG_OK) return rc;
   const long long P = g.P;
   const size_t ms_ = w.map_stride;
@@ -575,7 +595,8 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   float *tb = maps + extra_maps(op) * ms_;
   float *xt[4] = {tb, tb + ms_, tb + 2 * ms_, tb + 3 * ms_};          // transposed-layout maps
   float *img_t = tb + t_maps(op) * ms_;
-  FG_CUDA(cudaMemsetAsync(w.flags, 0, kWsFlags, s));
+  // epoch 0 is never wanted; earlier calls' words must not match this call's epochs
+  FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
   unsigned counter = 0;
   if (Cm > 1) {
     long long n = (long long)(Cm - 1) * P;
@@ -670,6 +691,7 @@ int fg_profile_begin(void) {
   }
   ps.ev.clear();
   ps.vp.clear();
+  ps.steps.clear();
   ps.on = true;
   return FG_OK;
 }
@@ -680,12 +702,15 @@ int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_passes) {
   ps.on = false;
   double total = 0.0, vps = 0.0;
   int rc = FG_OK;
+  ps.last_ms.clear();
+  ps.last_steps = ps.steps;
   for (size_t i = 0; i < ps.ev.size(); i++) {
     float ms = 0.0f;
     if (cudaEventSynchronize(ps.ev[i].second) != cudaSuccess ||
         cudaEventElapsedTime(&ms, ps.ev[i].first, ps.ev[i].second) != cudaSuccess)
       rc = fail(FG_ERR_CUDA, "event timing failed");
     total += ms;
+    ps.last_ms.push_back(ms);
     vps += (double)ps.vp[i];
     cudaEventDestroy(ps.ev[i].first);
     cudaEventDestroy(ps.ev[i].second);
@@ -695,7 +720,20 @@ int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_passes) {
   if (voxel_passes) *voxel_passes = vps;
   ps.ev.clear();
   ps.vp.clear();
+  ps.steps.clear();
   return rc;
+}
+
+int fg_profile_launch_times(float *ms, int *steps, int cap, int *n) {
+  ProfileState &ps = profile();
+  std::lock_guard<std::mutex> g(ps.mu);
+  const int k = (int)ps.last_ms.size();
+  for (int i = 0; i < k && i < cap; i++) {
+    if (ms) ms[i] = ps.last_ms[i];
+    if (steps) steps[i] = ps.last_steps[i];
+  }
+  if (n) *n = k;
+  return FG_OK;
 }
 
 int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2) {
@@ -723,7 +761,7 @@ int fg_set_tuning(int max_region_cells, int max_tiles) {
 
 size_t fg_workspace_bytes(int op, int C, int D, int H, int W) {
   if (op < FG_OP_PLAIN || op > FG_OP_GSF || C < 1 || D < 0 || H < 0 || W < 0) return 0;
-  return workspace_bytes(op, C, (long long)D * H * W);
+  return workspace_bytes(op, C, D, H, W);
 }
 
 int fg_workspace_status(void *workspace, void *stream) {

@@ -6,14 +6,14 @@
 // allocator and forbids allocation while its work executes (plugin or
 // operator callbacks, real-time loops that must not block on an allocator),
 // or plain C callers that have no device allocator at all.  They pass their
-// inputs and outputs and nothing else; the sweep kernels' scratch (progress
-// flags, the transposed distance map and the transposed image copy) comes
+// inputs and outputs and nothing else; the sweep kernels' scratch (halo
+// exchange words, the transposed distance map and the transposed image copy) comes
 // from `g_noalloc_scratch`, 16 MiB that every GPU loading the library holds
 // until the process exits.
 //
 // Rules of use:
 //   * Every call shares the one array and leaves its contents behind.  The
-//     parts that must start at zero (status word, progress flags) are cleared
+//     parts that must start at zero (status word, halo exchange words) are cleared
 //     by each call on its stream.  Calls whose GPU work overlaps (different
 //     streams, or different host threads without ordering) race on the array
 //     and give wrong results: order them on one stream.
@@ -52,7 +52,7 @@ extern "C" FG_API int fg_generalised_geodesic2d_noalloc(const float *image, int 
   if (need > kNoAllocScratchBytes) {
     std::string msg = "fg_generalised_geodesic2d_noalloc: this size needs " + std::to_string(need) +
                       " bytes of scratch; the fixed scratch array holds " + std::to_string(kNoAllocScratchBytes) +
-                      " bytes ((C + 1) * H * W * 4 plus about 9 KiB must fit)";
+                      " bytes ((C + 1) * H * W * 4 plus 32 * max(H, W) plus about 1 KiB must fit)";
     return fgi::set_error(FG_ERR_UNSUPPORTED, msg.c_str());
   }
   void *ws = nullptr;
@@ -66,7 +66,7 @@ extern "C" FG_API int fg_generalised_geodesic2d_noalloc(const float *image, int 
     }
     ws = g_noalloc_addr[dev];
   }
-  // the status word must start at zero (the progress flags are cleared by the transform itself)
+  // the status word must start at zero (the exchange words are cleared by the transform itself)
   e = cudaMemsetAsync(ws, 0, sizeof(int), static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return fgi::set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   return fg_generalised_geodesic2d(image, C, H, W, mask, Cm, out, v, l_grad, l_eucl, iterations, ws,

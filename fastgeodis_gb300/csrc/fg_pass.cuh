@@ -13,9 +13,12 @@
 //     layout allows).  Shared memory only holds the rows its neighbours read:
 //     the previous step's distances and image values.  One barrier per step.
 //   * With several tiles, the halo lets a CTA run S <= K steps on its own.
-//     Every S steps it replaces its halo cells of the last row by the exact
-//     values its neighbours published (per-tile progress flags,
-//     release/acquire, bounded waits).  Halo cells are never written back.
+//     At the last step of every chunk of S steps a CTA publishes its own
+//     cells as 64-bit exchange words (value and chunk epoch in one atomic
+//     access); at the start of the next chunk it replaces its halo cells of
+//     that row by the words of its neighbours, re-polling (bounded) only words
+//     that do not yet carry the wanted epoch.  One L2 round trip per hand-off,
+//     no fences, no flags.  Halo cells are never written back.
 //   * Layout: the swept axis is never the contiguous one in the read layout.
 //     The pass that hands over to a sweep along the contiguous axis writes
 //     its result transposed (step innermost), through an S-row shared ring
@@ -29,13 +32,13 @@
 
 namespace fgi {
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];\n" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_word(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ int ld_status(const int *p) {
   int v;
@@ -157,21 +160,10 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const bool active = valid != 0;
   const bool full = valid == 0xFu && a.vec;
   const unsigned halo = valid & ~own;
-  int nbr = -1;  // neighbour tile polled by this thread
-  if (tid < 8) {
-    int d1, d2;
-    if (CROSS == 2) {
-      int k = tid < 4 ? tid : tid + 1;
-      d1 = k / 3 - 1;
-      d2 = k % 3 - 1;
-    } else {
-      d1 = 0;
-      d2 = tid == 0 ? -1 : 1;
-    }
-    int n1 = ti1 + d1, n2 = ti2 + d2;
-    if ((CROSS == 2 || tid < 2) && n1 >= 0 && n1 < a.tiles1 && n2 >= 0 && n2 < a.tiles2) nbr = n1 * a.tiles2 + n2;
-  }
   const bool has_nb = a.tiles1 * a.tiles2 > 1;
+  // exchange words of this thread's run (cell (g1, g20) of the cross-section), parity 0, map 0
+  const long long xplane = (long long)a.N1 * a.N2;
+  unsigned long long *const xrun = has_nb ? a.xch + (long long)g1 * a.N2 + g20 : nullptr;
   __syncthreads();
 
   // running offsets: read layout of the next step to prefetch, write layout of the current step
@@ -210,20 +202,6 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     rnext += rstep;
   };
 
-  auto wait_neighbours = [&](unsigned target) {
-    if (nbr >= 0) {
-      unsigned spins = 0;
-      while ((int)(ld_acquire(a.flags + nbr) - target) < 0) {
-        if (++spins > kSpinLimit || ((spins & 1023u) == 0 && ld_status(a.status) != 0)) {
-          atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
-          break;
-        }
-      }
-      __threadfence();
-    }
-    __syncthreads();
-  };
-
   for (int k = 0; k < P; k++) {
     if (k < L) stage(k);
     else cp_async_commit();
@@ -233,15 +211,31 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     const int slot = t & (P - 1);
     // exact halo values of the previous row from the neighbour tiles
     if (has_nb && t > 0 && (t & (S - 1)) == 0) {
-      wait_neighbours(a.flag_base + (unsigned)(t >> lgS));
       if (halo) {
-        const long long so = wcur - wstep;  // write offset of step t-1
+        const unsigned want = a.epoch_base + (unsigned)(t >> lgS);
+        const unsigned long long *xw = xrun + (long long)((t >> lgS) & 1) * kMaxMaps * xplane;
         float *pr = dring + ((t - 1) & (SR - 1)) * M * rowf + cb;
+        unsigned long long wd[M][4];
 #pragma unroll
         for (int m = 0; m < M; m++)
 #pragma unroll
           for (int i = 0; i < 4; i++)
-            if (halo & (1u << i)) pr[m * rowf + i] = __ldcg(a.ddst[m] + so + i * a.wst2);
+            if (halo & (1u << i)) wd[m][i] = ld_word(xw + m * xplane + i);  // all in flight at once
+#pragma unroll
+        for (int m = 0; m < M; m++)
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+            if (halo & (1u << i)) {
+              unsigned spins = 0;
+              while ((unsigned)(wd[m][i] >> 32) != want) {
+                if (++spins > kSpinLimit || ((spins & 1023u) == 0 && ld_status(a.status) != 0)) {
+                  atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
+                  break;
+                }
+                wd[m][i] = ld_word(xw + m * xplane + i);
+              }
+              pr[m * rowf + i] = __uint_as_float((unsigned)wd[m][i]);
+            }
       }
       __syncthreads();
     }
@@ -343,6 +337,16 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
           out[m].w = (valid & 8u) ? best[m][3] : qnan;
         }
       }
+      if (has_nb && own && ((t + 1) & (S - 1)) == 0 && t + 1 < L) {
+        // last step of a chunk: publish the own cells for the neighbours' halos
+        const unsigned long long ep = (unsigned long long)(a.epoch_base + (unsigned)((t + 1) >> lgS)) << 32;
+        unsigned long long *xw = xrun + (long long)(((t + 1) >> lgS) & 1) * kMaxMaps * xplane;
+#pragma unroll
+        for (int m = 0; m < M; m++)
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+            if (own & (1u << i)) st_word(xw + m * xplane + i, ep | __float_as_uint(f4get(out[m], i)));
+      }
       float *dc = dring + (t & (SR - 1)) * M * rowf + cb;
 #pragma unroll
       for (int m = 0; m < M; m++) *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
@@ -386,10 +390,6 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
           }
       }
       __syncthreads();
-    }
-    if (has_nb && chunk_end && tid == 0) {
-      __threadfence();
-      st_release(a.flags + tile, a.flag_base + (unsigned)(t >> lgS) + 1u);
     }
   }
   cp_async_wait<0>();

@@ -81,6 +81,10 @@ FG_API int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2);
  * CUDA graph capture. */
 FG_API int fg_profile_begin(void);
 FG_API int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_passes);
+/* Per-launch times of the window closed by the last fg_profile_end, in launch
+ * order: up to `cap` entries of ms and of steps swept (the pass length);
+ * *n receives the number recorded. */
+FG_API int fg_profile_launch_times(float *ms, int *steps, int cap, int *n);
 
 /* Reads (and clears) the device status word of a workspace after
  * synchronising `stream`: FG_OK, or FG_ERR_TIMEOUT if a kernel gave up. */
@@ -202,8 +206,8 @@ FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int m
  * allocator and forbids allocation during execution, or C callers without a
  * device allocator.  It takes no workspace: its scratch is a fixed 16 MiB
  * device array inside this library, held by every GPU that loads the library
- * until the process exits.  Limit: (C + 1) * H * W * 4 bytes plus about 9 KiB
- * must fit in 16 MiB (for example C = 1 up to about 2 million pixels);
+ * until the process exits.  Limit: (C + 1) * H * W * 4 bytes plus
+ * 32 * max(H, W) bytes plus about 1 KiB must fit in 16 MiB (for example C = 1 up to about 2 million pixels);
  * larger sizes return FG_ERR_UNSUPPORTED.  All calls share the array: calls
  * whose GPU work overlaps race and give wrong results, so order them on one
  * stream.  The first call on a device looks up the array's address there
