@@ -177,10 +177,16 @@ def _run(kind: str, image, mask, v, lamb, iterations, spacing=None, theta=None):
         else:  # pragma: no cover
             raise AssertionError(kind)
         _lib.check(rc)
+        if host:
+            # result into page-locked host memory on the call's stream; the
+            # status read below synchronises that stream, so it is complete
+            # when the call returns
+            res = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+            res.copy_(out, non_blocking=True)
         if host or _CHECK_EVERY_CALL:
             _lib.check(L.fg_workspace_status(ptr(ws), sh))
         if host:
-            return out.cpu()
+            return res
         return out
 
 

@@ -25,7 +25,7 @@ FG_OP_GSF = 2
 
 # every symbol include/fastgeodis_gb300.h declares
 EXPORTED = (
-    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override",
+    "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override", "fg_plan_describe",
     "fg_profile_begin", "fg_profile_end", "fg_profile_launch_times",
     "fg_workspace_bytes", "fg_workspace_status",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
@@ -66,6 +66,7 @@ def load():
                                           ctypes.POINTER(ctypes.c_int)]
     L.fg_set_tuning.argtypes = [i, i]
     L.fg_plan_override.argtypes = [i, i, i, i, i, i]
+    L.fg_plan_describe.argtypes = [i, i, i, i, i, i, i, i, ctypes.POINTER(ctypes.c_int)]
     L.fg_plan_override.restype = i
     L.fg_set_tuning.restype = i
     L.fg_workspace_status.argtypes = [vp, vp]
@@ -111,6 +112,16 @@ def profile_launch_times():
     st = (ctypes.c_int * max(1, n.value))()
     check(L.fg_profile_launch_times(ms, st, n.value, ctypes.byref(n)))
     return [(float(ms[i]), int(st[i])) for i in range(n.value)]
+
+
+PLAN_FIELDS = ("S", "T1", "T2", "K1", "K2", "tiles1", "tiles2", "threads", "depth", "smem")
+
+
+def plan_describe(cross, N1, N2, C=1, maps=1, mode=0, transposed_write=False, sms=152) -> dict:
+    """The engine's plan for one pass (see fg_plan_describe); needs no GPU."""
+    out = (ctypes.c_int * len(PLAN_FIELDS))()
+    check(load().fg_plan_describe(cross, N1, N2, C, maps, mode, int(transposed_write), sms, out))
+    return dict(zip(PLAN_FIELDS, list(out)))
 
 
 def last_error() -> str:

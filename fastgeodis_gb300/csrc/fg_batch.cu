@@ -88,7 +88,7 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, 
   a.T1 = 1, a.T2 = N2, a.K1 = 0, a.K2 = 0, a.tiles1 = 1, a.tiles2 = 1;
   a.S = S;
   a.B2 = ((N2 + 3) & ~3) + 8;
-  a.rowf = a.B2;
+  a.rowf = ring_pitch(a.B2);
   bool vec = (H % 4 == 0) && (W % 4 == 0);
   const void *ptrs[6] = {a.img, it.out, it.t1, M > 1 ? it.d2 : it.out, M > 1 ? it.t2 : it.t1, it.image_t};
   for (int i = 0; i < 6; i++) vec = vec && ((reinterpret_cast<uintptr_t>(ptrs[i]) & 15) == 0);
@@ -166,7 +166,7 @@ size_t batch_smem(int max_C, int max_extent, int is_signed, int S) {
   const int M = is_signed ? 2 : 1;
   const int nch = pass_nch(max_C == 1 ? 1 : 0, MODE_GENERAL);
   const int depth = pass_depth(nch, M);
-  const int rowf = ((max_extent + 3) & ~3) + 8;  // one row: 4-cell apron, runs of 4, apron
+  const int rowf = ring_pitch(((max_extent + 3) & ~3) + 8);  // one row: 4-cell apron, runs of 4, apron
   // the largest pass: a transposed-writing one (S distance rows) over the longest side
   const size_t pass = (size_t)(S * M + 2 * max_C) * rowf * 4 + (size_t)depth * (M + max_C) * kThreads * 16 +
                       (size_t)max_extent * 8 + 64;

@@ -42,7 +42,7 @@ struct PassArgs {
   int tiles1, tiles2;
   int S;                          // steps per chunk: halo hand-off and transposed-flush period
   int B2;                         // floats per buffer row (4-cell left apron, runs of 4, right apron)
-  int rowf;                       // floats per buffer position (all rows), multiple of 32
+  int rowf;                       // floats per ring row (ring_pitch: 4 mod 32)
   int vec;                        // runs may use 16-byte global loads and stores
   int P;                          // steps of own inputs staged ahead (2, 4 or 8)
   // Halo exchange between tiles: 64-bit words [2 parities][kMaxMaps][N1*N2],
@@ -65,6 +65,13 @@ struct LaunchCfg {
   int threads;
   size_t smem;
 };
+
+// Pitch of the shared rings' rows: at least `floats`, a multiple of 4 (float4
+// access) and 4 mod 32, so that consecutive rows start 4 banks apart and the
+// transposed flush (one cell read from S consecutive rows) is conflict-free.
+__host__ __device__ constexpr int ring_pitch(int floats) {
+  return ((floats + 3) & ~3) + (36 - (((floats + 3) & ~3) % 32)) % 32;
+}
 
 // Shared-memory bytes of a pass kernel for a region of R1 x R2 cells.
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2, int *rowf,

@@ -190,10 +190,39 @@ struct Plan {
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
 std::atomic<int> g_tune_tiles{0};            // cap on tiles per pass (0: the SM count)
 
-// Cost model of one step of a pass in SM cycles: the slower of the step's
-// dependency chain and its issue time per 4-cell run, plus the neighbour
-// hand-off of a multi-tile plan spread over the S steps of a chunk.
-constexpr double kStepLatency = 250.0, kCyclesPerRun = 1.2, kHandoff = 3000.0;
+// Cost model of one step of a pass in SM cycles, fitted to single-tile and
+// multi-tile step times measured on GB300 (256^3 and 64^2 x 256 sweeps): a
+// fixed dependency chain, issue time per 4-cell run of the step's cone
+// (averaged over a chunk, whole warps), and the neighbour hand-off of a
+// multi-tile plan (an L2 round trip, longer with more tiles) spread over the
+// S steps of a chunk.
+constexpr double kStepBase = 620.0, kCyclesPerRunGeneral = 2.7, kCyclesPerRunEuclid = 1.4;
+constexpr double kHandoffBase = 2000.0, kHandoffPerTile = 8.0;
+
+// Runs computed per step, averaged over the S steps of a chunk and rounded up
+// to whole warps: the kernel orders runs innermost first and skips, at chunk
+// step j, the runs whose cone distance is <= j (run_cone_dist in the kernel).
+double cone_avg_runs(int cross, int R1, int R2, int K1, int K2, int S) {
+  const int rpr = (R2 + 3) / 4, nruns = R1 * rpr;
+  int count[9] = {0};  // runs by cone distance 0 .. S (S <= 8)
+  for (int q = 0; q < nruns; q++) {
+    const int r1 = q / rpr, u = q % rpr;
+    const int d1 = (cross == 2 && K1 > 0) ? std::min(r1, R1 - 1 - r1) : S;
+    int d = -1;
+    for (int i = 0; i < 4; i++) {
+      const int r2 = 4 * u + i;
+      if (r2 < R2) d = std::max(d, std::min(d1, K2 > 0 ? std::min(r2, R2 - 1 - r2) : S));
+    }
+    count[std::min(d, S)]++;
+  }
+  double sum = 0.0;
+  int active = nruns;  // runs with distance > j
+  for (int j = 0; j < S; j++) {
+    active -= count[j];
+    sum += (double)((active + 31) / 32 * 32);
+  }
+  return sum / S;
+}
 
 // Plan overrides set by the autotuner (fg_plan_override): cross-section shape -> (S, T1, T2).
 std::mutex g_override_mu;
@@ -239,8 +268,13 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     }
     (void)nown;
     if (sm > kSmemBudget) return -1;
-    double cost = std::max(kStepLatency, kCyclesPerRun * runs) + (multi ? kHandoff / S : 0.0);
-    if (sm > kSmemBudget / 2) cost *= 1.05;
+    // a 2D step has 3 candidates per cell instead of 9
+    const double per_run = (mode == MODE_EUCLID ? kCyclesPerRunEuclid
+                                                : (kCyclesPerRunGeneral + 0.8 * (C - 1)) * (M == 2 ? 1.8 : 1.0)) /
+                           (cross == 2 ? 1.0 : 3.0);
+    const double avg_runs = multi ? cone_avg_runs(cross, R1, R2, K1, K2, S) : (double)((runs + 31) / 32 * 32);
+    double cost = kStepBase + per_run * avg_runs + (multi ? (kHandoffBase + kHandoffPerTile * t1 * t2) / S : 0.0);
+    if (sm > kSmemBudget / 2) cost *= 1.05;  // one CTA per SM: no room for a concurrent transform
     if (!found || cost < best_cost - 1e-9) {
       int nt = std::max(32, std::min(kThreads, (runs + 31) / 32 * 32));
       best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm};
@@ -664,7 +698,7 @@ size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1
                        int *nown_max, int depth) {
   const int ci = mode == MODE_EUCLID ? 0 : C;  // image arrays staged
   const int B1 = cross == 2 ? R1 + 2 : 1, B2 = ((R2 + 3) & ~3) + 8;
-  const int rowf = (B1 * B2 + 3) & ~3;
+  const int rowf = ring_pitch(B1 * B2);
   const int SR = wt ? S : 2;
   const int nt = std::max(32, (R1 * ((R2 + 3) / 4) + 31) / 32 * 32);
   *B2o = B2;
@@ -748,6 +782,20 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2) {
     g_overrides[key] = std::make_tuple(S, T1, T2);
   }
   g_plan_epoch.fetch_add(1);
+  return FG_OK;
+}
+
+int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int transposed_write, int sms,
+                     int *plan) {
+  if (cross < 1 || cross > 2 || N1 < 1 || N2 < 1 || C < 0 || maps < 1 || maps > kMaxMaps || mode < 0 || mode > 2 ||
+      sms < 1 || !plan)
+    return fail(FG_ERR_INVALID_ARGUMENT, "plan query: bad arguments");
+  Plan p;
+  const int c = mode == MODE_EUCLID ? 0 : C;
+  if (!make_plan(cross, N1, N2, c, maps, mode, transposed_write != 0, std::min(sms, kMaxTiles), &p))
+    return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
+  const int v[10] = {p.S, p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem};
+  for (int i = 0; i < 10; i++) plan[i] = v[i];
   return FG_OK;
 }
 

@@ -78,6 +78,54 @@ __device__ __forceinline__ void f4set(float4 &v, int i, float x) {
   else v.w = x;
 }
 
+// min of three (PTX min.f32 with three inputs, sm_100+): NaN inputs are
+// ignored as by fminf, and the minimum of a set does not depend on the order
+// it is taken in, so folding candidates three at a time gives fminf's bits.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;\n" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// Cone of a chunk.  After a hand-off every cell of the last row is exact;
+// at chunk step j (0 <= j < S) only cells whose distance to the region's
+// halo boundary exceeds j are ever read again before the next hand-off (own
+// cells are at distance >= K = S).  Distance of run q (4 cells along cross
+// dimension 2), capped at S; -1 for a run outside the region.
+__device__ __forceinline__ int run_cone_dist(int q, int rpr, int R1, int R2, int K1, int K2, int S) {
+  const int r1 = q / rpr, u = q - r1 * rpr;
+  if (r1 >= R1) return -1;
+  const int d1 = K1 > 0 ? min(r1, R1 - 1 - r1) : S;
+  int d = -1;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int r2 = 4 * u + i;
+    if (r2 < R2) d = max(d, min(d1, K2 > 0 ? min(r2, R2 - 1 - r2) : S));
+  }
+  return min(d, S);
+}
+
+// Stable counting sort of the CTA's threads by key (0 .. nkeys-1): returns
+// this thread's position.  `scratch` holds nwarps * nkeys ints.  Ends with a
+// barrier after its last shared-memory read.
+__device__ __forceinline__ int cta_sort_position(int key, int nkeys, int *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  unsigned mine = 0;
+  for (int b = 0; b < nkeys; b++) {
+    const unsigned bal = __ballot_sync(0xffffffffu, key == b);
+    if (key == b) mine = bal;
+    if (lane == 0) scratch[warp * nkeys + b] = __popc(bal);
+  }
+  __syncthreads();
+  int pos = __popc(mine & ((1u << lane) - 1u));
+  for (int w = 0; w < nwarps; w++) {
+    for (int b = 0; b < key; b++) pos += scratch[w * nkeys + b];
+    if (w < warp) pos += scratch[w * nkeys + key];
+  }
+  __syncthreads();
+  return pos;
+}
+
 // channels staged per step and the prefetch depth (steps) of a kernel variant
 __host__ __device__ constexpr int pass_nch(int ct, int mode) {
   return mode == MODE_EUCLID ? 0 : (ct == 0 ? kMaxChannels : ct);
@@ -132,6 +180,21 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   int2 *otab = reinterpret_cast<int2 *>(oring + P * AR * NT);  // own cells (transposed flush)
 
   // --- set-up ---
+  const bool has_nb = a.tiles1 * a.tiles2 > 1;
+  const int rpr = (R2 + 3) >> 2;
+  // run of this thread: with neighbours, runs ordered innermost first, so
+  // the runs outside a step's cone are whole trailing warps
+  int qrun = tid, cdist = S;
+  if (has_nb) {
+    int *scr = reinterpret_cast<int *>(sm);  // nwarps * (S + 2) counters, then NT positions
+    int *perm = scr + nwarps * (S + 2);
+    const int key = S - run_cone_dist(tid, rpr, R1, R2, a.K1, a.K2, S);  // 0 .. S + 1
+    perm[cta_sort_position(key, S + 2, scr)] = tid;
+    __syncthreads();
+    qrun = perm[tid];
+    cdist = run_cone_dist(qrun, rpr, R1, R2, a.K1, a.K2, S);
+    __syncthreads();
+  }
   for (int i = tid; i < (SR * M + 2 * C) * rowf + P * AR * NT * 4; i += NT) sm[i] = qnan;
   int nown = 0;
   if (WT) {
@@ -143,8 +206,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
       otab[i] = make_int2((o1 + A1) * B2 + 4 + o2, (int)g);
     }
   }
-  const int rpr = (R2 + 3) >> 2;
-  const int r1 = tid / rpr, u = tid - (tid / rpr) * rpr;
+  const int r1 = qrun / rpr, u = qrun - (qrun / rpr) * rpr;
   const int g1 = rs1 + r1, g20 = rs2 + 4 * u;
   const int cb = (r1 + A1) * B2 + 4 + 4 * u;
   unsigned valid = 0, own = 0;
@@ -160,7 +222,6 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const bool active = valid != 0;
   const bool full = valid == 0xFu && a.vec;
   const unsigned halo = valid & ~own;
-  const bool has_nb = a.tiles1 * a.tiles2 > 1;
   // exchange words of this thread's run (cell (g1, g20) of the cross-section), parity 0, map 0
   const long long xplane = (long long)a.N1 * a.N2;
   unsigned long long *const xrun = has_nb ? a.xch + (long long)g1 * a.N2 + g20 : nullptr;
@@ -175,13 +236,19 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   long long rcur = r0;   // read offset of the current step
   long long wcur = w0;   // write offset of the current step
 
-  // stage the own inputs of the next step into ring slot `slot` (one commit group per step)
-  auto stage = [&](int slot) {
-    if (active) {
+  // stage the own inputs of step `step` into ring slot `slot` (one commit group per step)
+  // A run outside a step's cone still needs its image values at a chunk's
+  // last step: the next chunk's first step reads the whole previous row of
+  // the image (the exchange supplies only the distances).
+  auto stage = [&](int slot, int step) {
+    const int js = step & (S - 1);
+    const bool sd = active && cdist > js;           // distances and image
+    if (sd || (active && js == S - 1)) {            // image
       float4 *dst = oring + slot * AR * NT + tid;
       if (full) {
 #pragma unroll
-        for (int m = 0; m < M; m++) cp_async16(dst + m * NT, a.dsrc[m] + rnext);
+        for (int m = 0; m < M; m++)
+          if (sd) cp_async16(dst + m * NT, a.dsrc[m] + rnext);
 #pragma unroll
         for (int c = 0; c < NCH; c++)
           if (c < C) cp_async16(dst + (M + c) * NT, a.img + c * a.img_cs + rnext);
@@ -190,7 +257,8 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         for (int i = 0; i < 4; i++) {
           if (valid & (1u << i)) {
 #pragma unroll
-            for (int m = 0; m < M; m++) cp_async4(reinterpret_cast<float *>(dst + m * NT) + i, a.dsrc[m] + rnext + i);
+            for (int m = 0; m < M; m++)
+              if (sd) cp_async4(reinterpret_cast<float *>(dst + m * NT) + i, a.dsrc[m] + rnext + i);
 #pragma unroll
             for (int c = 0; c < NCH; c++)
               if (c < C) cp_async4(reinterpret_cast<float *>(dst + (M + c) * NT) + i, a.img + c * a.img_cs + rnext + i);
@@ -203,7 +271,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   };
 
   for (int k = 0; k < P; k++) {
-    if (k < L) stage(k);
+    if (k < L) stage(k, k);
     else cp_async_commit();
   }
 
@@ -243,7 +311,8 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     if (P == 8) cp_async_wait<7>();
     else if (P == 4) cp_async_wait<3>();
     else cp_async_wait<1>();
-    if (active) {
+    const int jstep = t & (S - 1);  // step within the chunk
+    if (active && cdist > jstep) {  // in this step's cone
       const float4 *mine = oring + slot * AR * NT + tid;
       float4 dold[M], icur[NCHR];
 #pragma unroll
@@ -258,7 +327,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
       } else {
         const float *dp0 = dring + ((t - 1) & (SR - 1)) * M * rowf;
         const float *ip0 = iring + ((t - 1) & 1) * C * rowf;
-        float best[M][4];
+        float best[M][4], pend[M][4];  // pend: a candidate of row 0 waiting for row 1's fold
         unsigned code[4] = {kTapeSelf, kTapeSelf, kTapeSelf, kTapeSelf};  // TAPE: argmin of map 0
 #pragma unroll
         for (int m = 0; m < M; m++)
@@ -284,6 +353,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
             float4 v = *reinterpret_cast<const float4 *>(q);
             dp[m][0] = q[-1], dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = q[4];
           }
+          float cand3[M][4][3];  // this row's three candidates per map and cell
 #pragma unroll
           for (int d2 = -1; d2 <= 1; d2++) {
             const int n = CROSS == 2 ? (d1 + 1) * 3 + (d2 + 1) : d2 + 1;
@@ -311,9 +381,26 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
                 if (TAPE && m == 0) {
                   // same value as fminf for the non-NaN current distance of an in-image cell
                   if (cand < best[m][i]) best[m][i] = cand, code[i] = 1 + n;
-                } else {
-                  best[m][i] = fminf(best[m][i], cand);
                 }
+                cand3[m][i][d2 + 1] = cand;
+              }
+            }
+          }
+          // fold the row into the running minimum, three values per min:
+          // old + 9 candidates (3D) in 4 three-way mins and one two-way min
+#pragma unroll
+          for (int m = 0; m < M; m++) {
+            if (TAPE && m == 0) continue;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+              const float c0 = cand3[m][i][0], c1 = cand3[m][i][1], c2 = cand3[m][i][2];
+              if (NR == 1 || r == 2) {
+                best[m][i] = fminf(fmin3(best[m][i], c0, c1), c2);
+              } else if (r == 0) {
+                best[m][i] = fmin3(best[m][i], c0, c1);
+                pend[m][i] = c2;
+              } else {
+                best[m][i] = fmin3(fmin3(best[m][i], pend[m][i], c0), c1, c2);
               }
             }
           }
@@ -366,9 +453,16 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
           }
         }
       }
+    } else if (active && jstep == S - 1) {
+      // outside the cone at a chunk's last step: pass the image values on
+      const float4 *mine = oring + slot * AR * NT + tid;
+      float *ic = iring + (t & 1) * C * rowf + cb;
+#pragma unroll
+      for (int c = 0; c < NCH; c++)
+        if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = mine[(M + c) * NT];
     }
     // the slot's values are consumed (they are in registers): refill it with step t+P
-    if (t + P < L) stage(slot);
+    if (t + P < L) stage(slot, t + P);
     else cp_async_commit();
     wcur += wstep;
     rcur += rstep;
@@ -395,8 +489,16 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   cp_async_wait<0>();
 }
 
+// Register budget of a variant.  Volume variants with one channel and one
+// map fit in 64 registers without spills, so two CTAs of up to 512 threads
+// share an SM (concurrent transforms on other streams then fill each other's
+// stalls).  The others keep up to 128: row sweeps (2D) are a few CTAs whose
+// per-step chain wants every register of ILP.
+template <int CROSS, int CT, int M>
+constexpr int pass_reg_cap() { return (CROSS == 2 && CT == 1 && M == 1) ? 64 : 128; }
+
 template <int CROSS, int CT, int M, int MODE, bool WT>
-__global__ void __launch_bounds__(kThreads, 1) fg_pass_kernel(const PassArgs a) {
+__global__ void __maxnreg__((pass_reg_cap<CROSS, CT, M>())) fg_pass_kernel(const PassArgs a) {
   extern __shared__ __align__(16) float sm[];
   pass_body<CROSS, CT, M, MODE, WT>(a, blockIdx.x, sm);
 }

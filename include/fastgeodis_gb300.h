@@ -73,6 +73,16 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * that does not fit the device falls back to the planner's choice. */
 FG_API int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2);
 
+/* The plan the engine uses for one pass (no counterpart in the reference):
+ * cross-section rank `cross` (1: a 2D row, 2: a 3D plane) of N1 x N2 cells,
+ * C image channels, `maps` distance maps (1 or 2), arithmetic mode (0
+ * general, 1 l_grad == 0, 2 l_eucl == 0 and l_grad == 1), transposed write
+ * or not, on a GPU of `sms` SMs.  Writes 10 ints to `plan`: S, T1, T2, K1,
+ * K2, tiles1, tiles2, threads, staging depth, shared-memory bytes.  Needs no
+ * GPU; honours fg_set_tuning and fg_plan_override. */
+FG_API int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int transposed_write, int sms,
+                            int *plan);
+
 /* Event timing of the sweep kernels (no counterpart in the reference):
  * between fg_profile_begin() and fg_profile_end(), every pass launch is
  * bracketed by CUDA events on its stream.  fg_profile_end synchronises those
