@@ -8,8 +8,20 @@
 
 namespace fgi {
 
-constexpr int kThreads = 512;            // largest CTA; one thread per run of 4 cells
-constexpr int kMaxRegion = kThreads * 4; // cells of one CTA's region (tile + halo)
+constexpr int kThreads = 512;            // largest CTA of a 128-register variant; one thread per run of 4 cells
+constexpr int kThreadsLean = 1024;       // largest CTA of a 64-register ("lean") variant
+constexpr int kMaxRegion = kThreadsLean * 4; // cells of one CTA's region (tile + halo), any plan
+
+// Lean variants: volume sweeps with at most one staged image channel and one
+// distance map.  They fit in 64 registers (fg_pass_kernel's cap), so a CTA
+// may have 1024 threads; the others stop at 512.  `cimg` is the number of
+// image channels the pass reads (0 when l_grad == 0).
+__host__ __device__ constexpr bool pass_lean(int cross, int cimg, int maps) {
+  return cross == 2 && cimg <= 1 && maps == 1;
+}
+__host__ __device__ constexpr int pass_max_threads(int cross, int cimg, int maps) {
+  return pass_lean(cross, cimg, maps) ? kThreadsLean : kThreads;
+}
 constexpr int kMaxMaps = 2;              // distance maps updated by one launch (they share the image)
 constexpr int kMaxChannels = 4;          // image channels held in registers
 constexpr int kMaxTiles = 2048;          // tiles of one pass (all co-resident)

@@ -246,6 +246,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   bool found = false;
   Plan best{};
   double best_cost = 0.0;
+  const int max_threads = pass_max_threads(cross, mode == MODE_EUCLID ? 0 : C, M);
   // returns 1 if the plan is valid, 0 if not, -1 if it is too large (so is every larger T1)
   auto consider = [&](int S, int T1, int T2, int t1, int t2) -> int {
     const bool multi = t1 * t2 > 1;
@@ -253,9 +254,9 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if ((t1 > 1 && T1 < K1) || (t2 > 1 && T2 < K2)) return 0;
     if (t2 > 1 && T2 % 4) return 0;  // runs of 4 must not straddle tiles
     int R1 = cross == 2 ? T1 + 2 * K1 : 1, R2 = T2 + 2 * K2;
-    if ((long long)R1 * R2 > max_region) return -1;
+    if ((long long)R1 * R2 > std::min(max_region, 4 * max_threads)) return -1;
     int runs = R1 * ((R2 + 3) / 4);
-    if (runs > kThreads) return -1;
+    if (runs > max_threads) return -1;
     int B2, rowf, nown;
     const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
     // deepest staging that still leaves room for a second CTA on the SM (then
@@ -274,9 +275,10 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
                            (cross == 2 ? 1.0 : 3.0);
     const double avg_runs = multi ? cone_avg_runs(cross, R1, R2, K1, K2, S) : (double)((runs + 31) / 32 * 32);
     double cost = kStepBase + per_run * avg_runs + (multi ? (kHandoffBase + kHandoffPerTile * t1 * t2) / S : 0.0);
-    if (sm > kSmemBudget / 2) cost *= 1.05;  // one CTA per SM: no room for a concurrent transform
+    const int nt = std::max(32, std::min(max_threads, (runs + 31) / 32 * 32));
+    // one CTA per SM (shared memory or registers): no room for a concurrent transform
+    if (sm > kSmemBudget / 2 || nt > kThreads) cost *= 1.05;
     if (!found || cost < best_cost - 1e-9) {
-      int nt = std::max(32, std::min(kThreads, (runs + 31) / 32 * 32));
       best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm};
       best_cost = cost;
       found = true;

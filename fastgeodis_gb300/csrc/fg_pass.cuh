@@ -495,7 +495,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
 // stalls).  The others keep up to 128: row sweeps (2D) are a few CTAs whose
 // per-step chain wants every register of ILP.
 template <int CROSS, int CT, int M>
-constexpr int pass_reg_cap() { return (CROSS == 2 && CT == 1 && M == 1) ? 64 : 128; }
+constexpr int pass_reg_cap() { return pass_lean(CROSS, CT, M) ? 64 : 128; }
 
 template <int CROSS, int CT, int M, int MODE, bool WT>
 __global__ void __maxnreg__((pass_reg_cap<CROSS, CT, M>())) fg_pass_kernel(const PassArgs a) {

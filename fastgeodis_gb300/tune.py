@@ -3,14 +3,20 @@
 The engine plans every pass (tile extents T1 x T2 of the cross-section, halo
 hand-off every S steps) from a cost model of one step.  `autotune` replaces the
 model's choice by timing: for each distinct pass cross-section of a transform
-it tries candidate plans, runs the whole transform on seeded synthetic data of
-that shape with each candidate, reads the pass-kernel time from the engine's
-event hooks (fg_profile_begin / fg_profile_end) and pins the fastest plan with
+it tries candidate plans, runs the workload on seeded synthetic data of that
+shape with each candidate, and pins the fastest plan with
 ``fg_plan_override``.  Cross-sections are tuned one after another with the
 others held fixed, so differences in the total are the tuned pass's own.
 
+A workload of several transforms of one shape that run at the same time
+(one per stream: several lambdas of one image, or concurrent requests) is
+tuned as such: the timed unit is all of them, launched on their own streams,
+and the candidates include plans with fewer, larger tiles (a fraction of the
+SMs per transform), which waste less work on halos while the transforms
+share the GPU.
+
 Every plan computes the same bits; only the time changes.  Pinned plans hold
-for the process (all shapes with that cross-section) until `clear`.
+for the process (all calls with that cross-section) until `clear`.
 """
 from __future__ import annotations
 
@@ -22,10 +28,11 @@ import torch
 
 from . import _lib
 
-# Limits of one tile's region, as the engine checks them (fg_common.cuh):
-# at most kMaxRegion cells and kThreads runs of 4 cells.
-MAX_REGION = 2048
-MAX_RUNS = 512
+# Limits of one CTA, as the engine checks them (fg_common.cuh): one thread per
+# run of 4 cells, 512 threads (1024 for volume sweeps with one image channel
+# and one map), regions of at most 4 cells per thread.
+THREADS = 512
+THREADS_LEAN = 1024
 
 Key = Tuple[int, int, int]        # (cross, N1, N2)
 Choice = Tuple[int, int, int]     # (S, T1, T2)
@@ -35,42 +42,49 @@ def _ceil(a: int, b: int) -> int:
     return -(-a // b)
 
 
-def candidates(cross: int, N1: int, N2: int, sms: int, steps=(4, 8), max_per_step: int = 24) -> List[Choice]:
+def candidates(cross: int, N1: int, N2: int, sms: int, steps=(4, 8), max_per_step: int = 24,
+               lean: bool = False, tile_fracs: Sequence[float] = (1.0,)) -> List[Choice]:
     """Valid plans for a cross-section: for each tile count along N2 the
-    smallest tile height T1 that keeps every tile co-resident on `sms` SMs."""
+    smallest tile height T1 that keeps the tiles within `frac * sms` (all
+    co-resident), for every fraction in `tile_fracs`."""
+    max_threads = THREADS_LEAN if (lean and cross == 2) else THREADS
+    max_region = 4 * max_threads
     out: List[Choice] = []
     for S in steps:
-        seen_T2 = set()
-        n = 0
-        for t2 in range(1, N2 + 1):
-            T2 = _ceil(N2, t2)
-            if t2 > 1:
-                T2 = (T2 + 3) // 4 * 4  # runs of 4 cells must not straddle tiles
-            if T2 in seen_T2 or _ceil(N2, T2) > sms:
-                continue
-            seen_T2.add(T2)
-            tt2 = _ceil(N2, T2)
-            K2 = S if tt2 > 1 else 0
-            if tt2 > 1 and T2 < K2:
-                break
-            if cross == 1:
-                T1, K1 = 1, 0
-            else:
-                T1 = next((c for c in range(1, N1 + 1) if _ceil(N1, c) * tt2 <= sms), None)
-                if T1 is None:
+        for frac in tile_fracs:
+            cap = max(1, int(sms * frac))
+            seen_T2 = set()
+            n = 0
+            for t2 in range(1, N2 + 1):
+                T2 = _ceil(N2, t2)
+                if t2 > 1:
+                    T2 = (T2 + 3) // 4 * 4  # runs of 4 cells must not straddle tiles
+                if T2 in seen_T2 or _ceil(N2, T2) > cap:
                     continue
-                K1 = S if _ceil(N1, T1) > 1 else 0
-                if K1 and T1 < K1:
-                    T1 = min(K1, N1)
+                seen_T2.add(T2)
+                tt2 = _ceil(N2, T2)
+                K2 = S if tt2 > 1 else 0
+                if tt2 > 1 and T2 < K2:
+                    break
+                if cross == 1:
+                    T1, K1 = 1, 0
+                else:
+                    T1 = next((c for c in range(1, N1 + 1) if _ceil(N1, c) * tt2 <= cap), None)
+                    if T1 is None:
+                        continue
                     K1 = S if _ceil(N1, T1) > 1 else 0
-            R1 = T1 + 2 * K1 if cross == 2 else 1
-            R2 = T2 + 2 * K2
-            if R1 * R2 > MAX_REGION or R1 * _ceil(R2, 4) > MAX_RUNS:
-                continue
-            out.append((S, T1, T2))
-            n += 1
-            if n >= max_per_step:
-                break
+                    if K1 and T1 < K1:
+                        T1 = min(K1, N1)
+                        K1 = S if _ceil(N1, T1) > 1 else 0
+                R1 = T1 + 2 * K1 if cross == 2 else 1
+                R2 = T2 + 2 * K2
+                if R1 * R2 > max_region or R1 * _ceil(R2, 4) > max_threads:
+                    continue
+                if (S, T1, T2) not in out:
+                    out.append((S, T1, T2))
+                    n += 1
+                if n >= max_per_step:
+                    break
     return out
 
 
@@ -102,47 +116,65 @@ def clear(shape: Sequence[int]) -> None:
 
 def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing=(1.0, 1.0, 1.0),
              iterations: int = 1, repeats: int = 3, device=None, max_per_step: int = 24,
-             verbose: bool = False) -> Dict[Key, Tuple[int, int, int, float]]:
+             lambs: Optional[Sequence[float]] = None, verbose: bool = False) -> Dict[Key, Tuple[int, int, int, float]]:
     """Measure candidate plans for a 2D (H, W) or 3D (D, H, W) transform of
     `channels` image channels and pin the fastest for each cross-section.
 
-    Returns {(cross, N1, N2): (S, T1, T2, best pass-kernel ms of a transform)}.
-    The model's own plan competes as the unpinned entry (S = 0)."""
+    `lambs`: the workload's transforms that run at the same time, one per
+    stream (default: one transform with `lamb`).  Returns
+    {(cross, N1, N2): (S, T1, T2, best ms of the workload)}; the model's own
+    plan competes as the unpinned entry (S = 0)."""
     import fastgeodis_gb300 as fg
 
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
     shape = tuple(int(s) for s in shape)
+    lambs = [float(lamb)] if lambs is None else [float(x) for x in lambs]
     L = _lib.load()
     g = torch.Generator(device="cpu").manual_seed(0)
-    img = torch.rand((1, channels) + shape, generator=g).to(dev)
-    msk = torch.ones((1, 1) + shape, device=dev)
-    msk.view(-1)[msk.numel() // 2] = 0.0
-    if len(shape) == 2:
-        run = lambda: fg.generalised_geodesic2d(img, msk, 1e10, lamb, iterations)
-    else:
-        run = lambda: fg.generalised_geodesic3d(img, msk, list(spacing), 1e10, lamb, iterations)
-
-    def measure() -> float:
-        run()  # first launch of a plan sets up its kernel attributes
-        torch.cuda.synchronize(dev)
-        best = math.inf
-        for _ in range(repeats):
-            _lib.profile_begin()
-            run()
-            ms, _, _ = _lib.profile_end()
-            best = min(best, ms)
-        return best
-
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     result = {}
     with torch.cuda.device(dev):
+        img = torch.rand((1, channels) + shape, generator=g).to(dev)
+        msk = torch.ones((1, 1) + shape, device=dev)
+        msk.view(-1)[msk.numel() // 2] = 0.0
+        main = torch.cuda.current_stream(dev)
+        streams = [torch.cuda.Stream(dev) for _ in lambs]
+
+        def run():
+            for s in streams:
+                s.wait_stream(main)
+            for lm, s in zip(lambs, streams):
+                with torch.cuda.stream(s):
+                    if len(shape) == 2:
+                        fg.generalised_geodesic2d(img, msk, 1e10, lm, iterations)
+                    else:
+                        fg.generalised_geodesic3d(img, msk, list(spacing), 1e10, lm, iterations)
+            for s in streams:
+                main.wait_stream(s)
+
+        def measure() -> float:
+            run()  # first launch of a plan sets up its kernel attributes
+            torch.cuda.synchronize(dev)
+            best = math.inf
+            for _ in range(repeats):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(main)
+                run()
+                e1.record(main)
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            return best
+
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fracs = (1.0,) if len(lambs) == 1 else (1.0, 0.75, 0.5, 0.34)
+        lean = channels <= 1
         for key in pass_keys(shape):
             cross, N1, N2 = key
             _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0))
             best_c, best_t = (0, 0, 0), measure()
             if verbose:
                 print(f"[tune] {key} model plan: {best_t:.3f} ms")
-            for c in candidates(cross, N1, N2, sms, max_per_step=max_per_step):
+            for c in candidates(cross, N1, N2, sms, max_per_step=max_per_step, lean=lean, tile_fracs=fracs):
                 _lib.check(L.fg_plan_override(cross, N1, N2, *c))
                 t = measure()
                 if verbose:
@@ -151,6 +183,7 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
                     best_c, best_t = c, t
             _lib.check(L.fg_plan_override(cross, N1, N2, *best_c))
             result[key] = best_c + (best_t,)
+        fg.check_status(dev)
     return result
 
 

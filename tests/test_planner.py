@@ -1,0 +1,103 @@
+"""CPU tests of the pass planner through fg_plan_describe: every plan it
+returns respects the kernel's limits (region cells, threads, co-resident
+tiles, shared memory) and the tiling rules, for 2D rows and 3D planes, and
+honours plan overrides and tuning caps.  No kernel is launched."""
+import pytest
+
+from fastgeodis_gb300 import _lib
+
+SMEM_LIMIT = 227 * 1024
+SHAPES = [(1, 1, 1), (1, 1, 5), (1, 1, 300), (1, 1, 512), (1, 1, 2048), (1, 1, 4099),
+          (2, 1, 1), (2, 3, 7), (2, 16, 16), (2, 64, 64), (2, 128, 256), (2, 256, 256), (2, 40, 600),
+          (2, 2048, 8), (2, 300, 257)]
+
+
+def max_threads(cross, C, maps, mode):
+    """1024 for the 64-register volume variants (one image channel or none, one map), else 512."""
+    cimg = 0 if mode == 1 else C
+    return 1024 if (cross == 2 and cimg <= 1 and maps == 1) else 512
+
+
+def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
+    S, T1, T2, K1, K2, t1, t2, nt, depth, smem = (p[k] for k in _lib.PLAN_FIELDS)
+    assert S in (1, 2, 4, 8) and depth in (2, 4, 8)
+    assert t1 == -(-N1 // T1) and t2 == -(-N2 // T2)
+    assert t1 * t2 <= sms, "all tiles must be co-resident"
+    if cross == 1:
+        assert T1 == 1 and K1 == 0
+    assert K1 == (S if t1 > 1 else 0) and K2 == (S if t2 > 1 else 0)
+    if t2 > 1:
+        assert T2 % 4 == 0, "runs of 4 must not straddle tiles"
+    assert T1 >= K1 and T2 >= K2, "a halo reaches only the adjacent tiles"
+    R1 = T1 + 2 * K1 if cross == 2 else 1
+    R2 = T2 + 2 * K2
+    runs = R1 * (-(-R2 // 4))
+    mt = max_threads(cross, C, maps, mode)
+    assert R1 * R2 <= 4 * mt and runs <= nt <= mt and nt % 32 == 0
+    assert smem <= SMEM_LIMIT
+
+
+@pytest.mark.parametrize("cross,N1,N2", SHAPES)
+@pytest.mark.parametrize("C,maps,mode", [(1, 1, 0), (1, 1, 1), (1, 1, 2), (3, 1, 0), (4, 2, 0), (1, 2, 1)])
+@pytest.mark.parametrize("wt", [False, True])
+def test_plans_respect_kernel_limits(cross, N1, N2, C, maps, mode, wt):
+    try:
+        p = _lib.plan_describe(cross, N1, N2, C, maps, mode, wt, 152)
+    except RuntimeError:
+        # only cross-sections larger than the SMs' regions may lack a plan
+        assert N1 * N2 > 152 * 1024
+        return
+    check_plan(cross, N1, N2, p, 152, C, maps, mode)
+
+
+@pytest.mark.parametrize("sms", [1, 8, 76, 152])
+def test_plans_scale_with_sm_count(sms):
+    for cross, N1, N2 in [(1, 1, 2048), (2, 64, 64), (2, 30, 40)]:
+        try:
+            p = _lib.plan_describe(cross, N1, N2, 1, 1, 0, False, sms)
+        except RuntimeError:
+            assert N1 * N2 > sms * 1024
+            continue
+        check_plan(cross, N1, N2, p, sms)
+
+
+def test_override_is_used_and_cleared():
+    L = _lib.load()
+    base = _lib.plan_describe(2, 256, 256)
+    _lib.check(L.fg_plan_override(2, 256, 256, 4, 20, 24))
+    try:
+        p = _lib.plan_describe(2, 256, 256)
+        assert (p["S"], p["T1"], p["T2"]) == (4, 20, 24)
+        check_plan(2, 256, 256, p, 152)
+    finally:
+        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0))
+    assert _lib.plan_describe(2, 256, 256) == base
+
+
+def test_override_that_does_not_fit_falls_back_to_the_model():
+    L = _lib.load()
+    base = _lib.plan_describe(2, 256, 256)
+    _lib.check(L.fg_plan_override(2, 256, 256, 8, 64, 64))  # region 80 x 80 > 2048 cells
+    try:
+        assert _lib.plan_describe(2, 256, 256) == base
+    finally:
+        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0))
+
+
+def test_tuning_caps_region_and_tiles():
+    L = _lib.load()
+    _lib.check(L.fg_set_tuning(200, 40))
+    try:
+        p = _lib.plan_describe(2, 64, 64)
+        R1 = p["T1"] + 2 * p["K1"]
+        R2 = p["T2"] + 2 * p["K2"]
+        assert R1 * R2 <= 200 and p["tiles1"] * p["tiles2"] <= 40
+    finally:
+        _lib.check(L.fg_set_tuning(0, 0))
+
+
+def test_bad_queries():
+    with pytest.raises(ValueError):
+        _lib.plan_describe(3, 4, 4)
+    with pytest.raises(ValueError):
+        _lib.plan_describe(2, 4, 4, maps=3)

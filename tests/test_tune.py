@@ -11,11 +11,14 @@ from fastgeodis_gb300 import _lib, tune
 @pytest.mark.parametrize("cross,N1,N2", [(1, 1, 5), (1, 1, 300), (1, 1, 2048), (2, 7, 9), (2, 128, 256),
                                          (2, 256, 256), (2, 40, 600), (2, 2048, 8)])
 @pytest.mark.parametrize("sms", [152, 8])
-def test_candidates_follow_the_tiling_rules(cross, N1, N2, sms):
-    cands = tune.candidates(cross, N1, N2, sms)
+@pytest.mark.parametrize("lean", [False, True])
+@pytest.mark.parametrize("fracs", [(1.0,), (1.0, 0.5, 0.34)])
+def test_candidates_follow_the_tiling_rules(cross, N1, N2, sms, lean, fracs):
+    cands = tune.candidates(cross, N1, N2, sms, lean=lean, tile_fracs=fracs)
     if cross == 1 or N1 * N2 <= sms * 512:
         assert cands, "a cross-section that fits the SMs has a plan"
     assert len(set(cands)) == len(cands)
+    max_threads = tune.THREADS_LEAN if (lean and cross == 2) else tune.THREADS
     for S, T1, T2 in cands:
         assert S in (4, 8)
         t1, t2 = -(-N1 // T1), -(-N2 // T2)
@@ -31,7 +34,15 @@ def test_candidates_follow_the_tiling_rules(cross, N1, N2, sms):
             assert T1 >= K1
         R1 = T1 + 2 * K1 if cross == 2 else 1
         R2 = T2 + 2 * K2
-        assert R1 * R2 <= tune.MAX_REGION and R1 * (-(-R2 // 4)) <= tune.MAX_RUNS
+        assert R1 * R2 <= 4 * max_threads and R1 * (-(-R2 // 4)) <= max_threads
+
+
+def test_fewer_tile_candidates_for_concurrent_transforms():
+    one = tune.candidates(2, 256, 256, 152, lean=True)
+    conc = tune.candidates(2, 256, 256, 152, lean=True, tile_fracs=(1.0, 0.5, 0.34))
+    assert set(one) <= set(conc)
+    tiles = lambda c: -(-256 // c[1]) * -(-256 // c[2])  # noqa: E731
+    assert min(tiles(c) for c in conc) <= 52 < min(tiles(c) for c in one)
 
 
 def test_pass_keys():
@@ -67,7 +78,7 @@ def _case(shape, C, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape,C", [((300, 517), 1), ((40, 72, 64), 2), ((24, 24, 24), 1)])
+@pytest.mark.parametrize("shape,C", [((300, 517), 1), ((40, 72, 64), 2), ((24, 24, 24), 1), ((12, 160, 144), 1)])
 def test_every_candidate_plan_gives_the_oracle_bits(shape, C):
     import fastgeodis_gb300 as fg
     from golden_cases import bits_equal
@@ -86,7 +97,8 @@ def test_every_candidate_plan_gives_the_oracle_bits(shape, C):
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     try:
         for key in tune.pass_keys(shape):
-            for c in tune.candidates(*key, sms):
+            # fewer, larger tiles too: 1024-thread regions where the variant allows them
+            for c in tune.candidates(*key, sms, lean=(C == 1), tile_fracs=(1.0, 0.3, 0.1), max_per_step=8):
                 _lib.check(L.fg_plan_override(*key, *c))
                 got = run()[0].cpu().numpy()
                 assert bits_equal(got, want), (key, c, np.abs(got - want).max())
@@ -104,7 +116,7 @@ def test_autotune_pins_plans_and_keeps_results():
 
     shape = (36, 80, 96)
     try:
-        res = tune.autotune(shape, channels=1, lamb=0.5, iterations=1, repeats=2, max_per_step=6)
+        res = tune.autotune(shape, channels=1, lambs=[0.0, 0.5], iterations=1, repeats=2, max_per_step=4)
         assert set(res) == set(tune.pass_keys(shape))
         for S, T1, T2, ms in res.values():
             assert ms > 0 and S in (0, 4, 8)
