@@ -168,7 +168,8 @@ size_t batch_smem(int max_C, int max_extent, int is_signed, int S) {
   const int depth = pass_depth(nch, M);
   const int rowf = ring_pitch(((max_extent + 3) & ~3) + 8);  // one row: 4-cell apron, runs of 4, apron
   // the largest pass: a transposed-writing one (S distance rows) over the longest side
-  const size_t pass = (size_t)(S * M + 2 * max_C) * rowf * 4 + (size_t)depth * (M + max_C) * kThreads * 16 +
+  const size_t pass = (size_t)(S * M + 2 * max_C) * (rowf + pass_edge_floats(1, 1, max_extent)) * 4 +
+                      (size_t)depth * (M + max_C) * kThreads * 16 +
                       (size_t)max_extent * 8 + 64;
   const size_t transpose = (size_t)(kThreads / 32) * 32 * 33 * 4;
   return std::max(pass, transpose);

@@ -85,6 +85,17 @@ __host__ __device__ constexpr int ring_pitch(int floats) {
   return ((floats + 3) & ~3) + (36 - (((floats + 3) & ~3) % 32)) % 32;
 }
 
+// Floats of one edge array of a ring row set (volume sweeps only): for every
+// row position (apron rows included) and run of 4 cells, the boundary cells of
+// the neighbouring runs as a float2 (left neighbour's last cell, right
+// neighbour's first).  A thread then reads its 6-cell neighbourhood of a row
+// as one float4 and one float2, without bank conflicts.  Row sweeps (2D) read
+// one row per step and keep long rings (up to 2048 cells x S rows), so they
+// read the two edge cells directly and have no edge arrays.
+__host__ __device__ constexpr int pass_edge_floats(int cross, int R1, int R2) {
+  return cross == 2 ? ring_pitch((R1 + 2) * (((R2 + 3) / 4) + 2) * 2) : 0;
+}
+
 // Shared-memory bytes of a pass kernel for a region of R1 x R2 cells.
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2, int *rowf,
                        int *nown_max, int depth);

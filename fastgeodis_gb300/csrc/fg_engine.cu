@@ -706,7 +706,7 @@ size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1
   *B2o = B2;
   *rowfo = rowf;
   *nown_max = R1 * R2;
-  return (size_t)(SR * M + 2 * ci) * rowf * 4 + (size_t)depth * (M + ci) * nt * 16 +
+  return (size_t)(SR * M + 2 * ci) * (rowf + pass_edge_floats(cross, R1, R2)) * 4 + (size_t)depth * (M + ci) * nt * 16 +
          (wt ? (size_t)R1 * R2 * 8 : 0) + 64;
 }
 

@@ -173,15 +173,18 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const int o2lo = a.K2, o2hi = a.K2 + min(a.T2, a.N2 - ti2 * a.T2);
   const float qnan = __int_as_float(0x7fffffff);
 
+  const int rpr = (R2 + 3) >> 2;                               // runs per region row
+  const int edgef = pass_edge_floats(CROSS, R1, R2);
   const int AR = M + C;                                        // arrays staged per step
   float *dring = sm;                                           // [SR][M][rowf] distances, last SR steps
-  float *iring = sm + SR * M * rowf;                           // [2][C][rowf] image values, last 2 steps
-  float4 *oring = reinterpret_cast<float4 *>(iring + 2 * C * rowf);  // [P][AR][NT] own inputs in flight
+  float *iring = dring + SR * M * rowf;                        // [2][C][rowf] image values, last 2 steps
+  float *dedge = iring + 2 * C * rowf;                         // [SR][M][edgef] run edges of dring
+  float *iedge = dedge + SR * M * edgef;                       // [2][C][edgef] run edges of iring
+  float4 *oring = reinterpret_cast<float4 *>(iedge + 2 * C * edgef);  // [P][AR][NT] own inputs in flight
   int2 *otab = reinterpret_cast<int2 *>(oring + P * AR * NT);  // own cells (transposed flush)
 
   // --- set-up ---
   const bool has_nb = a.tiles1 * a.tiles2 > 1;
-  const int rpr = (R2 + 3) >> 2;
   // run of this thread: with neighbours, runs ordered innermost first, so
   // the runs outside a step's cone are whole trailing warps
   int qrun = tid, cdist = S;
@@ -195,7 +198,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     cdist = run_cone_dist(qrun, rpr, R1, R2, a.K1, a.K2, S);
     __syncthreads();
   }
-  for (int i = tid; i < (SR * M + 2 * C) * rowf + P * AR * NT * 4; i += NT) sm[i] = qnan;
+  for (int i = tid; i < (SR * M + 2 * C) * (rowf + edgef) + P * AR * NT * 4; i += NT) sm[i] = qnan;
   int nown = 0;
   if (WT) {
     const int O1 = o1hi - o1lo, O2 = o2hi - o2lo;
@@ -209,6 +212,17 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const int r1 = qrun / rpr, u = qrun - (qrun / rpr) * rpr;
   const int g1 = rs1 + r1, g20 = rs2 + 4 * u;
   const int cb = (r1 + A1) * B2 + 4 + 4 * u;
+  // this run's float2 in an edge array; it writes its first cell into the left
+  // run's slot (e0 - 1) and its last into the right run's (e0 + 2)
+  const int EP2 = (rpr + 2) * 2;  // floats per edge row
+  const int e0 = (r1 + A1) * EP2 + (u + 1) * 2;
+  constexpr bool EDGES = CROSS == 2;  // edge arrays (pass_edge_floats)
+  auto put_edges = [&](float *edge, const float4 &v) {
+    if (EDGES) {
+      edge[e0 - 1] = v.x;
+      edge[e0 + 2] = v.w;
+    }
+  };
   unsigned valid = 0, own = 0;
   if (r1 < R1) {
 #pragma unroll
@@ -302,7 +316,12 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
                 }
                 wd[m][i] = ld_word(xw + m * xplane + i);
               }
-              pr[m * rowf + i] = __uint_as_float((unsigned)wd[m][i]);
+              const float hv = __uint_as_float((unsigned)wd[m][i]);
+              pr[m * rowf + i] = hv;
+              // a run's first and last cells also live in its neighbours' edge slots
+              float *pe = dedge + ((t - 1) & (SR - 1)) * M * edgef + m * edgef;
+              if (EDGES && i == 0) pe[e0 - 1] = hv;
+              if (EDGES && i == 3) pe[e0 + 2] = hv;
             }
       }
       __syncthreads();
@@ -327,6 +346,8 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
       } else {
         const float *dp0 = dring + ((t - 1) & (SR - 1)) * M * rowf;
         const float *ip0 = iring + ((t - 1) & 1) * C * rowf;
+        const float *de0 = dedge + ((t - 1) & (SR - 1)) * M * edgef + e0;
+        const float *ie0 = iedge + ((t - 1) & 1) * C * edgef + e0;
         float best[M][4], pend[M][4];  // pend: a candidate of row 0 waiting for row 1's fold
         unsigned code[4] = {kTapeSelf, kTapeSelf, kTapeSelf, kTapeSelf};  // TAPE: argmin of map 0
 #pragma unroll
@@ -342,16 +363,20 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
           for (int c = 0; c < NCH; c++) {
             if (c < C) {
               const float *q = ip0 + c * rowf + pc;
-              float4 v = *reinterpret_cast<const float4 *>(q);
-              ip[c][0] = q[-1], ip[c][1] = v.x, ip[c][2] = v.y, ip[c][3] = v.z, ip[c][4] = v.w, ip[c][5] = q[4];
+              const float4 v = *reinterpret_cast<const float4 *>(q);
+              const float2 ev = EDGES ? *reinterpret_cast<const float2 *>(ie0 + c * edgef + d1 * EP2)
+                                      : make_float2(q[-1], q[4]);
+              ip[c][0] = ev.x, ip[c][1] = v.x, ip[c][2] = v.y, ip[c][3] = v.z, ip[c][4] = v.w, ip[c][5] = ev.y;
             }
           }
           float dp[M][6];
 #pragma unroll
           for (int m = 0; m < M; m++) {
             const float *q = dp0 + m * rowf + pc;
-            float4 v = *reinterpret_cast<const float4 *>(q);
-            dp[m][0] = q[-1], dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = q[4];
+            const float4 v = *reinterpret_cast<const float4 *>(q);
+            const float2 ev = EDGES ? *reinterpret_cast<const float2 *>(de0 + m * edgef + d1 * EP2)
+                                    : make_float2(q[-1], q[4]);
+            dp[m][0] = ev.x, dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = ev.y;
           }
           float cand3[M][4][3];  // this row's three candidates per map and cell
 #pragma unroll
@@ -435,12 +460,20 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
             if (own & (1u << i)) st_word(xw + m * xplane + i, ep | __float_as_uint(f4get(out[m], i)));
       }
       float *dc = dring + (t & (SR - 1)) * M * rowf + cb;
+      float *dce = dedge + (t & (SR - 1)) * M * edgef;
 #pragma unroll
-      for (int m = 0; m < M; m++) *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
+      for (int m = 0; m < M; m++) {
+        *reinterpret_cast<float4 *>(dc + m * rowf) = out[m];
+        put_edges(dce + m * edgef, out[m]);
+      }
       float *ic = iring + (t & 1) * C * rowf + cb;
+      float *ice = iedge + (t & 1) * C * edgef;
 #pragma unroll
       for (int c = 0; c < NCH; c++)
-        if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = icur[c];
+        if (c < C) {
+          *reinterpret_cast<float4 *>(ic + c * rowf) = icur[c];
+          put_edges(ice + c * edgef, icur[c]);
+        }
       if (!WT && t > 0 && own) {
 #pragma unroll
         for (int m = 0; m < M; m++) {
@@ -457,9 +490,14 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
       // outside the cone at a chunk's last step: pass the image values on
       const float4 *mine = oring + slot * AR * NT + tid;
       float *ic = iring + (t & 1) * C * rowf + cb;
+      float *ice = iedge + (t & 1) * C * edgef;
 #pragma unroll
       for (int c = 0; c < NCH; c++)
-        if (c < C) *reinterpret_cast<float4 *>(ic + c * rowf) = mine[(M + c) * NT];
+        if (c < C) {
+          const float4 v = mine[(M + c) * NT];
+          *reinterpret_cast<float4 *>(ic + c * rowf) = v;
+          put_edges(ice + c * edgef, v);
+        }
     }
     // the slot's values are consumed (they are in registers): refill it with step t+P
     if (t + P < L) stage(slot, t + P);
