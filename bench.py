@@ -607,8 +607,8 @@ def run_gpu_arm(args, w, rank, world):
         t_tune = time.perf_counter()
         tuned = tune.autotune(shape, channels=int(w["image"].shape[1]), lambs=w["lambs"],
                               spacing=w.get("spacing", (1.0, 1.0, 1.0)), iterations=1)
-        tuned = {"plans": {",".join(map(str, k)): [v[0], v[1], v[2]] for k, v in tuned.items()},
-                 "note": "(cross, N1, N2): (S, T1, T2); S = 0 keeps the cost model's plan",
+        tuned = {"plans": {",".join(map(str, k)): [v[0], v[1], v[2], v[3]] for k, v in tuned.items()},
+                 "note": "(cross, N1, N2): (S, T1, T2, lean); S = 0 keeps the cost model's plan",
                  "seconds": round(time.perf_counter() - t_tune, 2)}
 
     # the step's transforms are independent: one CUDA stream each, so their

@@ -65,7 +65,7 @@ def load():
     L.fg_profile_launch_times.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), i,
                                           ctypes.POINTER(ctypes.c_int)]
     L.fg_set_tuning.argtypes = [i, i]
-    L.fg_plan_override.argtypes = [i, i, i, i, i, i]
+    L.fg_plan_override.argtypes = [i, i, i, i, i, i, i]
     L.fg_plan_describe.argtypes = [i, i, i, i, i, i, i, i, ctypes.POINTER(ctypes.c_int)]
     L.fg_plan_override.restype = i
     L.fg_set_tuning.restype = i
@@ -114,7 +114,7 @@ def profile_launch_times():
     return [(float(ms[i]), int(st[i])) for i in range(n.value)]
 
 
-PLAN_FIELDS = ("S", "T1", "T2", "K1", "K2", "tiles1", "tiles2", "threads", "depth", "smem")
+PLAN_FIELDS = ("S", "T1", "T2", "K1", "K2", "tiles1", "tiles2", "threads", "depth", "smem", "lean")
 
 
 def plan_describe(cross, N1, N2, C=1, maps=1, mode=0, transposed_write=False, sms=152) -> dict:

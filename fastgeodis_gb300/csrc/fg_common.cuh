@@ -12,10 +12,13 @@ constexpr int kThreads = 512;            // largest CTA of a 128-register varian
 constexpr int kThreadsLean = 1024;       // largest CTA of a 64-register ("lean") variant
 constexpr int kMaxRegion = kThreadsLean * 4; // cells of one CTA's region (tile + halo), any plan
 
-// Lean variants: volume sweeps with at most one staged image channel and one
-// distance map.  They fit in 64 registers (fg_pass_kernel's cap), so a CTA
-// may have 1024 threads; the others stop at 512.  `cimg` is the number of
-// image channels the pass reads (0 when l_grad == 0).
+// Lean-capable variants: volume sweeps with at most one staged image channel
+// and one distance map.  Besides the 128-register kernel they have a
+// 64-register one (fg_pass_kernel<..., LEAN = true>), whose CTAs may have
+// 1024 threads, or share an SM two at a time up to 512 threads; it executes
+// about 30% more instructions (register pressure), so plans use it only for
+// regions above 512 runs or when the autotuner measures it faster.  `cimg`
+// is the number of image channels the pass reads (0 when l_grad == 0).
 __host__ __device__ constexpr bool pass_lean(int cross, int cimg, int maps) {
   return cross == 2 && cimg <= 1 && maps == 1;
 }
@@ -76,6 +79,7 @@ struct LaunchCfg {
   int tiles;
   int threads;
   size_t smem;
+  bool lean;  // the 64-register kernel (required above 512 threads)
 };
 
 // Pitch of the shared rings' rows: at least `floats`, a multiple of 4 (float4

@@ -185,6 +185,7 @@ DeviceInfo device_info() {
 struct Plan {
   int T1, T2, K1, K2, tiles1, tiles2, S, NT, B2, rowf, P;
   size_t smem;
+  bool lean;  // 64-register kernel
 };
 
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
@@ -196,7 +197,7 @@ std::atomic<int> g_tune_tiles{0};            // cap on tiles per pass (0: the SM
 // (averaged over a chunk, whole warps), and the neighbour hand-off of a
 // multi-tile plan (an L2 round trip, longer with more tiles) spread over the
 // S steps of a chunk.
-constexpr double kStepBase = 620.0, kCyclesPerRunGeneral = 2.7, kCyclesPerRunEuclid = 1.4;
+constexpr double kStepBase = 620.0, kCyclesPerRunGeneral = 2.4, kCyclesPerRunEuclid = 1.3;
 constexpr double kHandoffBase = 2000.0, kHandoffPerTile = 8.0;
 
 // Runs computed per step, averaged over the S steps of a chunk and rounded up
@@ -224,9 +225,9 @@ double cone_avg_runs(int cross, int R1, int R2, int K1, int K2, int S) {
   return sum / S;
 }
 
-// Plan overrides set by the autotuner (fg_plan_override): cross-section shape -> (S, T1, T2).
+// Plan overrides set by the autotuner (fg_plan_override): cross-section shape -> (S, T1, T2, lean).
 std::mutex g_override_mu;
-std::map<std::tuple<int, int, int>, std::tuple<int, int, int>> g_overrides;
+std::map<std::tuple<int, int, int>, std::tuple<int, int, int, int>> g_overrides;
 std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older cache entries are stale
 
 bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int max_tiles, Plan *out) {
@@ -247,8 +248,9 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   Plan best{};
   double best_cost = 0.0;
   const int max_threads = pass_max_threads(cross, mode == MODE_EUCLID ? 0 : C, M);
+  const bool lean_capable = pass_lean(cross, mode == MODE_EUCLID ? 0 : C, M);
   // returns 1 if the plan is valid, 0 if not, -1 if it is too large (so is every larger T1)
-  auto consider = [&](int S, int T1, int T2, int t1, int t2) -> int {
+  auto consider = [&](int S, int T1, int T2, int t1, int t2, bool want_lean) -> int {
     const bool multi = t1 * t2 > 1;
     int K1 = (cross == 2 && t1 > 1) ? S : 0, K2 = t2 > 1 ? S : 0;
     if ((t1 > 1 && T1 < K1) || (t2 > 1 && T2 < K2)) return 0;
@@ -276,25 +278,27 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     const double avg_runs = multi ? cone_avg_runs(cross, R1, R2, K1, K2, S) : (double)((runs + 31) / 32 * 32);
     double cost = kStepBase + per_run * avg_runs + (multi ? (kHandoffBase + kHandoffPerTile * t1 * t2) / S : 0.0);
     const int nt = std::max(32, std::min(max_threads, (runs + 31) / 32 * 32));
+    const bool lean = nt > kThreads || (want_lean && lean_capable);
+    if (lean) cost += 0.13 * per_run * avg_runs;  // the 64-register kernel's extra instructions
     // one CTA per SM (shared memory or registers): no room for a concurrent transform
     if (sm > kSmemBudget / 2 || nt > kThreads) cost *= 1.05;
     if (!found || cost < best_cost - 1e-9) {
-      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm};
+      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean};
       best_cost = cost;
       found = true;
     }
     return 1;
   };
-  int ovS = 0, ovT1 = 0, ovT2 = 0;
+  int ovS = 0, ovT1 = 0, ovT2 = 0, ovLean = 0;
   {
     std::lock_guard<std::mutex> g(g_override_mu);
     auto it = g_overrides.find(std::make_tuple(cross, N1, N2));
-    if (it != g_overrides.end()) std::tie(ovS, ovT1, ovT2) = it->second;
+    if (it != g_overrides.end()) std::tie(ovS, ovT1, ovT2, ovLean) = it->second;
   }
   if (ovS > 0) {
     const int T1 = cross == 2 ? std::min(ovT1, N1) : 1, T2 = std::min(ovT2, N2);
     const int t1 = (N1 + T1 - 1) / T1, t2 = (N2 + T2 - 1) / T2;
-    if ((long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2);
+    if ((long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, ovLean != 0);
   }
   for (int S : {8, 4, 2, 1}) {
     if (found) break;  // an override that fits wins
@@ -304,7 +308,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
         if (tiles2 > 1) T2 = (T2 + 3) & ~3;
         int t2 = (N2 + T2 - 1) / T2;
         if (tiles2 > 1 && t2 != tiles2) continue;
-        consider(S, 1, T2, 1, t2);
+        consider(S, 1, T2, 1, t2, false);
         if (T2 <= 4) break;
       }
     } else {
@@ -313,7 +317,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
         for (int T1 = 1; T1 <= N1; T1++) {
           int t1 = (N1 + T1 - 1) / T1;
           if ((long long)t1 * t2 > max_tiles) continue;
-          if (consider(S, T1, T2, t1, t2) != 0) break;  // larger T1 only grows the region
+          if (consider(S, T1, T2, t1, t2, false) != 0) break;  // larger T1 only grows the region
         }
         if (T2 >= N2) break;
       }
@@ -327,9 +331,9 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (debug)
       fprintf(stderr,
               "[fg plan] cross=%d N=%dx%d C=%d M=%d mode=%d wt=%d -> T=%dx%d K=%d,%d tiles=%dx%d S=%d NT=%d "
-              "P=%d smem=%zu cost=%.0f\n",
+              "P=%d smem=%zu lean=%d cost=%.0f\n",
               cross, N1, N2, C, M, mode, (int)wt, best.T1, best.T2, best.K1, best.K2, best.tiles1, best.tiles2,
-              best.S, best.NT, best.P, best.smem, best_cost);
+              best.S, best.NT, best.P, best.smem, (int)best.lean, best_cost);
   }
   return found;
 }
@@ -425,7 +429,7 @@ ProfileState &profile() {
 std::mutex g_launch_mu;  // serialises the per-device function attribute set-up
 
 int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt, cudaStream_t s) {
-  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem};
+  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean};
   ProfileState &ps = profile();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   {
@@ -772,7 +776,7 @@ int fg_profile_launch_times(float *ms, int *steps, int cap, int *n) {
   return FG_OK;
 }
 
-int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2) {
+int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean) {
   if (cross < 1 || cross > 2 || N1 < 1 || N2 < 1) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad shape");
   std::lock_guard<std::mutex> g(g_override_mu);
   auto key = std::make_tuple(cross, N1, N2);
@@ -781,7 +785,7 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2) {
   } else {
     if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    g_overrides[key] = std::make_tuple(S, T1, T2);
+    g_overrides[key] = std::make_tuple(S, T1, T2, lean != 0 ? 1 : 0);
   }
   g_plan_epoch.fetch_add(1);
   return FG_OK;
@@ -796,8 +800,8 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
   const int c = mode == MODE_EUCLID ? 0 : C;
   if (!make_plan(cross, N1, N2, c, maps, mode, transposed_write != 0, std::min(sms, kMaxTiles), &p))
     return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
-  const int v[10] = {p.S, p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem};
-  for (int i = 0; i < 10; i++) plan[i] = v[i];
+  const int v[11] = {p.S, p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem, (int)p.lean};
+  for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }
 

@@ -527,23 +527,18 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   cp_async_wait<0>();
 }
 
-// Register budget of a variant.  Volume variants with one channel and one
-// map fit in 64 registers without spills, so two CTAs of up to 512 threads
-// share an SM (concurrent transforms on other streams then fill each other's
-// stalls).  The others keep up to 128: row sweeps (2D) are a few CTAs whose
-// per-step chain wants every register of ILP.
-template <int CROSS, int CT, int M>
-constexpr int pass_reg_cap() { return pass_lean(CROSS, CT, M) ? 64 : 128; }
-
-template <int CROSS, int CT, int M, int MODE, bool WT>
-__global__ void __maxnreg__((pass_reg_cap<CROSS, CT, M>())) fg_pass_kernel(const PassArgs a) {
+// Register budget: 128 (CTAs up to 512 threads), or 64 for the lean kernel
+// of a lean-capable variant (pass_lean: no spills at 64; CTAs up to 1024
+// threads, or two CTAs of up to 512 threads per SM).
+template <int CROSS, int CT, int M, int MODE, bool WT, bool LEAN>
+__global__ void __maxnreg__((LEAN ? 64 : 128)) fg_pass_kernel(const PassArgs a) {
   extern __shared__ __align__(16) float sm[];
   pass_body<CROSS, CT, M, MODE, WT>(a, blockIdx.x, sm);
 }
 
-template <int CROSS, int CT, int M, int MODE, bool WT>
+template <int CROSS, int CT, int M, int MODE, bool WT, bool LEAN>
 int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
-  auto fn = fg_pass_kernel<CROSS, CT, M, MODE, WT>;
+  auto fn = fg_pass_kernel<CROSS, CT, M, MODE, WT, LEAN>;
   static unsigned long long configured = 0;  // bit per device (set under the engine's launch lock)
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -562,14 +557,23 @@ int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
   return FG_OK;
 }
 
+template <int CROSS, int CT, int M, int MODE, bool WT>
+int launch_regs(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
+  if constexpr (pass_lean(CROSS, CT, M)) {
+    if (c.lean) return launch_variant<CROSS, CT, M, MODE, WT, true>(a, c, s);
+  }
+  if (c.threads > kThreads) return set_error(FG_ERR_UNSUPPORTED, "a 128-register sweep CTA has at most 512 threads");
+  return launch_variant<CROSS, CT, M, MODE, WT, false>(a, c, s);
+}
+
 template <int CROSS, int M, bool WT>
 int launch_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStream_t s) {
   const bool one = a.C == 1;
-  if (mode == MODE_EUCLID) return launch_variant<CROSS, 1, M, MODE_EUCLID, WT>(a, c, s);
+  if (mode == MODE_EUCLID) return launch_regs<CROSS, 1, M, MODE_EUCLID, WT>(a, c, s);
   if (mode == MODE_GEO)
-    return one ? launch_variant<CROSS, 1, M, MODE_GEO, WT>(a, c, s) : launch_variant<CROSS, 0, M, MODE_GEO, WT>(a, c, s);
-  return one ? launch_variant<CROSS, 1, M, MODE_GENERAL, WT>(a, c, s)
-             : launch_variant<CROSS, 0, M, MODE_GENERAL, WT>(a, c, s);
+    return one ? launch_regs<CROSS, 1, M, MODE_GEO, WT>(a, c, s) : launch_regs<CROSS, 0, M, MODE_GEO, WT>(a, c, s);
+  return one ? launch_regs<CROSS, 1, M, MODE_GENERAL, WT>(a, c, s)
+             : launch_regs<CROSS, 0, M, MODE_GENERAL, WT>(a, c, s);
 }
 
 template <int CROSS>

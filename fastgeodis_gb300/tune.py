@@ -36,6 +36,8 @@ THREADS_LEAN = 1024
 
 Key = Tuple[int, int, int]        # (cross, N1, N2)
 Choice = Tuple[int, int, int]     # (S, T1, T2)
+# A pinned plan: (S, T1, T2, lean); lean = 1 asks for the 64-register kernel
+# (fg_plan_override), 0 leaves it to the planner.
 
 
 def _ceil(a: int, b: int) -> int:
@@ -101,29 +103,31 @@ def pass_keys(shape: Sequence[int]) -> List[Key]:
     return list(dict.fromkeys(keys))
 
 
-def pin(choices: Dict[Key, Choice]) -> None:
+def pin(choices: Dict[Key, Tuple[int, int, int, int]]) -> None:
+    """Pin plans {(cross, N1, N2): (S, T1, T2, lean)}."""
     L = _lib.load()
-    for (cross, N1, N2), (S, T1, T2) in choices.items():
-        _lib.check(L.fg_plan_override(cross, N1, N2, S, T1, T2))
+    for (cross, N1, N2), (S, T1, T2, lean) in choices.items():
+        _lib.check(L.fg_plan_override(cross, N1, N2, S, T1, T2, lean))
 
 
 def clear(shape: Sequence[int]) -> None:
     """Unpin the plans of a shape's cross-sections (the cost model decides again)."""
     L = _lib.load()
     for cross, N1, N2 in pass_keys(shape):
-        _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0))
+        _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0, 0))
 
 
 def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing=(1.0, 1.0, 1.0),
              iterations: int = 1, repeats: int = 3, device=None, max_per_step: int = 24,
-             lambs: Optional[Sequence[float]] = None, verbose: bool = False) -> Dict[Key, Tuple[int, int, int, float]]:
+             lambs: Optional[Sequence[float]] = None, verbose: bool = False) -> Dict[Key, Tuple[int, int, int, int, float]]:
     """Measure candidate plans for a 2D (H, W) or 3D (D, H, W) transform of
     `channels` image channels and pin the fastest for each cross-section.
 
     `lambs`: the workload's transforms that run at the same time, one per
-    stream (default: one transform with `lamb`).  Returns
-    {(cross, N1, N2): (S, T1, T2, best ms of the workload)}; the model's own
-    plan competes as the unpinned entry (S = 0)."""
+    stream (default: one transform with `lamb`).  With several, the 64-register
+    kernel is tried too (two CTAs of different transforms per SM).  Returns
+    {(cross, N1, N2): (S, T1, T2, lean, best ms of the workload)}; the model's
+    own plan competes as the unpinned entry (S = 0)."""
     import fastgeodis_gb300 as fg
 
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -170,15 +174,21 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
         lean = channels <= 1
         for key in pass_keys(shape):
             cross, N1, N2 = key
-            _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0))
-            best_c, best_t = (0, 0, 0), measure()
+            _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0, 0))
+            best_c, best_t = (0, 0, 0, 0), measure()
             if verbose:
                 print(f"[tune] {key} model plan: {best_t:.3f} ms")
+            trials = []
             for c in candidates(cross, N1, N2, sms, max_per_step=max_per_step, lean=lean, tile_fracs=fracs):
+                trials.append(c + (0,))
+                small = (c[1] + 2 * c[0]) * _ceil(c[2] + 2 * c[0], 4) <= THREADS
+                if lean and cross == 2 and len(lambs) > 1 and small:
+                    trials.append(c + (1,))  # 64-register kernel: two CTAs per SM
+            for c in trials:
                 _lib.check(L.fg_plan_override(cross, N1, N2, *c))
                 t = measure()
                 if verbose:
-                    print(f"[tune] {key} S={c[0]} T={c[1]}x{c[2]}: {t:.3f} ms")
+                    print(f"[tune] {key} S={c[0]} T={c[1]}x{c[2]} lean={c[3]}: {t:.3f} ms")
                 if t < best_t:
                     best_c, best_t = c, t
             _lib.check(L.fg_plan_override(cross, N1, N2, *best_c))
@@ -188,7 +198,7 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
 
 
 def save(result: Dict[Key, Tuple], path: str) -> None:
-    """Write tuned plans as JSON ({"cross,N1,N2": [S, T1, T2, ms]})."""
+    """Write tuned plans as JSON ({"cross,N1,N2": [S, T1, T2, lean, ms]})."""
     with open(path, "w") as f:
         json.dump({",".join(map(str, k)): list(v) for k, v in result.items()}, f, indent=1)
 
@@ -199,5 +209,5 @@ def load(path: str, apply: bool = True) -> Dict[Key, Tuple]:
         raw = json.load(f)
     result = {tuple(int(x) for x in k.split(",")): tuple(v) for k, v in raw.items()}
     if apply:
-        pin({k: tuple(int(x) for x in v[:3]) for k, v in result.items() if int(v[0]) > 0})
+        pin({k: tuple(int(x) for x in v[:4]) for k, v in result.items() if int(v[0]) > 0})
     return result

@@ -19,7 +19,7 @@ def max_threads(cross, C, maps, mode):
 
 
 def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
-    S, T1, T2, K1, K2, t1, t2, nt, depth, smem = (p[k] for k in _lib.PLAN_FIELDS)
+    S, T1, T2, K1, K2, t1, t2, nt, depth, smem, lean = (p[k] for k in _lib.PLAN_FIELDS)
     assert S in (1, 2, 4, 8) and depth in (2, 4, 8)
     assert t1 == -(-N1 // T1) and t2 == -(-N2 // T2)
     assert t1 * t2 <= sms, "all tiles must be co-resident"
@@ -34,6 +34,11 @@ def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
     runs = R1 * (-(-R2 // 4))
     mt = max_threads(cross, C, maps, mode)
     assert R1 * R2 <= 4 * mt and runs <= nt <= mt and nt % 32 == 0
+    assert lean in (0, 1)
+    if lean:
+        assert mt == 1024, "only lean-capable variants use the 64-register kernel"
+    else:
+        assert nt <= 512, "the 128-register kernel stops at 512 threads"
     assert smem <= SMEM_LIMIT
 
 
@@ -64,24 +69,37 @@ def test_plans_scale_with_sm_count(sms):
 def test_override_is_used_and_cleared():
     L = _lib.load()
     base = _lib.plan_describe(2, 256, 256)
-    _lib.check(L.fg_plan_override(2, 256, 256, 4, 20, 24))
+    _lib.check(L.fg_plan_override(2, 256, 256, 4, 20, 24, 0))
     try:
         p = _lib.plan_describe(2, 256, 256)
         assert (p["S"], p["T1"], p["T2"]) == (4, 20, 24)
         check_plan(2, 256, 256, p, 152)
     finally:
-        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0))
+        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0, 0))
     assert _lib.plan_describe(2, 256, 256) == base
+
+
+def test_lean_override():
+    L = _lib.load()
+    _lib.check(L.fg_plan_override(2, 256, 256, 8, 14, 32, 1))
+    try:
+        p = _lib.plan_describe(2, 256, 256)          # one channel, one map: lean-capable
+        assert p["lean"] == 1 and p["threads"] <= 512
+        q = _lib.plan_describe(2, 256, 256, C=3)     # three channels: no 64-register kernel
+        assert q["lean"] == 0
+    finally:
+        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0, 0))
+    assert _lib.plan_describe(2, 256, 256)["lean"] == 0 or _lib.plan_describe(2, 256, 256)["threads"] > 512
 
 
 def test_override_that_does_not_fit_falls_back_to_the_model():
     L = _lib.load()
     base = _lib.plan_describe(2, 256, 256)
-    _lib.check(L.fg_plan_override(2, 256, 256, 8, 64, 64))  # region 80 x 80 > 2048 cells
+    _lib.check(L.fg_plan_override(2, 256, 256, 8, 64, 64, 0))  # region 80 x 80 > 2048 cells
     try:
         assert _lib.plan_describe(2, 256, 256) == base
     finally:
-        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0))
+        _lib.check(L.fg_plan_override(2, 256, 256, 0, 0, 0, 0))
 
 
 def test_tuning_caps_region_and_tiles():

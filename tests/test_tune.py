@@ -56,10 +56,10 @@ def test_pass_keys():
 
 def test_override_validation_and_round_trip(tmp_path):
     L = _lib.load()
-    assert L.fg_plan_override(2, 64, 64, 3, 8, 8) == _lib.FG_ERR_INVALID_ARGUMENT  # S not a power of two <= 8
-    assert L.fg_plan_override(2, 64, 64, 4, 8, 6) == _lib.FG_ERR_INVALID_ARGUMENT  # T2 not a multiple of 4
-    assert L.fg_plan_override(3, 64, 64, 4, 8, 8) == _lib.FG_ERR_INVALID_ARGUMENT
-    res = {(2, 64, 64): (4, 8, 16, 0.5), (1, 1, 100): (8, 1, 52, 0.25), (2, 9, 9): (0, 0, 0, 0.1)}
+    assert L.fg_plan_override(2, 64, 64, 3, 8, 8, 0) == _lib.FG_ERR_INVALID_ARGUMENT  # S not a power of two <= 8
+    assert L.fg_plan_override(2, 64, 64, 4, 8, 6, 0) == _lib.FG_ERR_INVALID_ARGUMENT  # T2 not a multiple of 4
+    assert L.fg_plan_override(3, 64, 64, 4, 8, 8, 0) == _lib.FG_ERR_INVALID_ARGUMENT
+    res = {(2, 64, 64): (4, 8, 16, 1, 0.5), (1, 1, 100): (8, 1, 52, 0, 0.25), (2, 9, 9): (0, 0, 0, 0, 0.1)}
     path = str(tmp_path / "plans.json")
     tune.save(res, path)
     back = tune.load(path)
@@ -99,10 +99,11 @@ def test_every_candidate_plan_gives_the_oracle_bits(shape, C):
         for key in tune.pass_keys(shape):
             # fewer, larger tiles too: 1024-thread regions where the variant allows them
             for c in tune.candidates(*key, sms, lean=(C == 1), tile_fracs=(1.0, 0.3, 0.1), max_per_step=8):
-                _lib.check(L.fg_plan_override(*key, *c))
-                got = run()[0].cpu().numpy()
-                assert bits_equal(got, want), (key, c, np.abs(got - want).max())
-            _lib.check(L.fg_plan_override(*key, 0, 0, 0))
+                for lean in ((0, 1) if C == 1 and len(shape) == 3 else (0,)):  # both register budgets
+                    _lib.check(L.fg_plan_override(*key, *c, lean))
+                    got = run()[0].cpu().numpy()
+                    assert bits_equal(got, want), (key, c, lean, np.abs(got - want).max())
+            _lib.check(L.fg_plan_override(*key, 0, 0, 0, 0))
         fg.check_status()
     finally:
         tune.clear(shape)
@@ -118,8 +119,8 @@ def test_autotune_pins_plans_and_keeps_results():
     try:
         res = tune.autotune(shape, channels=1, lambs=[0.0, 0.5], iterations=1, repeats=2, max_per_step=4)
         assert set(res) == set(tune.pass_keys(shape))
-        for S, T1, T2, ms in res.values():
-            assert ms > 0 and S in (0, 4, 8)
+        for S, T1, T2, lean, ms in res.values():
+            assert ms > 0 and S in (0, 4, 8) and lean in (0, 1)
         img, m = _case(shape, 1, 5)
         got = fg.generalised_geodesic3d(torch.from_numpy(img)[None].cuda(), torch.from_numpy(m)[None].cuda(),
                                         [1.0, 1.0, 1.0], 1e10, 0.5, 2)[0].cpu().numpy()
