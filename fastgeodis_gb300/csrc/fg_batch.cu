@@ -127,9 +127,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             batch_pass_args(it, M, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), M), r2, status, &s_args);
           __syncthreads();
           if (wt)
-            pass_body<1, CT, M, MODE_GENERAL, true>(s_args, 0, sm);
+            pass_body<1, CT, M, MODE_GENERAL, true, false, false>(s_args, 0, sm);
           else
-            pass_body<1, CT, M, MODE_GENERAL, false>(s_args, 0, sm);
+            pass_body<1, CT, M, MODE_GENERAL, false, false, false>(s_args, 0, sm);
           __threadfence();
           __syncthreads();
         }
@@ -260,9 +260,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           __syncthreads();
           if (wt)
-            pass_body<1, CT, 1, MODE_GENERAL, true, true>(s_args, 0, sm);
+            pass_body<1, CT, 1, MODE_GENERAL, true, true, false>(s_args, 0, sm);
           else
-            pass_body<1, CT, 1, MODE_GENERAL, false, true>(s_args, 0, sm);
+            pass_body<1, CT, 1, MODE_GENERAL, false, true, false>(s_args, 0, sm);
           __threadfence();
           __syncthreads();
         }

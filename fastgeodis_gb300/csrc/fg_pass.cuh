@@ -149,7 +149,9 @@ __device__ __forceinline__ void cp_async_wait() {
 // The body of one pass over tile `tile`, shared by the per-pass kernel and the
 // batched kernel.  `ar` may live in parameter or shared memory; it is copied
 // into registers first so the step loop never reloads its fields.
-template <int CROSS, int CT, int M, int MODE, bool WT, bool TAPE = false>
+// MULTI = false compiles a single-tile body (no halo exchange, no cone): the
+// batched kernels, whose CTA always owns a whole image.
+template <int CROSS, int CT, int M, int MODE, bool WT, bool TAPE = false, bool MULTI = true>
 __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, float *sm) {
   const PassArgs a = ar;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
@@ -184,7 +186,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   int2 *otab = reinterpret_cast<int2 *>(oring + P * AR * NT);  // own cells (transposed flush)
 
   // --- set-up ---
-  const bool has_nb = a.tiles1 * a.tiles2 > 1;
+  const bool has_nb = MULTI && a.tiles1 * a.tiles2 > 1;
   // run of this thread: with neighbours, runs ordered innermost first, so
   // the runs outside a step's cone are whole trailing warps
   int qrun = tid, cdist = S;
@@ -348,7 +350,10 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         const float *ip0 = iring + ((t - 1) & 1) * C * rowf;
         const float *de0 = dedge + ((t - 1) & (SR - 1)) * M * edgef + e0;
         const float *ie0 = iedge + ((t - 1) & 1) * C * edgef + e0;
-        float best[M][4], pend[M][4];  // pend: a candidate of row 0 waiting for row 1's fold
+        // running minimum per map and cell, folded three values per min: the
+        // old value and 9 candidates (3D) in 4 three-way mins and one two-way
+        // min; an even-numbered candidate waits in pend for the next one
+        float best[M][4], pend[M][4];
         unsigned code[4] = {kTapeSelf, kTapeSelf, kTapeSelf, kTapeSelf};  // TAPE: argmin of map 0
 #pragma unroll
         for (int m = 0; m < M; m++)
@@ -378,10 +383,10 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
                                     : make_float2(q[-1], q[4]);
             dp[m][0] = ev.x, dp[m][1] = v.x, dp[m][2] = v.y, dp[m][3] = v.z, dp[m][4] = v.w, dp[m][5] = ev.y;
           }
-          float cand3[M][4][3];  // this row's three candidates per map and cell
 #pragma unroll
           for (int d2 = -1; d2 <= 1; d2++) {
             const int n = CROSS == 2 ? (d1 + 1) * 3 + (d2 + 1) : d2 + 1;
+            const int k = r * 3 + (d2 + 1);  // candidate number 0 .. 3 * NR - 1
 #pragma unroll
             for (int i = 0; i < 4; i++) {
               float l1 = 0.0f;
@@ -406,26 +411,13 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
                 if (TAPE && m == 0) {
                   // same value as fminf for the non-NaN current distance of an in-image cell
                   if (cand < best[m][i]) best[m][i] = cand, code[i] = 1 + n;
+                } else if (k == 3 * NR - 1) {
+                  best[m][i] = fminf(best[m][i], cand);  // the last candidate
+                } else if (k & 1) {
+                  best[m][i] = fmin3(best[m][i], pend[m][i], cand);
+                } else {
+                  pend[m][i] = cand;  // waits for the next candidate
                 }
-                cand3[m][i][d2 + 1] = cand;
-              }
-            }
-          }
-          // fold the row into the running minimum, three values per min:
-          // old + 9 candidates (3D) in 4 three-way mins and one two-way min
-#pragma unroll
-          for (int m = 0; m < M; m++) {
-            if (TAPE && m == 0) continue;
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-              const float c0 = cand3[m][i][0], c1 = cand3[m][i][1], c2 = cand3[m][i][2];
-              if (NR == 1 || r == 2) {
-                best[m][i] = fminf(fmin3(best[m][i], c0, c1), c2);
-              } else if (r == 0) {
-                best[m][i] = fmin3(best[m][i], c0, c1);
-                pend[m][i] = c2;
-              } else {
-                best[m][i] = fmin3(fmin3(best[m][i], pend[m][i], c0), c1, c2);
               }
             }
           }
@@ -559,7 +551,7 @@ int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
 
 template <int CROSS, int CT, int M, int MODE, bool WT>
 int launch_regs(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
-  if constexpr (pass_lean(CROSS, CT, M)) {
+  if constexpr (pass_lean(CROSS, CT == 0 ? kMaxChannels : CT, M)) {  // CT = 0: up to 4 channels
     if (c.lean) return launch_variant<CROSS, CT, M, MODE, WT, true>(a, c, s);
   }
   if (c.threads > kThreads) return set_error(FG_ERR_UNSUPPORTED, "a 128-register sweep CTA has at most 512 threads");
