@@ -32,7 +32,7 @@ EXPORTED = (
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
     "fg_grad_geodesic2d_forward", "fg_grad_geodesic2d_backward",
-    "fg_generalised_geodesic2d_noalloc",
+    "fg_generalised_geodesic2d_noalloc", "fg_click_mask",
 )
 
 _lib = None
@@ -64,6 +64,7 @@ def load():
                                  ctypes.POINTER(ctypes.c_double)]
     L.fg_profile_launch_times.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), i,
                                           ctypes.POINTER(ctypes.c_int)]
+    L.fg_click_mask.argtypes = [vp, i, i, i, ctypes.POINTER(ctypes.c_int), i, i, vp]
     L.fg_set_tuning.argtypes = [i, i]
     L.fg_plan_override.argtypes = [i, i, i, i, i, i, i]
     L.fg_plan_describe.argtypes = [i, i, i, i, i, i, i, i, ctypes.POINTER(ctypes.c_int)]

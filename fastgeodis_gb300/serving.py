@@ -58,6 +58,35 @@ class Request:
         return (self.t_done - self.t_submit) * 1e3
 
 
+def click_mask(shape, clicks, radius: int, device=None):
+    """Soft mask [1, 1, *shape] (2D (H, W) or 3D (D, H, W)) that is 0 within
+    Euclidean distance `radius` of any click and 1 elsewhere, written on the
+    device by one kernel (fg_click_mask) on the current stream."""
+    import ctypes
+
+    import torch
+
+    from . import _lib
+
+    shape = tuple(int(s) for s in shape)
+    if len(shape) not in (2, 3):
+        raise ValueError("shape must be (H, W) or (D, H, W)")
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    D, H, W = shape if len(shape) == 3 else (1,) + shape
+    flat = []
+    for c in clicks:
+        c = [int(v) for v in c]
+        if len(c) != len(shape):
+            raise ValueError(f"click {c} does not match a {len(shape)}D shape")
+        flat += c if len(c) == 3 else [0] + c
+    arr = (ctypes.c_int * max(1, len(flat)))(*flat)
+    with torch.cuda.device(dev):
+        m = torch.empty((1, 1) + shape, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        _lib.check(_lib.load().fg_click_mask(m.data_ptr(), D, H, W, arr, len(flat) // 3, int(radius), stream))
+    return m
+
+
 class Scheduler:
     """Continuous-batching admission: FIFO queue, in-flight slots, memory budget."""
 
@@ -202,15 +231,7 @@ class GpuExecutor:
         return 2 * P * 4 + ws  # soft mask + output + workspace
 
     def _mask(self, img, req):
-        torch = self.torch
-        shape = img.shape[2:]
-        m = torch.ones((1, 1) + tuple(shape), device=self.device)
-        grids = torch.meshgrid(*[torch.arange(n, device=self.device) for n in shape], indexing="ij")
-        r2 = req.radius * req.radius
-        for c in req.clicks:
-            dist2 = sum((g - int(ci)) ** 2 for g, ci in zip(grids, c))
-            m[0, 0][dist2 <= r2] = 0.0
-        return m
+        return click_mask(tuple(img.shape[2:]), req.clicks, req.radius, self.device)
 
     def start(self, req: Request, slot: int):
         import fastgeodis_gb300 as fg

@@ -214,6 +214,15 @@ FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int ma
 FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
                                        int iterations, int *counter, int *status, void *stream);
 
+/* Soft mask of an interactive request from its clicks (no counterpart in the
+ * reference, whose callers build masks on the host): writes mask[D][H][W]
+ * (D = 1 for a 2D image) with 0.0 at every voxel within Euclidean distance
+ * `radius` of a click and 1.0 elsewhere.  clicks: host array of n_clicks
+ * (z, y, x) triples (z = 0 in 2D), at most 64; copied into the launch, so
+ * the array may be reused as soon as the call returns.  Exact integer test,
+ * one 4-byte write per voxel, on `stream`. */
+FG_API int fg_click_mask(float *mask, int D, int H, int W, const int *clicks, int n_clicks, int radius, void *stream);
+
 /* Allocation-free variant of fg_generalised_geodesic2d (no counterpart in
  * the reference).  For callers that cannot allocate device memory when they
  * need the transform -- code running inside a framework that owns the

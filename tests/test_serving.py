@@ -118,3 +118,45 @@ def test_gpu_mix_equals_standalone_calls():
         fg.check_status()
     finally:
         srv.close()
+
+
+def _torch_click_mask(shape, clicks, radius):
+    """Plain PyTorch reference of the click mask (on the CPU)."""
+    grids = torch.meshgrid(*[torch.arange(n) for n in shape], indexing="ij")
+    m = torch.ones(shape)
+    for c in clicks:
+        d2 = sum((g - int(ci)) ** 2 for g, ci in zip(grids, c))
+        m[d2 <= radius * radius] = 0.0
+    return m[None, None]
+
+
+def test_click_mask_argument_errors():
+    import ctypes
+
+    from fastgeodis_gb300 import _lib
+    from fastgeodis_gb300.serving import click_mask
+
+    L = _lib.load()
+    arr = (ctypes.c_int * 3)(0, 0, 0)
+    assert L.fg_click_mask(None, 1, 4, 4, arr, 1, 1, None) == _lib.FG_ERR_INVALID_ARGUMENT
+    big = (ctypes.c_int * 195)()
+    buf = (ctypes.c_float * 16)()
+    assert L.fg_click_mask(ctypes.cast(buf, ctypes.c_void_p), 1, 4, 4, big, 65, 1, None) == _lib.FG_ERR_UNSUPPORTED
+    assert L.fg_click_mask(ctypes.cast(buf, ctypes.c_void_p), 1, 4, 4, arr, 1, -1, None) == _lib.FG_ERR_INVALID_ARGUMENT
+    with pytest.raises(ValueError):
+        click_mask((4, 4), [(1, 2, 3)], 1, device="cpu")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,clicks,radius", [
+    ((300, 257), [(0, 0), (150, 100), (299, 256)], 3),
+    ((64, 65), [(10, 70), (-3, 5)], 4),           # clicks outside the image still mark what they reach
+    ((40, 64, 48), [(0, 0, 0), (20, 31, 47), (39, 63, 10)], 2),
+    ((17, 9, 33), [(8, 4, 16)], 0),               # radius 0: the click voxel only
+    ((5, 6, 7), [], 3),                           # no clicks: all ones
+])
+def test_click_mask_matches_torch(shape, clicks, radius):
+    from fastgeodis_gb300.serving import click_mask
+
+    got = click_mask(shape, clicks, radius).cpu()
+    assert torch.equal(got, _torch_click_mask(shape, clicks, radius))
