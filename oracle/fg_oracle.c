@@ -26,6 +26,9 @@
  *                                             fastgeodis_cpu.cpp:173-174
  *   - signed transform D(M) - D(1-M)         FastGeodis/fastgeodis.cpp:241-258
  *   - GSF composition                        FastGeodis/fastgeodis.cpp:319-343
+ *   - Toivanen's sequential raster scan (2D and 3D, plain / signed / GSF)
+ *                                             FastGeodis/geodis_toivanen.cpp:35-348,
+ *                                             FastGeodis/fastgeodis.cpp:260-277, 345-369
  *
  * The transposes of the reference are replaced by index arithmetic: the
  * value computed for every cell is the same expression on the same operands,
@@ -268,6 +271,182 @@ FGO_API void fgo_gsf3d(const float *img, int C, int Dd, int H, int W,
                        int iters, int nthreads)
 {
     gsf_common(1, img, C, Dd, H, W, mask, Cm, spacing, theta, out, v, lambda, iters, nthreads);
+}
+
+/* ------------------------------------------------------------------ */
+/* Toivanen's raster scan, float32, exact reference arithmetic         */
+/* ------------------------------------------------------------------ */
+/*
+ * FastGeodis/geodis_toivanen.cpp: L1 distance :35-38; 2D forward/backward
+ * pair :40-146 and driver :148-164; 3D pair :166-329 and driver :331-348.
+ * A forward pass visits every cell in memory order (depth, rows, columns)
+ * and replaces it by the minimum of itself and the candidates of its causal
+ * neighbours, which already hold this pass's values where they come earlier
+ * in the order (the 3D set also reads four cells of the next plane, which
+ * still hold the previous pass's values); the backward pass runs in reverse
+ * order with the mirrored set.  The reference runs it on one thread; so
+ * does this restatement.
+ */
+static float toiv_l1(const float *img, int C, int64_t cstr, int64_t a, int64_t b)
+{
+    if (C == 1)
+        return fabsf(img[a] - img[b]);
+    float s = 0.0f;
+    for (int c = 0; c < C; c++)
+        s += fabsf(img[c * cstr + a] - img[c * cstr + b]);
+    return s;
+}
+
+static void toiv_pass(const float *img, int C, int Dd, int H, int W, float *D, int n,
+                      const int *dz, const int *dh, const int *dw, const float *ld,
+                      int backward, float lg, float le)
+{
+    int64_t P = (int64_t)Dd * H * W, HW = (int64_t)H * W;
+    for (int64_t k = 0; k < P; k++) {
+        int64_t i = backward ? P - 1 - k : k;
+        int z = (int)(i / HW), h = (int)((i / W) % H), w = (int)(i % W);
+        float nd = D[i];
+        for (int j = 0; j < n; j++) {
+            int zi = z + dz[j], hi = h + dh[j], wi = w + dw[j];
+            if (zi < 0 || zi >= Dd || hi < 0 || hi >= H || wi < 0 || wi >= W)
+                continue;
+            int64_t q = ((int64_t)zi * H + hi) * W + wi;
+            float cur = D[q] + le * ld[j] + lg * toiv_l1(img, C, P, i, q);
+            if (cur < nd) /* std::min(new_dist, cur_dist) */
+                nd = cur;
+        }
+        D[i] = nd;
+    }
+}
+
+/* geodis_toivanen.cpp:56-57, 101-102 */
+static const int T2_DZ[4] = {0, 0, 0, 0};
+static const int T2F_DH[4] = {-1, -1, -1, 0}, T2F_DW[4] = {-1, 0, 1, -1};
+static const int T2B_DH[4] = {0, 1, 1, 1}, T2B_DW[4] = {1, -1, 0, 1};
+/* geodis_toivanen.cpp:182-184, 209-211 */
+static const int T3F_DZ[13] = {-1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1};
+static const int T3F_DH[13] = {-1, -1, -1, 0, 0, -1, -1, -1, 0, -1, -1, -1, 0};
+static const int T3F_DW[13] = {-1, 0, 1, -1, 0, -1, 0, 1, -1, -1, 0, 1, -1};
+static const int T3B_DZ[13] = {-1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1};
+static const int T3B_DH[13] = {0, 1, 1, 1, 0, 1, 1, 1, 0, 0, 1, 1, 1};
+static const int T3B_DW[13] = {1, -1, 0, 1, 1, -1, 0, 1, 0, 1, -1, 0, 1};
+
+FGO_API void fgo_toivanen2d(const float *img, int C, int H, int W, const float *mask,
+                            int Cm, float *out, float v, float lg, float le, int iters)
+{
+    int64_t P = (int64_t)H * W;
+    const float r2 = sqrtf(2.0f);
+    const float ldf[4] = {r2, 1.0f, r2, 1.0f}, ldb[4] = {1.0f, r2, 1.0f, r2};
+    for (int64_t i = 0; i < (int64_t)Cm * P; i++)
+        out[i] = v * mask[i];
+    for (int it = 0; it < iters; it++) {
+        toiv_pass(img, C, 1, H, W, out, 4, T2_DZ, T2F_DH, T2F_DW, ldf, 0, lg, le);
+        toiv_pass(img, C, 1, H, W, out, 4, T2_DZ, T2B_DH, T2B_DW, ldb, 1, lg, le);
+    }
+}
+
+/* geodis_toivanen.cpp:186-207, 213-234: sqrt of the summed squared spacings
+ * of the axes a neighbour moves along, summed in axis order */
+static void toiv_table(const float *sp, const int *dz, const int *dh, const int *dw, float *ld)
+{
+    for (int i = 0; i < 13; i++) {
+        float v = 0.0f;
+        if (dz[i] != 0) v += sp[0] * sp[0];
+        if (dh[i] != 0) v += sp[1] * sp[1];
+        if (dw[i] != 0) v += sp[2] * sp[2];
+        ld[i] = sqrtf(v);
+    }
+}
+
+FGO_API void fgo_toivanen3d(const float *img, int C, int Dd, int H, int W,
+                            const float *mask, int Cm, const float *spacing,
+                            float *out, float v, float lg, float le, int iters)
+{
+    int64_t P = (int64_t)Dd * H * W;
+    float ldf[13], ldb[13];
+    toiv_table(spacing, T3F_DZ, T3F_DH, T3F_DW, ldf);
+    toiv_table(spacing, T3B_DZ, T3B_DH, T3B_DW, ldb);
+    for (int64_t i = 0; i < (int64_t)Cm * P; i++)
+        out[i] = v * mask[i];
+    for (int it = 0; it < iters; it++) {
+        toiv_pass(img, C, Dd, H, W, out, 13, T3F_DZ, T3F_DH, T3F_DW, ldf, 0, lg, le);
+        toiv_pass(img, C, Dd, H, W, out, 13, T3B_DZ, T3B_DH, T3B_DW, ldb, 1, lg, le);
+    }
+}
+
+/* Signed and GSF compositions of the Toivanen transform: FastGeodis/fastgeodis.cpp
+ * :260-277 (D(M) - D(1-M)) and :345-369 (GSF), the same as the raster ones. */
+static void toiv_signed(int is3d, const float *img, int C, int Dd, int H, int W,
+                        const float *mask, int Cm, const float *spacing, float *out,
+                        float v, float lg, float le, int iters)
+{
+    int64_t n = (int64_t)Cm * Dd * H * W;
+    float *inv = (float *)malloc(n * sizeof(float));
+    float *db = (float *)malloc(n * sizeof(float));
+    for (int64_t i = 0; i < n; i++)
+        inv[i] = 1.0f - mask[i];
+    if (is3d) {
+        fgo_toivanen3d(img, C, Dd, H, W, mask, Cm, spacing, out, v, lg, le, iters);
+        fgo_toivanen3d(img, C, Dd, H, W, inv, Cm, spacing, db, v, lg, le, iters);
+    } else {
+        fgo_toivanen2d(img, C, H, W, mask, Cm, out, v, lg, le, iters);
+        fgo_toivanen2d(img, C, H, W, inv, Cm, db, v, lg, le, iters);
+    }
+    for (int64_t i = 0; i < n; i++)
+        out[i] = out[i] - db[i];
+    free(inv);
+    free(db);
+}
+
+FGO_API void fgo_signed_toivanen2d(const float *img, int C, int H, int W, const float *mask,
+                                   int Cm, float *out, float v, float lg, float le, int iters)
+{
+    toiv_signed(0, img, C, 1, H, W, mask, Cm, NULL, out, v, lg, le, iters);
+}
+
+FGO_API void fgo_signed_toivanen3d(const float *img, int C, int Dd, int H, int W,
+                                   const float *mask, int Cm, const float *spacing,
+                                   float *out, float v, float lg, float le, int iters)
+{
+    toiv_signed(1, img, C, Dd, H, W, mask, Cm, spacing, out, v, lg, le, iters);
+}
+
+static void toiv_gsf(int is3d, const float *img, int C, int Dd, int H, int W,
+                     const float *mask, int Cm, const float *spacing, float theta,
+                     float *out, float v, float lambda, int iters)
+{
+    int64_t n = (int64_t)Cm * Dd * H * W;
+    float le = 1.0f - lambda;
+    float *ds = (float *)malloc(n * sizeof(float));
+    float *a = (float *)malloc(n * sizeof(float));
+    float *s1 = (float *)malloc(n * sizeof(float));
+    float *s2 = (float *)malloc(n * sizeof(float));
+    toiv_signed(is3d, img, C, Dd, H, W, mask, Cm, spacing, ds, v, lambda, le, iters);
+    for (int64_t i = 0; i < n; i++)
+        a[i] = 1.0f - (ds[i] > theta ? 1.0f : 0.0f);
+    toiv_signed(is3d, img, C, Dd, H, W, a, Cm, spacing, s1, v, lambda, le, iters);
+    for (int64_t i = 0; i < n; i++)
+        a[i] = ds[i] > -theta ? 1.0f : 0.0f;
+    toiv_signed(is3d, img, C, Dd, H, W, a, Cm, spacing, s2, v, lambda, le, iters);
+    for (int64_t i = 0; i < n; i++)
+        out[i] = -s1[i] + s2[i];
+    free(ds);
+    free(a);
+    free(s1);
+    free(s2);
+}
+
+FGO_API void fgo_gsf_toivanen2d(const float *img, int C, int H, int W, const float *mask,
+                                int Cm, float theta, float *out, float v, float lambda, int iters)
+{
+    toiv_gsf(0, img, C, 1, H, W, mask, Cm, NULL, theta, out, v, lambda, iters);
+}
+
+FGO_API void fgo_gsf_toivanen3d(const float *img, int C, int Dd, int H, int W,
+                                const float *mask, int Cm, float theta, const float *spacing,
+                                float *out, float v, float lambda, int iters)
+{
+    toiv_gsf(1, img, C, Dd, H, W, mask, Cm, spacing, theta, out, v, lambda, iters);
 }
 
 /* ------------------------------------------------------------------ */

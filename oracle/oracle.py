@@ -36,6 +36,12 @@ def lib():
         L.fgo_gsf3d.argtypes = [f32p, i, i, i, i, f32p, i, f, f32p, f32p, f, f, i, i]
         L.fgo_geodesic2d_f64.argtypes = [f64p, i, i, i, f64p, i, f64p, d, d, d, i, i]
         L.fgo_geodesic3d_f64.argtypes = [f64p, i, i, i, i, f64p, i, f64p, f64p, d, d, d, i, i]
+        L.fgo_toivanen2d.argtypes = [f32p, i, i, i, f32p, i, f32p, f, f, f, i]
+        L.fgo_toivanen3d.argtypes = [f32p, i, i, i, i, f32p, i, f32p, f32p, f, f, f, i]
+        L.fgo_signed_toivanen2d.argtypes = L.fgo_toivanen2d.argtypes
+        L.fgo_signed_toivanen3d.argtypes = L.fgo_toivanen3d.argtypes
+        L.fgo_gsf_toivanen2d.argtypes = [f32p, i, i, i, f32p, i, f, f32p, f, f, i]
+        L.fgo_gsf_toivanen3d.argtypes = [f32p, i, i, i, i, f32p, i, f, f32p, f32p, f, f, i]
         L.fgo_max_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -127,6 +133,49 @@ def gsf3d(image, mask, theta, spacing, v, lamb, iterations, nthreads=None):
     lib().fgo_gsf3d(_p32(image), C, D, H, W, _p32(mask), mask.shape[0], float(np.float32(theta)),
                     _p32(sp), _p32(out), float(np.float32(v)), float(np.float32(lamb)),
                     int(iterations), _threads(nthreads))
+    return out
+
+
+# Toivanen's sequential raster scan (FastGeodis/geodis_toivanen.cpp), one thread.
+
+def toivanen2d(image, mask, v, lamb, iterations=2, signed=False):
+    image, mask = _f32(image), _f32(mask)
+    C, H, W = image.shape
+    out = np.empty(mask.shape, np.float32)
+    fn = lib().fgo_signed_toivanen2d if signed else lib().fgo_toivanen2d
+    fn(_p32(image), C, H, W, _p32(mask), mask.shape[0], _p32(out), float(np.float32(v)),
+       float(np.float32(lamb)), _l_eucl_from_python(lamb), int(iterations))
+    return out
+
+
+def toivanen3d(image, mask, spacing, v, lamb, iterations=4, signed=False):
+    image, mask = _f32(image), _f32(mask)
+    C, D, H, W = image.shape
+    sp = np.asarray(spacing, np.float32)
+    out = np.empty(mask.shape, np.float32)
+    fn = lib().fgo_signed_toivanen3d if signed else lib().fgo_toivanen3d
+    fn(_p32(image), C, D, H, W, _p32(mask), mask.shape[0], _p32(sp), _p32(out), float(np.float32(v)),
+       float(np.float32(lamb)), _l_eucl_from_python(lamb), int(iterations))
+    return out
+
+
+def gsf_toivanen2d(image, mask, theta, v, lamb, iterations):
+    image, mask = _f32(image), _f32(mask)
+    C, H, W = image.shape
+    out = np.empty(mask.shape, np.float32)
+    lib().fgo_gsf_toivanen2d(_p32(image), C, H, W, _p32(mask), mask.shape[0], float(np.float32(theta)),
+                             _p32(out), float(np.float32(v)), float(np.float32(lamb)), int(iterations))
+    return out
+
+
+def gsf_toivanen3d(image, mask, theta, spacing, v, lamb, iterations):
+    image, mask = _f32(image), _f32(mask)
+    C, D, H, W = image.shape
+    sp = np.asarray(spacing, np.float32)
+    out = np.empty(mask.shape, np.float32)
+    lib().fgo_gsf_toivanen3d(_p32(image), C, D, H, W, _p32(mask), mask.shape[0], float(np.float32(theta)),
+                             _p32(sp), _p32(out), float(np.float32(v)), float(np.float32(lamb)),
+                             int(iterations))
     return out
 
 

@@ -95,6 +95,32 @@ def cases(rng):
     m = np.ones((1, 1, 6, 9), np.float32); m[0, 0, 2, 2] = 0
     out.append(dict(name="g3d_d1", op="geodesic3d", image=img, mask=m, v=1e10, lamb=0.5, iter=2,
                     spacing=[1.0, 1.5, 0.5]))
+    # Toivanen's raster scan (FastGeodis/geodis_toivanen.cpp), same families
+    img = smooth_noise(rng, (45, 38), 3.0, 0, 255)[None]
+    m = disks(rng, (45, 38), 3, 3)[None]
+    for lamb in (0.0, 0.6, 1.0):
+        out.append(dict(name=f"t2d_l{lamb}", op="toivanen2d", image=img, mask=m, v=1e10, lamb=lamb, iter=2))
+    out.append(dict(name="ts2d", op="signed_toivanen2d", image=img, mask=m, v=1e10, lamb=0.7, iter=1))
+    out.append(dict(name="tgsf2d", op="gsf_toivanen2d", image=img, mask=m, v=1e10, lamb=0.8, iter=2, theta=0.5))
+    img = (rng.random((3, 20, 33)) * 255).astype(np.float32)
+    m = rng.random((2, 20, 33)).astype(np.float32)
+    out.append(dict(name="t2d_c3_cm2", op="toivanen2d", image=img, mask=m, v=4.0, lamb=0.5, iter=3))
+    img = (rng.random((1, 1, 23)) * 10).astype(np.float32)
+    m = np.ones((1, 1, 23), np.float32); m[0, 0, 9] = 0
+    out.append(dict(name="t2d_h1", op="toivanen2d", image=img, mask=m, v=1e10, lamb=0.5, iter=2))
+    img = smooth_noise(rng, (9, 12, 14), 2.0, 0, 1)[None]
+    m = np.ones((1, 9, 12, 14), np.float32); m[0, 3:5, 4:6, 5:8] = 0
+    for lamb in (0.0, 0.5, 1.0):
+        out.append(dict(name=f"t3d_l{lamb}", op="toivanen3d", image=img, mask=m, v=1e10, lamb=lamb, iter=2,
+                        spacing=[2.0, 0.5, 0.7]))
+    out.append(dict(name="ts3d", op="signed_toivanen3d", image=img, mask=m, v=1e10, lamb=1.0, iter=2,
+                    spacing=[1.0, 1.0, 1.0]))
+    out.append(dict(name="tgsf3d", op="gsf_toivanen3d", image=img, mask=m, v=1e10, lamb=1.0, iter=1,
+                    spacing=[2.0, 0.5, 0.5], theta=0.01))
+    img = rng.random((2, 5, 7, 6)).astype(np.float32)
+    m = disks(rng, (5, 7, 6), 1, 1)[None]
+    out.append(dict(name="t3d_c2", op="toivanen3d", image=img, mask=m, v=1e10, lamb=0.5, iter=3,
+                    spacing=[1.0, 1.5, 0.5]))
     return out
 
 
@@ -118,6 +144,18 @@ def run_reference(ref, c):
         r = ref.GSF2d(img, m, c["theta"], v, lamb, it)
     elif op == "gsf3d":
         r = ref.GSF3d(img, m, c["theta"], c["spacing"], v, lamb, it)
+    elif op == "toivanen2d":
+        r = ref.generalised_geodesic2d_toivanen(img, m, v, lamb, 1 - lamb, it)
+    elif op == "toivanen3d":
+        r = ref.generalised_geodesic3d_toivanen(img, m, c["spacing"], v, lamb, 1 - lamb, it)
+    elif op == "signed_toivanen2d":
+        r = ref.signed_generalised_geodesic2d_toivanen(img, m, v, lamb, 1 - lamb, it)
+    elif op == "signed_toivanen3d":
+        r = ref.signed_generalised_geodesic3d_toivanen(img, m, c["spacing"], v, lamb, 1 - lamb, it)
+    elif op == "gsf_toivanen2d":
+        r = ref.GSF2d_toivanen(img, m, c["theta"], v, lamb, it)
+    elif op == "gsf_toivanen3d":
+        r = ref.GSF3d_toivanen(img, m, c["theta"], c["spacing"], v, lamb, it)
     else:
         raise ValueError(op)
     return r[0].numpy()

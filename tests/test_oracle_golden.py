@@ -27,13 +27,27 @@ def run_oracle(c):
         return oracle.gsf2d(img, m, c["theta"], v, lamb, it)
     if op == "gsf3d":
         return oracle.gsf3d(img, m, c["theta"], c["spacing"], v, lamb, it)
+    if op == "toivanen2d":
+        return oracle.toivanen2d(img, m, v, lamb, it)
+    if op == "toivanen3d":
+        return oracle.toivanen3d(img, m, c["spacing"], v, lamb, it)
+    if op == "signed_toivanen2d":
+        return oracle.toivanen2d(img, m, v, lamb, it, signed=True)
+    if op == "signed_toivanen3d":
+        return oracle.toivanen3d(img, m, c["spacing"], v, lamb, it, signed=True)
+    if op == "gsf_toivanen2d":
+        return oracle.gsf_toivanen2d(img, m, c["theta"], v, lamb, it)
+    if op == "gsf_toivanen3d":
+        return oracle.gsf_toivanen3d(img, m, c["theta"], c["spacing"], v, lamb, it)
     raise ValueError(op)
 
 
 def test_golden_set_present():
-    assert len(CASES) >= 20
+    assert len(CASES) >= 35
     ops = {c["op"] for c in CASES.values()}
-    assert ops == {"geodesic2d", "geodesic3d", "signed2d", "signed3d", "gsf2d", "gsf3d"}
+    assert ops == {"geodesic2d", "geodesic3d", "signed2d", "signed3d", "gsf2d", "gsf3d",
+                   "toivanen2d", "toivanen3d", "signed_toivanen2d", "signed_toivanen3d",
+                   "gsf_toivanen2d", "gsf_toivanen3d"}
 
 
 @pytest.mark.parametrize("name", names())

@@ -16,6 +16,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 CASES = {c["name"]: c for c in load_all()}
+RASTER = [n for n in names() if "toivanen" not in CASES[n]["op"]]  # Toivanen's scan: test_toivanen_gpu.py
 DEV = "cuda"
 
 
@@ -48,7 +49,7 @@ def tuning():
     _lib.check(L.fg_set_tuning(0, 0))
 
 
-@pytest.mark.parametrize("name", names())
+@pytest.mark.parametrize("name", RASTER)
 def test_golden_bits(name):
     c = CASES[name]
     got = run_gpu(c)
