@@ -40,6 +40,12 @@ __all__ = [
     "signed_generalised_geodesic3d",
     "GSF2d",
     "GSF3d",
+    "generalised_geodesic2d_toivanen",
+    "generalised_geodesic3d_toivanen",
+    "signed_generalised_geodesic2d_toivanen",
+    "signed_generalised_geodesic3d_toivanen",
+    "GSF2d_toivanen",
+    "GSF3d_toivanen",
     "check_status",
 ]
 
@@ -119,7 +125,7 @@ def _workspace(device: torch.device, nbytes: int, stream) -> torch.Tensor:
         return ws
 
 
-def _run(kind: str, image, mask, v, lamb, iterations, spacing=None, theta=None):
+def _run(kind: str, image, mask, v, lamb, iterations, spacing=None, theta=None, toivanen=False):
     is3d = kind.endswith("3d")
     dims = 5 if is3d else 4
     _check_input_dimensions(image, mask, dims)
@@ -156,23 +162,25 @@ def _run(kind: str, image, mask, v, lamb, iterations, spacing=None, theta=None):
         ptr = lambda t: t.data_ptr()  # noqa: E731
         if is3d:
             sp = (_ctypes_float3(spacing))
+        # the C entry of this kind; Toivanen's scan has the same arguments under a suffixed name
+        fn = lambda name: getattr(L, name + ("_toivanen" if toivanen else ""))  # noqa: E731
         if kind == "plain2d":
-            rc = L.fg_generalised_geodesic2d(ptr(img), C, H, W, ptr(msk), Cm, ptr(out), vf, lg, le, it,
+            rc = fn("fg_generalised_geodesic2d")(ptr(img), C, H, W, ptr(msk), Cm, ptr(out), vf, lg, le, it,
                                              ptr(ws), ws.numel(), sh)
         elif kind == "signed2d":
-            rc = L.fg_signed_generalised_geodesic2d(ptr(img), C, H, W, ptr(msk), Cm, ptr(out), vf, lg, le,
+            rc = fn("fg_signed_generalised_geodesic2d")(ptr(img), C, H, W, ptr(msk), Cm, ptr(out), vf, lg, le,
                                                     it, ptr(ws), ws.numel(), sh)
         elif kind == "plain3d":
-            rc = L.fg_generalised_geodesic3d(ptr(img), C, D, H, W, ptr(msk), Cm, sp, ptr(out), vf, lg, le,
+            rc = fn("fg_generalised_geodesic3d")(ptr(img), C, D, H, W, ptr(msk), Cm, sp, ptr(out), vf, lg, le,
                                              it, ptr(ws), ws.numel(), sh)
         elif kind == "signed3d":
-            rc = L.fg_signed_generalised_geodesic3d(ptr(img), C, D, H, W, ptr(msk), Cm, sp, ptr(out), vf,
+            rc = fn("fg_signed_generalised_geodesic3d")(ptr(img), C, D, H, W, ptr(msk), Cm, sp, ptr(out), vf,
                                                     lg, le, it, ptr(ws), ws.numel(), sh)
         elif kind == "gsf2d":
-            rc = L.fg_GSF2d(ptr(img), C, H, W, ptr(msk), Cm, float(theta), vf, lam, it, ptr(out), ptr(ws),
+            rc = fn("fg_GSF2d")(ptr(img), C, H, W, ptr(msk), Cm, float(theta), vf, lam, it, ptr(out), ptr(ws),
                             ws.numel(), sh)
         elif kind == "gsf3d":
-            rc = L.fg_GSF3d(ptr(img), C, D, H, W, ptr(msk), Cm, float(theta), sp, vf, lam, it, ptr(out),
+            rc = fn("fg_GSF3d")(ptr(img), C, D, H, W, ptr(msk), Cm, float(theta), sp, vf, lam, it, ptr(out),
                             ptr(ws), ws.numel(), sh)
         else:  # pragma: no cover
             raise AssertionError(kind)
@@ -268,6 +276,53 @@ def GSF3d(image: torch.Tensor, softmask: torch.Tensor, theta: float, spacing: Li
           iter: int):
     r"""Geodesic symmetric filtering of a 3D soft mask."""
     return _run("gsf3d", image, softmask, v, lamb, iter, spacing=spacing, theta=theta)
+
+
+# ---------------------------------------------------------------------------
+# Toivanen's raster scan (FastGeodis/__init__.py:165-308, 587-656).  The
+# reference runs it on the CPU only and rejects CUDA tensors; here CPU tensors
+# give the reference's CPU bits (computed on the GPU by a wavefront of the same
+# sequential scan) and CUDA tensors are accepted as well.
+# ---------------------------------------------------------------------------
+
+def generalised_geodesic2d_toivanen(image: torch.Tensor, softmask: torch.Tensor, v: float, lamb: float,
+                                    iter: int = 2):
+    r"""Generalised geodesic distance of a 2D image by Toivanen's raster scan
+    (Toivanen, Pattern Recognition Letters 17.5, 1996): one forward and one
+    backward pass over the whole image per iteration, each cell taking the
+    minimum over its four causal neighbours.  Arguments as in
+    :func:`generalised_geodesic2d`."""
+    return _run("plain2d", image, softmask, v, lamb, iter, toivanen=True)
+
+
+def generalised_geodesic3d_toivanen(image: torch.Tensor, softmask: torch.Tensor, spacing: List, v: float,
+                                    lamb: float, iter: int = 4):
+    r"""Generalised geodesic distance of a 3D volume by Toivanen's raster scan
+    (13 neighbours per pass).  Arguments as in :func:`generalised_geodesic3d`."""
+    return _run("plain3d", image, softmask, v, lamb, iter, spacing=spacing, toivanen=True)
+
+
+def signed_generalised_geodesic2d_toivanen(image: torch.Tensor, softmask: torch.Tensor, v: float, lamb: float,
+                                           iter: int = 2):
+    r"""Signed distance ``D(softmask) - D(1 - softmask)`` by Toivanen's scan, 2D."""
+    return _run("signed2d", image, softmask, v, lamb, iter, toivanen=True)
+
+
+def signed_generalised_geodesic3d_toivanen(image: torch.Tensor, softmask: torch.Tensor, spacing: List, v: float,
+                                           lamb: float, iter: int = 4):
+    r"""Signed distance ``D(softmask) - D(1 - softmask)`` by Toivanen's scan, 3D."""
+    return _run("signed3d", image, softmask, v, lamb, iter, spacing=spacing, toivanen=True)
+
+
+def GSF2d_toivanen(image: torch.Tensor, softmask: torch.Tensor, theta: float, v: float, lamb: float, iter: int):
+    r"""Geodesic symmetric filtering (as :func:`GSF2d`) by Toivanen's scan."""
+    return _run("gsf2d", image, softmask, v, lamb, iter, theta=theta, toivanen=True)
+
+
+def GSF3d_toivanen(image: torch.Tensor, softmask: torch.Tensor, theta: float, spacing: List, v: float, lamb: float,
+                   iter: int):
+    r"""Geodesic symmetric filtering (as :func:`GSF3d`) by Toivanen's scan."""
+    return _run("gsf3d", image, softmask, v, lamb, iter, spacing=spacing, theta=theta, toivanen=True)
 
 
 from .batch import GeodesicBatch2d, generalised_geodesic2d_batch, signed_generalised_geodesic2d_batch  # noqa: E402

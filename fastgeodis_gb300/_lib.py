@@ -33,6 +33,9 @@ EXPORTED = (
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
     "fg_grad_geodesic2d_forward", "fg_grad_geodesic2d_backward",
     "fg_generalised_geodesic2d_noalloc", "fg_click_mask",
+    "fg_generalised_geodesic2d_toivanen", "fg_generalised_geodesic3d_toivanen",
+    "fg_signed_generalised_geodesic2d_toivanen", "fg_signed_generalised_geodesic3d_toivanen",
+    "fg_GSF2d_toivanen", "fg_GSF3d_toivanen",
 )
 
 _lib = None
@@ -84,6 +87,9 @@ def load():
     L.fg_grad_geodesic2d_forward.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_grad_geodesic2d_backward.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
+    for name in ("fg_generalised_geodesic2d", "fg_generalised_geodesic3d", "fg_signed_generalised_geodesic2d",
+                 "fg_signed_generalised_geodesic3d", "fg_GSF2d", "fg_GSF3d"):
+        getattr(L, name + "_toivanen").argtypes = getattr(L, name).argtypes  # same arguments
     for name in EXPORTED:
         if name not in ("fg_last_error",):
             getattr(L, name).restype = getattr(L, name).restype or i

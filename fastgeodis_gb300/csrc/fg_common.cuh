@@ -110,6 +110,11 @@ constexpr int max_pass_depth(int nch, int m) { return (nch + m <= 4) ? 8 : 2; }
 int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 
+// Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
+// in place, one CTA each; spacing_sq = nullptr for images.
+int launch_toivanen(const float *img, int C, int D, int H, int W, const float *spacing_sq, float *const *maps,
+                    int nmaps, float lg, float le, int iterations, cudaStream_t s);
+
 // Host error reporting shared by the units.
 int set_error(int code, const char *msg);
 

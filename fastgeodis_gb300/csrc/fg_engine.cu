@@ -618,9 +618,12 @@ int check_common(const float *image, int C, int D, int H, int W, const float *ma
   return FG_OK;
 }
 
-// Common driver for plain / signed / GSF in 2D and 3D.
+// Common driver for plain / signed / GSF in 2D and 3D, by the raster scan of
+// fastgeodis_cpu.cpp (toivanen = false) or Toivanen's scan of
+// geodis_toivanen.cpp (toivanen = true); the compositions are the same
+// (FastGeodis/fastgeodis.cpp:241-258, 319-343 and :260-277, 345-369).
 int run_op(int op, const Geometry &g, const float *image, const float *mask, int Cm, float *out, float v, float lg,
-           float le, float theta, int iterations, void *ws, size_t ws_bytes, void *stream) {
+           float le, float theta, int iterations, void *ws, size_t ws_bytes, void *stream, bool toivanen = false) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int rc = check_common(image, g.C, g.D, g.H, g.W, mask, Cm, out);
   if (rc != FG_OK) return rc;
@@ -636,14 +639,20 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   float *xt[4] = {tb, tb + ms_, tb + 2 * ms_, tb + 3 * ms_};          // transposed-layout maps
   float *img_t = tb + t_maps(op) * ms_;
   // epoch 0 is never wanted; earlier calls' words must not match this call's epochs
-  FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
+  if (!toivanen) FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
   unsigned counter = 0;
+  auto sweep = [&](const MapSet &ms) {
+    if (toivanen)
+      return launch_toivanen(image, g.C, g.is3d ? g.D : 1, g.H, g.W, g.is3d ? g.spacing_sq : nullptr, ms.r, ms.M,
+                             ms.lg, ms.le, iterations, s);
+    return run_transform(g, image, img_t, ms, iterations, w, &counter, s);
+  };
   if (Cm > 1) {
     long long n = (long long)(Cm - 1) * P;
     fg_unswept_kernel<<<ew_grid(n), 256, 0, s>>>(out + P, mask + P, n, v, theta, op);
     FG_CUDA(cudaGetLastError());
   }
-  if (iterations > 0) {
+  if (iterations > 0 && !toivanen) {
     dim3 tg((g.W + 31) / 32, (g.H + 31) / 32, g.C * g.D);
     fg_transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(image, img_t, g.D, g.H, g.W);
     FG_CUDA(cudaGetLastError());
@@ -652,14 +661,14 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
     fg_init_kernel<<<ew_grid(P), 256, 0, s>>>(out, mask, P, v, INIT_VM);
     FG_CUDA(cudaGetLastError());
     MapSet ms{1, {out}, {xt[0]}, lg, le};
-    return run_transform(g, image, img_t, ms, iterations, w, &counter, s);
+    return sweep(ms);
   }
   if (op == FG_OP_SIGNED) {
     fg_init_kernel<<<ew_grid(P), 256, 0, s>>>(out, mask, P, v, INIT_VM);
     fg_init_kernel<<<ew_grid(P), 256, 0, s>>>(xr[0], mask, P, v, INIT_V1M);
     FG_CUDA(cudaGetLastError());
     MapSet ms{2, {out, xr[0]}, {xt[0], xt[1]}, lg, le};
-    rc = run_transform(g, image, img_t, ms, iterations, w, &counter, s);
+    rc = sweep(ms);
     if (rc != FG_OK) return rc;
     fg_sub_kernel<<<ew_grid(P), 256, 0, s>>>(out, out, xr[0], P);
     FG_CUDA(cudaGetLastError());
@@ -671,7 +680,7 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   FG_CUDA(cudaGetLastError());
   {
     MapSet ms{2, {xr[0], xr[1]}, {xt[0], xt[1]}, lg, le};
-    rc = run_transform(g, image, img_t, ms, iterations, w, &counter, s);
+    rc = sweep(ms);
     if (rc != FG_OK) return rc;
   }
   // Ds = xr0 - xr1; the four initial maps go to out, xr1, xr2, xr3
@@ -679,7 +688,7 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   FG_CUDA(cudaGetLastError());
   {
     MapSet ms{4, {out, xr[1], xr[2], xr[3]}, {xt[0], xt[1], xt[2], xt[3]}, lg, le};
-    rc = run_transform(g, image, img_t, ms, iterations, w, &counter, s);
+    rc = sweep(ms);
     if (rc != FG_OK) return rc;
   }
   fg_gsf_final_kernel<<<ew_grid(P), 256, 0, s>>>(out, out, xr[1], xr[2], xr[3], P);
@@ -882,6 +891,62 @@ int fg_GSF3d(const float *image, int C, int D, int H, int W, const float *mask, 
   const float le = 1.0f - lambda;
   return run_op(FG_OP_GSF, g, image, mask, Cm, out, v, lambda, le, theta, iterations, workspace, workspace_bytes,
                 stream);
+}
+
+// Toivanen's raster scan (FastGeodis/fastgeodis.cpp:148-177, 260-277, 345-369;
+// CPU only in the reference): same arguments as the raster entries above.
+int fg_generalised_geodesic2d_toivanen(const float *image, int C, int H, int W, const float *mask, int Cm, float *out,
+                                       float v, float l_grad, float l_eucl, int iterations, void *workspace,
+                                       size_t workspace_bytes, void *stream) {
+  return run_op(FG_OP_PLAIN, geom2d(C, H, W), image, mask, Cm, out, v, l_grad, l_eucl, 0.0f, iterations, workspace,
+                workspace_bytes, stream, true);
+}
+
+int fg_generalised_geodesic3d_toivanen(const float *image, int C, int D, int H, int W, const float *mask, int Cm,
+                                       const float *spacing, float *out, float v, float l_grad, float l_eucl,
+                                       int iterations, void *workspace, size_t workspace_bytes, void *stream) {
+  Geometry g;
+  int rc = geom3d(C, D, H, W, spacing, &g);
+  if (rc != FG_OK) return rc;
+  return run_op(FG_OP_PLAIN, g, image, mask, Cm, out, v, l_grad, l_eucl, 0.0f, iterations, workspace, workspace_bytes,
+                stream, true);
+}
+
+int fg_signed_generalised_geodesic2d_toivanen(const float *image, int C, int H, int W, const float *mask, int Cm,
+                                              float *out, float v, float l_grad, float l_eucl, int iterations,
+                                              void *workspace, size_t workspace_bytes, void *stream) {
+  return run_op(FG_OP_SIGNED, geom2d(C, H, W), image, mask, Cm, out, v, l_grad, l_eucl, 0.0f, iterations, workspace,
+                workspace_bytes, stream, true);
+}
+
+int fg_signed_generalised_geodesic3d_toivanen(const float *image, int C, int D, int H, int W, const float *mask,
+                                              int Cm, const float *spacing, float *out, float v, float l_grad,
+                                              float l_eucl, int iterations, void *workspace, size_t workspace_bytes,
+                                              void *stream) {
+  Geometry g;
+  int rc = geom3d(C, D, H, W, spacing, &g);
+  if (rc != FG_OK) return rc;
+  return run_op(FG_OP_SIGNED, g, image, mask, Cm, out, v, l_grad, l_eucl, 0.0f, iterations, workspace,
+                workspace_bytes, stream, true);
+}
+
+int fg_GSF2d_toivanen(const float *image, int C, int H, int W, const float *mask, int Cm, float theta, float v,
+                      float lambda, int iterations, float *out, void *workspace, size_t workspace_bytes,
+                      void *stream) {
+  const float le = 1.0f - lambda;  // float arithmetic, FastGeodis/fastgeodis.cpp:347
+  return run_op(FG_OP_GSF, geom2d(C, H, W), image, mask, Cm, out, v, lambda, le, theta, iterations, workspace,
+                workspace_bytes, stream, true);
+}
+
+int fg_GSF3d_toivanen(const float *image, int C, int D, int H, int W, const float *mask, int Cm, float theta,
+                      const float *spacing, float v, float lambda, int iterations, float *out, void *workspace,
+                      size_t workspace_bytes, void *stream) {
+  Geometry g;
+  int rc = geom3d(C, D, H, W, spacing, &g);
+  if (rc != FG_OK) return rc;
+  const float le = 1.0f - lambda;
+  return run_op(FG_OP_GSF, g, image, mask, Cm, out, v, lambda, le, theta, iterations, workspace, workspace_bytes,
+                stream, true);
 }
 
 }  // extern "C"

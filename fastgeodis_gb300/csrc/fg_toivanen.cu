@@ -1,0 +1,187 @@
+// Toivanen's raster scan on the GPU, as a wavefront.
+//
+// Reference: FastGeodis/geodis_toivanen.cpp (CPU only there; one thread).
+// Each iteration is a forward pass that visits every cell in memory order
+// (depth, rows, columns) and replaces it by the minimum of itself and the
+// candidates (D[n] + l_eucl*ld[n]) + l_grad*L1 of its causal neighbours n,
+// then a backward pass in reverse order with the mirrored neighbour set
+// (2D :40-146, 3D :166-329).  A cell reads neighbours that the sequential
+// order has already updated in this pass and, in 3D, four cells of the next
+// plane that it has not (they keep the previous pass's values).
+//
+// Wavefront: give cell (z, h, w) the wave t = 4z + 2h + w (2D: z = 0).  Every
+// neighbour the sequential order updates first has a smaller wave (offsets
+// change t by -7 .. -1) and each next-plane neighbour a larger one (+1 .. +3),
+// so sweeping the waves in order, the cells of a wave in parallel and a
+// barrier between waves, every cell reads exactly the values the sequential
+// scan reads: the results are the reference's bits.  The backward pass is the
+// same schedule on the mirrored coordinates.
+//
+// One CTA sweeps one distance map (signed and GSF run their maps on separate
+// CTAs); data stays in global memory (L1/L2) and the CTA's barrier orders the
+// waves, so nothing waits on another CTA.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fg_common.cuh"
+
+namespace fgi {
+namespace {
+
+constexpr int kToivMaps = 4;
+
+struct ToivArgs {
+  const float *img;   // [C][D][H][W]
+  long long img_cs;   // elements between channels
+  int C;
+  float *dist[kToivMaps];  // one map per CTA, [D][H][W] (channel 0 of the distance tensor)
+  int D, H, W;             // D = 1 for images
+  float lg, le;
+  float ldf[13], ldb[13];  // step lengths of the forward and backward neighbours
+  int iterations;
+};
+
+// Neighbour offsets (dz, dh, dw) in the reference's order:
+// 2D forward / backward geodis_toivanen.cpp:56-57, 101-102;
+// 3D forward / backward :182-184, :209-211.
+template <bool IS3D, bool BWD>
+__device__ __forceinline__ void toiv_offset(int j, int &dz, int &dh, int &dw) {
+  if (!IS3D) {
+    constexpr int fh[4] = {-1, -1, -1, 0}, fw[4] = {-1, 0, 1, -1};
+    constexpr int bh[4] = {0, 1, 1, 1}, bw[4] = {1, -1, 0, 1};
+    dz = 0;
+    dh = BWD ? bh[j] : fh[j];
+    dw = BWD ? bw[j] : fw[j];
+  } else {
+    constexpr int fz[13] = {-1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1};
+    constexpr int fh[13] = {-1, -1, -1, 0, 0, -1, -1, -1, 0, -1, -1, -1, 0};
+    constexpr int fw[13] = {-1, 0, 1, -1, 0, -1, 0, 1, -1, -1, 0, 1, -1};
+    constexpr int bz[13] = {-1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1};
+    constexpr int bh[13] = {0, 1, 1, 1, 0, 1, 1, 1, 0, 0, 1, 1, 1};
+    constexpr int bw[13] = {1, -1, 0, 1, 1, -1, 0, 1, 0, 1, -1, 0, 1};
+    dz = BWD ? bz[j] : fz[j];
+    dh = BWD ? bh[j] : fh[j];
+    dw = BWD ? bw[j] : fw[j];
+  }
+}
+
+template <bool IS3D, bool BWD>
+__device__ __forceinline__ void toiv_cell(const ToivArgs &a, float *dm, int z, int h, int w) {
+  constexpr int N = IS3D ? 13 : 4;
+  const int H = a.H, W = a.W;
+  const long long i = ((long long)z * H + h) * W + w;
+  float nd = dm[i];
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    int dz, dh, dw;
+    toiv_offset<IS3D, BWD>(j, dz, dh, dw);
+    const int zi = z + dz, hi = h + dh, wi = w + dw;
+    if (zi < 0 || zi >= a.D || hi < 0 || hi >= H || wi < 0 || wi >= W) continue;
+    const long long q = ((long long)zi * H + hi) * W + wi;
+    float l1;
+    if (a.C == 1) {
+      l1 = fabsf(__fsub_rn(__ldg(a.img + i), __ldg(a.img + q)));  // geodis_toivanen.cpp:35-38
+    } else {
+      l1 = 0.0f;
+      for (int c = 0; c < a.C; c++)
+        l1 = __fadd_rn(l1, fabsf(__fsub_rn(__ldg(a.img + c * a.img_cs + i), __ldg(a.img + c * a.img_cs + q))));
+    }
+    const float ld = BWD ? a.ldb[j] : a.ldf[j];
+    const float cur = __fadd_rn(__fadd_rn(dm[q], __fmul_rn(a.le, ld)), __fmul_rn(a.lg, l1));
+    nd = cur < nd ? cur : nd;  // std::min(new_dist, cur_dist)
+  }
+  dm[i] = nd;
+}
+
+// One pass: waves t = 0 .. T-1 of the (mirrored, if BWD) coordinates.
+template <bool IS3D, bool BWD>
+__device__ __forceinline__ void toiv_pass(const ToivArgs &a, float *dm) {
+  const int D = a.D, H = a.H, W = a.W;
+  const int T = 4 * (D - 1) + 2 * (H - 1) + (W - 1) + 1;
+  const int wb = min(H, (W - 1) / 2 + 1);  // cells of one wave in one plane, at most
+  for (int t = 0; t < T; t++) {
+    const int x = t - 2 * (H - 1) - (W - 1);
+    const int zlo = x > 0 ? (x + 3) / 4 : 0, zhi = min(D - 1, t / 4);
+    const int n = (zhi - zlo + 1) * wb;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const int zm = zlo + k / wb, j = k - (k / wb) * wb;
+      const int rem = t - 4 * zm;
+      const int y = rem - (W - 1);
+      const int hm = (y > 0 ? (y + 1) / 2 : 0) + j;
+      if (hm > min(H - 1, rem / 2)) continue;
+      const int wm = rem - 2 * hm;  // 0 <= wm < W by the bounds on hm
+      if (BWD)
+        toiv_cell<IS3D, true>(a, dm, D - 1 - zm, H - 1 - hm, W - 1 - wm);
+      else
+        toiv_cell<IS3D, false>(a, dm, zm, hm, wm);
+    }
+    __syncthreads();  // the wave's writes are visible to the next wave
+  }
+}
+
+template <bool IS3D>
+__global__ void __launch_bounds__(1024, 1) fg_toivanen_kernel(const ToivArgs a) {
+  float *dm = a.dist[blockIdx.x];
+  for (int it = 0; it < a.iterations; it++) {
+    toiv_pass<IS3D, false>(a, dm);
+    toiv_pass<IS3D, true>(a, dm);
+  }
+}
+
+}  // namespace
+
+int launch_toivanen(const float *img, int C, int D, int H, int W, const float *spacing_sq, float *const *maps,
+                    int nmaps, float lg, float le, int iterations, cudaStream_t s) {
+  if (nmaps < 1 || nmaps > kToivMaps) return set_error(FG_ERR_INVALID_ARGUMENT, "toivanen: 1 to 4 maps per launch");
+  if (iterations <= 0) return FG_OK;
+  ToivArgs a{};
+  a.img = img;
+  a.img_cs = (long long)D * H * W;
+  a.C = C;
+  for (int m = 0; m < nmaps; m++) a.dist[m] = maps[m];
+  a.D = D, a.H = H, a.W = W;
+  a.lg = lg, a.le = le;
+  a.iterations = iterations;
+  const bool is3d = spacing_sq != nullptr;
+  if (!is3d) {
+    const float r2 = sqrtf(2.0f);  // geodis_toivanen.cpp:59, :104
+    const float f[4] = {r2, 1.0f, r2, 1.0f}, b[4] = {1.0f, r2, 1.0f, r2};
+    for (int j = 0; j < 4; j++) a.ldf[j] = f[j], a.ldb[j] = b[j];
+  } else {
+    // geodis_toivanen.cpp:186-207, :213-234: sqrt of the summed squared spacings
+    // of the axes a neighbour moves along, summed in axis order
+    const int fz[13] = {-1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1};
+    const int fh[13] = {-1, -1, -1, 0, 0, -1, -1, -1, 0, -1, -1, -1, 0};
+    const int fw[13] = {-1, 0, 1, -1, 0, -1, 0, 1, -1, -1, 0, 1, -1};
+    const int bz[13] = {-1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1};
+    const int bh[13] = {0, 1, 1, 1, 0, 1, 1, 1, 0, 0, 1, 1, 1};
+    const int bw[13] = {1, -1, 0, 1, 1, -1, 0, 1, 0, 1, -1, 0, 1};
+    for (int j = 0; j < 13; j++) {
+      float vf = 0.0f, vb = 0.0f;
+      if (fz[j]) vf += spacing_sq[0];
+      if (fh[j]) vf += spacing_sq[1];
+      if (fw[j]) vf += spacing_sq[2];
+      if (bz[j]) vb += spacing_sq[0];
+      if (bh[j]) vb += spacing_sq[1];
+      if (bw[j]) vb += spacing_sq[2];
+      a.ldf[j] = sqrtf(vf);
+      a.ldb[j] = sqrtf(vb);
+    }
+  }
+  // threads: the most cells one wave can hold, in whole warps
+  const long long wb = std::min(H, (W - 1) / 2 + 1);
+  const long long planes = std::min<long long>(D, (2LL * (H - 1) + (W - 1)) / 4 + 1);
+  const int threads = (int)std::max<long long>(32, std::min<long long>(1024, (wb * planes + 31) / 32 * 32));
+  if (is3d)
+    fg_toivanen_kernel<true><<<nmaps, threads, 0, s>>>(a);
+  else
+    fg_toivanen_kernel<false><<<nmaps, threads, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  return FG_OK;
+}
+
+}  // namespace fgi

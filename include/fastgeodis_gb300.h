@@ -154,6 +154,35 @@ FG_API int fg_GSF3d(const float *image, int C, int D, int H, int W, const float 
              int iterations, float *out, void *workspace,
              size_t workspace_bytes, void *stream);
 
+/* Toivanen's raster scan: replace FastGeodisCpp.generalised_geodesic2d/3d_toivanen,
+ * signed_generalised_geodesic2d/3d_toivanen and GSF2d/3d_toivanen
+ * (reference: FastGeodis/__init__.py:165-308, 587-656 -> FastGeodis/fastgeodis.cpp
+ *  :148-177, 260-277, 345-369 -> FastGeodis/geodis_toivanen.cpp:40-348, CPU only
+ *  there).  Same arguments, workspace and status rules as the raster entries
+ * above; any channel count.  Results equal the reference's CPU output bit for
+ * bit: the sequential scan runs as a wavefront, one CTA per distance map. */
+FG_API int fg_generalised_geodesic2d_toivanen(const float *image, int C, int H, int W, const float *mask, int Cm,
+                                              float *out, float v, float l_grad, float l_eucl, int iterations,
+                                              void *workspace, size_t workspace_bytes, void *stream);
+FG_API int fg_generalised_geodesic3d_toivanen(const float *image, int C, int D, int H, int W, const float *mask,
+                                              int Cm, const float *spacing, float *out, float v, float l_grad,
+                                              float l_eucl, int iterations, void *workspace, size_t workspace_bytes,
+                                              void *stream);
+FG_API int fg_signed_generalised_geodesic2d_toivanen(const float *image, int C, int H, int W, const float *mask,
+                                                     int Cm, float *out, float v, float l_grad, float l_eucl,
+                                                     int iterations, void *workspace, size_t workspace_bytes,
+                                                     void *stream);
+FG_API int fg_signed_generalised_geodesic3d_toivanen(const float *image, int C, int D, int H, int W,
+                                                     const float *mask, int Cm, const float *spacing, float *out,
+                                                     float v, float l_grad, float l_eucl, int iterations,
+                                                     void *workspace, size_t workspace_bytes, void *stream);
+FG_API int fg_GSF2d_toivanen(const float *image, int C, int H, int W, const float *mask, int Cm, float theta,
+                             float v, float lambda, int iterations, float *out, void *workspace,
+                             size_t workspace_bytes, void *stream);
+FG_API int fg_GSF3d_toivanen(const float *image, int C, int D, int H, int W, const float *mask, int Cm,
+                             float theta, const float *spacing, float v, float lambda, int iterations, float *out,
+                             void *workspace, size_t workspace_bytes, void *stream);
+
 /* One image of a batched 2D transform (see fg_batch_geodesic2d).  All
  * pointers are device pointers; float32, contiguous.  The scratch buffers
  * belong to the caller and must not overlap between items. */

@@ -16,7 +16,6 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 CASES = {c["name"]: c for c in load_all()}
-RASTER = [n for n in names() if "toivanen" not in CASES[n]["op"]]  # Toivanen's scan: test_toivanen_gpu.py
 DEV = "cuda"
 
 
@@ -37,8 +36,20 @@ def run_gpu(c):
         r = fg.signed_generalised_geodesic3d(img, m, c["spacing"], v, lamb, it)
     elif op == "gsf2d":
         r = fg.GSF2d(img, m, c["theta"], v, lamb, it)
-    else:
+    elif op == "gsf3d":
         r = fg.GSF3d(img, m, c["theta"], c["spacing"], v, lamb, it)
+    elif op == "toivanen2d":
+        r = fg.generalised_geodesic2d_toivanen(img, m, v, lamb, it)
+    elif op == "toivanen3d":
+        r = fg.generalised_geodesic3d_toivanen(img, m, c["spacing"], v, lamb, it)
+    elif op == "signed_toivanen2d":
+        r = fg.signed_generalised_geodesic2d_toivanen(img, m, v, lamb, it)
+    elif op == "signed_toivanen3d":
+        r = fg.signed_generalised_geodesic3d_toivanen(img, m, c["spacing"], v, lamb, it)
+    elif op == "gsf_toivanen2d":
+        r = fg.GSF2d_toivanen(img, m, c["theta"], v, lamb, it)
+    else:
+        r = fg.GSF3d_toivanen(img, m, c["theta"], c["spacing"], v, lamb, it)
     return r[0].cpu().numpy()
 
 
@@ -49,7 +60,7 @@ def tuning():
     _lib.check(L.fg_set_tuning(0, 0))
 
 
-@pytest.mark.parametrize("name", RASTER)
+@pytest.mark.parametrize("name", names())
 def test_golden_bits(name):
     c = CASES[name]
     got = run_gpu(c)
