@@ -52,6 +52,14 @@ def smooth_noise(rng, shape, sigma, lo, hi):
 
 
 def workload(name: str, seed: int = 1):
+    if name in ("t1", "t2"):
+        # Toivanen's raster scan on the c1 / c2 data (two passes per iteration)
+        w = workload("c1" if name == "t1" else "c2", seed)
+        w.update(name=name, method="toivanen",
+                 desc=w["desc"].replace("generalised_geodesic", "generalised_geodesic_toivanen", 1)
+                      .replace("geodesic_toivanen2d", "geodesic2d_toivanen")
+                      .replace("geodesic_toivanen3d", "geodesic3d_toivanen"))
+        return w
     rng = np.random.default_rng(seed)
     if name in ("c2", "vol256"):
         shape = (128, 256, 256) if name == "c2" else (256, 256, 256)
@@ -404,7 +412,7 @@ def run_serve_arm(args, rank, world):
 
 def voxel_passes(w) -> float:
     n = float(np.prod(w["image"].shape[2:]))
-    per = 6 if w["dims"] == 3 else 4
+    per = 2 if w.get("method") == "toivanen" else (6 if w["dims"] == 3 else 4)
     return n * per * w["iters"] * len(w["lambs"])
 
 
@@ -512,6 +520,11 @@ def cpu_transform_fn(kind_pref="reference"):
         def f(w, lamb):
             img = torch.from_numpy(w["image"])
             m = torch.from_numpy(w["mask"])
+            if w.get("method") == "toivanen":  # geodis_toivanen.cpp: one thread
+                if w["dims"] == 3:
+                    return ref.generalised_geodesic3d_toivanen(img, m, w["spacing"], w["v"], lamb, 1 - lamb,
+                                                               w["iters"])
+                return ref.generalised_geodesic2d_toivanen(img, m, w["v"], lamb, 1 - lamb, w["iters"])
             if w["dims"] == 3:
                 return ref.generalised_geodesic3d(img, m, w["spacing"], w["v"], lamb, 1 - lamb, w["iters"])
             return ref.generalised_geodesic2d(img, m, w["v"], lamb, 1 - lamb, w["iters"])
@@ -520,6 +533,10 @@ def cpu_transform_fn(kind_pref="reference"):
     cores = oracle.max_threads()
 
     def f(w, lamb):
+        if w.get("method") == "toivanen":
+            if w["dims"] == 3:
+                return oracle.toivanen3d(w["image"][0], w["mask"][0], w["spacing"], w["v"], lamb, w["iters"])
+            return oracle.toivanen2d(w["image"][0], w["mask"][0], w["v"], lamb, w["iters"])
         if w["dims"] == 3:
             return oracle.geodesic3d(w["image"][0], w["mask"][0], w["spacing"], w["v"], lamb, w["iters"])
         return oracle.geodesic2d(w["image"][0], w["mask"][0], w["v"], lamb, w["iters"])
@@ -531,6 +548,8 @@ def time_cpu_sample(w, kind_pref="reference", max_runs=None, budget_s=20.0):
     """Times single transforms (cycling through the workload's lambs) until
     about `budget_s` seconds of CPU work; returns Gvp/s and a description."""
     f, kind, cores = cpu_transform_fn(kind_pref)
+    if w.get("method") == "toivanen":
+        cores = 1  # Toivanen's scan is sequential in the reference (and the port)
     vp_one = voxel_passes(w) / len(w["lambs"])
     f(w, w["lambs"][0])  # warm-up (page-in, thread pool)
     t_total, runs = 0.0, 0
@@ -551,6 +570,8 @@ def run_reference_arm(args, w, rank):
     if rank != 0:
         return
     f, kind, cores = cpu_transform_fn("reference")
+    if w.get("method") == "toivanen":
+        cores = 1  # Toivanen's scan is sequential in the reference (and the port)
     vp_one = voxel_passes(w) / len(w["lambs"])
     for i in range(args.warmup):
         f(w, w["lambs"][i % len(w["lambs"])])
@@ -575,7 +596,15 @@ def run_reference_arm(args, w, rank):
 
 
 def metric_name(w):
-    return ("generalised_geodesic3d throughput" if w["dims"] == 3 else "generalised_geodesic2d throughput")
+    name = "generalised_geodesic3d" if w["dims"] == 3 else "generalised_geodesic2d"
+    return name + ("_toivanen" if w.get("method") == "toivanen" else "") + " throughput"
+
+
+def transform_fns(fg, w):
+    """The public functions of the workload's method: (3D, 2D)."""
+    if w.get("method") == "toivanen":
+        return fg.generalised_geodesic3d_toivanen, fg.generalised_geodesic2d_toivanen
+    return fg.generalised_geodesic3d, fg.generalised_geodesic2d
 
 
 # ---------------------------------------------------------------------------
@@ -600,7 +629,7 @@ def run_gpu_arm(args, w, rank, world):
     msk = torch.from_numpy(w["mask"]).to(dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     tuned = None
-    if args.tune:  # untimed: measures candidate plans with the step's transforms running together
+    if args.tune and w.get("method") != "toivanen":  # untimed: plans of the step's transforms run together
         from fastgeodis_gb300 import tune
 
         shape = tuple(w["image"].shape[2:])
@@ -616,6 +645,8 @@ def run_gpu_arm(args, w, rank, world):
     main = torch.cuda.current_stream()
     streams = [torch.cuda.Stream() for _ in w["lambs"]]
 
+    f3, f2 = transform_fns(fg, w)
+
     def step(im, mk):
         outs = []
         for s in streams:
@@ -623,9 +654,9 @@ def run_gpu_arm(args, w, rank, world):
         for lamb, s in zip(w["lambs"], streams):
             with torch.cuda.stream(s):
                 if w["dims"] == 3:
-                    outs.append(fg.generalised_geodesic3d(im, mk, w["spacing"], w["v"], lamb, w["iters"]))
+                    outs.append(f3(im, mk, w["spacing"], w["v"], lamb, w["iters"]))
                 else:
-                    outs.append(fg.generalised_geodesic2d(im, mk, w["v"], lamb, w["iters"]))
+                    outs.append(f2(im, mk, w["v"], lamb, w["iters"]))
         for s in streams:
             main.wait_stream(s)
         return outs
@@ -685,8 +716,8 @@ def run_gpu_arm(args, w, rank, world):
         with torch.cuda.device(dev), torch.cuda.stream(streams[k]):
             lamb = w["lambs"][k]
             if w["dims"] == 3:
-                return fg.generalised_geodesic3d(h_img, h_msk, w["spacing"], w["v"], lamb, w["iters"])
-            return fg.generalised_geodesic2d(h_img, h_msk, w["v"], lamb, w["iters"])
+                return f3(h_img, h_msk, w["spacing"], w["v"], lamb, w["iters"])
+            return f2(h_img, h_msk, w["v"], lamb, w["iters"])
 
     from concurrent.futures import ThreadPoolExecutor
 
@@ -736,12 +767,14 @@ def run_gpu_arm(args, w, rank, world):
         "data": "synthetic",
         "config": {"workload": w["desc"], "parallelism": f"replicas x{world}",
                    "streams": f"{len(w['lambs'])} transforms per step on {len(w['lambs'])} CUDA streams",
-                   "plans": {"autotuned": tuned} if tuned else "cost model",
+                   "plans": ({"autotuned": tuned} if tuned else
+                             "wavefront, no plan" if w.get("method") == "toivanen" else "cost model"),
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)",
                    "wall_s_timed_region": round(wall, 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "fg_pass_kernel", "avg_launch_ms": round(avg_launch_ms, 5),
+                     "kernel": "fg_toivanen_kernel" if w.get("method") == "toivanen" else "fg_pass_kernel",
+                     "avg_launch_ms": round(avg_launch_ms, 5),
                      "alg_bytes_per_launch": int(alg_bytes_launch), "peak_source": peak_kind,
                      "pass_time_share": round(pass_ms / (ms * args.steps), 4),
                      "achieved_aggregate": round(pass_vp * bytes_per_vp / (ms * args.steps * 1e-3) / 1e9, 1)},
@@ -764,7 +797,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "c3", "c4", "c5", "t1", "t2"])
     ap.add_argument("--requests", type=int, default=300, help="requests of the served stream (c5)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--no-tune", dest="tune", action="store_false",

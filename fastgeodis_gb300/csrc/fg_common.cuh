@@ -111,9 +111,10 @@ int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, b
 int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
-// in place, one CTA each; spacing_sq = nullptr for images.
+// in place; spacing_sq = nullptr for images.  bar: 4 counters (16 bytes) of
+// scratch the launch clears, status: the workspace status word.
 int launch_toivanen(const float *img, int C, int D, int H, int W, const float *spacing_sq, float *const *maps,
-                    int nmaps, float lg, float le, int iterations, cudaStream_t s);
+                    int nmaps, float lg, float le, int iterations, unsigned *bar, int *status, cudaStream_t s);
 
 // Host error reporting shared by the units.
 int set_error(int code, const char *msg);

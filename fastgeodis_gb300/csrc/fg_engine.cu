@@ -428,8 +428,10 @@ ProfileState &profile() {
 
 std::mutex g_launch_mu;  // serialises the per-device function attribute set-up
 
-int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt, cudaStream_t s) {
-  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean};
+// Runs `launch` on stream s, bracketed by timing events while profiling is on;
+// vp: cells x maps the launch updates, steps: its sequential steps.
+template <typename Launch>
+int profiled_launch(cudaStream_t s, long long vp, int steps, Launch launch) {
   ProfileState &ps = profile();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   {
@@ -443,17 +445,24 @@ int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bo
   int rc;
   {
     std::lock_guard<std::mutex> g(g_launch_mu);
-    rc = cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
+    rc = launch();
   }
   if (rc != FG_OK) return rc;
   if (e0) {
     FG_CUDA(cudaEventRecord(e1, s));
     std::lock_guard<std::mutex> g(ps.mu);
     ps.ev.emplace_back(e0, e1);
-    ps.vp.push_back((long long)a.L * a.N1 * a.N2 * M);
-    ps.steps.push_back(a.L);
+    ps.vp.push_back(vp);
+    ps.steps.push_back(steps);
   }
   return FG_OK;
+}
+
+int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt, cudaStream_t s) {
+  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean};
+  return profiled_launch(s, (long long)a.L * a.N1 * a.N2 * M, a.L, [&] {
+    return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
+  });
 }
 
 // The cheapest exact arithmetic for the weights: l_grad == 0 drops the image
@@ -641,10 +650,19 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   // epoch 0 is never wanted; earlier calls' words must not match this call's epochs
   if (!toivanen) FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
   unsigned counter = 0;
+  // Toivanen's group barriers: 4 counters in the spare bytes of the header
+  unsigned *toiv_bar = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(w.status) + 64);
   auto sweep = [&](const MapSet &ms) {
-    if (toivanen)
-      return launch_toivanen(image, g.C, g.is3d ? g.D : 1, g.H, g.W, g.is3d ? g.spacing_sq : nullptr, ms.r, ms.M,
-                             ms.lg, ms.le, iterations, s);
+    if (toivanen) {
+      // one launch runs every iteration: 2 passes of D*H*W cells per map, in
+      // 4(D-1) + 2(H-1) + W waves each
+      const int D = g.is3d ? g.D : 1;
+      const long long waves = 4LL * (D - 1) + 2LL * (g.H - 1) + g.W;
+      return profiled_launch(s, 2LL * iterations * g.P * ms.M, (int)(2 * iterations * waves), [&] {
+        return launch_toivanen(image, g.C, D, g.H, g.W, g.is3d ? g.spacing_sq : nullptr, ms.r, ms.M, ms.lg, ms.le,
+                               iterations, toiv_bar, w.status, s);
+      });
+    }
     return run_transform(g, image, img_t, ms, iterations, w, &counter, s);
   };
   if (Cm > 1) {

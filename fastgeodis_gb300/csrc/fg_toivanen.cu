@@ -17,9 +17,14 @@
 // scan reads: the results are the reference's bits.  The backward pass is the
 // same schedule on the mirrored coordinates.
 //
-// One CTA sweeps one distance map (signed and GSF run their maps on separate
-// CTAs); data stays in global memory (L1/L2) and the CTA's barrier orders the
-// waves, so nothing waits on another CTA.
+// Each distance map is swept by its own group of CTAs (signed and GSF run
+// their maps side by side).  A small image's waves fit one CTA, whose barrier
+// orders them.  A volume's waves hold thousands of cells, so its group spans up
+// to one CTA per SM (cooperative launch, all resident) and the waves are
+// ordered by a grid barrier of the group: an arrive counter in the workspace
+// header, polled with acquire loads under a bound (FG_ERR_TIMEOUT in the
+// status word if it ever expires).  Distances are read and written through L2
+// (.cg): another SM's L1 may hold a line from an earlier wave.
 
 #include <cuda_runtime.h>
 
@@ -37,12 +42,46 @@ struct ToivArgs {
   const float *img;   // [C][D][H][W]
   long long img_cs;   // elements between channels
   int C;
-  float *dist[kToivMaps];  // one map per CTA, [D][H][W] (channel 0 of the distance tensor)
+  float *dist[kToivMaps];  // one map per group of CTAs, [D][H][W] (channel 0 of the distance tensor)
   int D, H, W;             // D = 1 for images
   float lg, le;
   float ldf[13], ldb[13];  // step lengths of the forward and backward neighbours
   int iterations;
+  int group;               // CTAs per map
+  unsigned *bar;           // arrive counters, one per map (zero at launch)
+  int *status;             // FG_ERR_TIMEOUT if a barrier wait expired
 };
+
+__device__ __forceinline__ unsigned toiv_ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int toiv_ld_status(const int *p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Barrier of the `group` CTAs of one map: the n-th call returns once all of
+// them have arrived n times.  Bounded: after kSpinLimit polls (or once another
+// CTA has recorded a timeout) it records FG_ERR_TIMEOUT and returns.
+__device__ __forceinline__ void toiv_group_sync(const ToivArgs &a, unsigned *bar, unsigned &arrivals) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    arrivals += (unsigned)a.group;
+    __threadfence();  // this CTA's cell writes (ordered by the barrier above) before the arrival
+    atomicAdd(bar, 1u);
+    unsigned spins = 0;
+    while (toiv_ld_acquire(bar) < arrivals) {
+      if (++spins > kSpinLimit || ((spins & 1023u) == 0 && toiv_ld_status(a.status) != 0)) {
+        atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
+        break;
+      }
+    }
+  }
+  __syncthreads();
+}
 
 // Neighbour offsets (dz, dh, dw) in the reference's order:
 // 2D forward / backward geodis_toivanen.cpp:56-57, 101-102;
@@ -68,12 +107,19 @@ __device__ __forceinline__ void toiv_offset(int j, int &dz, int &dh, int &dw) {
   }
 }
 
-template <bool IS3D, bool BWD>
+// GROUP: the map is swept by several CTAs, so distances go through L2 (.cg);
+// one CTA reads its own writes through its SM's L1.
+template <bool IS3D, bool BWD, bool GROUP>
+__device__ __forceinline__ float toiv_ld(const float *p) {
+  return GROUP ? __ldcg(p) : *p;
+}
+
+template <bool IS3D, bool BWD, bool GROUP>
 __device__ __forceinline__ void toiv_cell(const ToivArgs &a, float *dm, int z, int h, int w) {
   constexpr int N = IS3D ? 13 : 4;
   const int H = a.H, W = a.W;
   const long long i = ((long long)z * H + h) * W + w;
-  float nd = dm[i];
+  float nd = toiv_ld<IS3D, BWD, GROUP>(dm + i);
 #pragma unroll
   for (int j = 0; j < N; j++) {
     int dz, dh, dw;
@@ -90,15 +136,18 @@ __device__ __forceinline__ void toiv_cell(const ToivArgs &a, float *dm, int z, i
         l1 = __fadd_rn(l1, fabsf(__fsub_rn(__ldg(a.img + c * a.img_cs + i), __ldg(a.img + c * a.img_cs + q))));
     }
     const float ld = BWD ? a.ldb[j] : a.ldf[j];
-    const float cur = __fadd_rn(__fadd_rn(dm[q], __fmul_rn(a.le, ld)), __fmul_rn(a.lg, l1));
+    const float cur = __fadd_rn(__fadd_rn(toiv_ld<IS3D, BWD, GROUP>(dm + q), __fmul_rn(a.le, ld)), __fmul_rn(a.lg, l1));
     nd = cur < nd ? cur : nd;  // std::min(new_dist, cur_dist)
   }
-  dm[i] = nd;
+  if (GROUP)
+    __stcg(dm + i, nd);
+  else
+    dm[i] = nd;
 }
 
 // One pass: waves t = 0 .. T-1 of the (mirrored, if BWD) coordinates.
-template <bool IS3D, bool BWD>
-__device__ __forceinline__ void toiv_pass(const ToivArgs &a, float *dm) {
+template <bool IS3D, bool BWD, bool GROUP>
+__device__ __forceinline__ void toiv_pass(const ToivArgs &a, float *dm, int rank, unsigned *bar, unsigned &arrivals) {
   const int D = a.D, H = a.H, W = a.W;
   const int T = 4 * (D - 1) + 2 * (H - 1) + (W - 1) + 1;
   const int wb = min(H, (W - 1) / 2 + 1);  // cells of one wave in one plane, at most
@@ -106,7 +155,7 @@ __device__ __forceinline__ void toiv_pass(const ToivArgs &a, float *dm) {
     const int x = t - 2 * (H - 1) - (W - 1);
     const int zlo = x > 0 ? (x + 3) / 4 : 0, zhi = min(D - 1, t / 4);
     const int n = (zhi - zlo + 1) * wb;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = rank * blockDim.x + threadIdx.x; k < n; k += a.group * blockDim.x) {
       const int zm = zlo + k / wb, j = k - (k / wb) * wb;
       const int rem = t - 4 * zm;
       const int y = rem - (W - 1);
@@ -114,27 +163,40 @@ __device__ __forceinline__ void toiv_pass(const ToivArgs &a, float *dm) {
       if (hm > min(H - 1, rem / 2)) continue;
       const int wm = rem - 2 * hm;  // 0 <= wm < W by the bounds on hm
       if (BWD)
-        toiv_cell<IS3D, true>(a, dm, D - 1 - zm, H - 1 - hm, W - 1 - wm);
+        toiv_cell<IS3D, true, GROUP>(a, dm, D - 1 - zm, H - 1 - hm, W - 1 - wm);
       else
-        toiv_cell<IS3D, false>(a, dm, zm, hm, wm);
+        toiv_cell<IS3D, false, GROUP>(a, dm, zm, hm, wm);
     }
-    __syncthreads();  // the wave's writes are visible to the next wave
+    if (GROUP)
+      toiv_group_sync(a, bar, arrivals);  // the wave's writes are visible to the next wave
+    else
+      __syncthreads();
   }
 }
 
-template <bool IS3D>
+template <bool IS3D, bool GROUP>
 __global__ void __launch_bounds__(1024, 1) fg_toivanen_kernel(const ToivArgs a) {
-  float *dm = a.dist[blockIdx.x];
+  const int map = blockIdx.x / a.group, rank = blockIdx.x - map * a.group;
+  float *dm = a.dist[map];
+  unsigned *bar = GROUP ? a.bar + map : nullptr;  // counters exist for grouped launches only
+  unsigned arrivals = 0;
   for (int it = 0; it < a.iterations; it++) {
-    toiv_pass<IS3D, false>(a, dm);
-    toiv_pass<IS3D, true>(a, dm);
+    toiv_pass<IS3D, false, GROUP>(a, dm, rank, bar, arrivals);
+    toiv_pass<IS3D, true, GROUP>(a, dm, rank, bar, arrivals);
   }
+}
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 1;
+  return std::max(1, sms);
 }
 
 }  // namespace
 
 int launch_toivanen(const float *img, int C, int D, int H, int W, const float *spacing_sq, float *const *maps,
-                    int nmaps, float lg, float le, int iterations, cudaStream_t s) {
+                    int nmaps, float lg, float le, int iterations, unsigned *bar, int *status, cudaStream_t s) {
   if (nmaps < 1 || nmaps > kToivMaps) return set_error(FG_ERR_INVALID_ARGUMENT, "toivanen: 1 to 4 maps per launch");
   if (iterations <= 0) return FG_OK;
   ToivArgs a{};
@@ -171,15 +233,36 @@ int launch_toivanen(const float *img, int C, int D, int H, int W, const float *s
       a.ldb[j] = sqrtf(vb);
     }
   }
-  // threads: the most cells one wave can hold, in whole warps
+  // threads: the most cells one wave can hold, in whole warps; beyond 4096
+  // cells a group of 256-thread CTAs, at most one per SM for each map
   const long long wb = std::min(H, (W - 1) / 2 + 1);
   const long long planes = std::min<long long>(D, (2LL * (H - 1) + (W - 1)) / 4 + 1);
-  const int threads = (int)std::max<long long>(32, std::min<long long>(1024, (wb * planes + 31) / 32 * 32));
-  if (is3d)
-    fg_toivanen_kernel<true><<<nmaps, threads, 0, s>>>(a);
-  else
-    fg_toivanen_kernel<false><<<nmaps, threads, 0, s>>>(a);
-  cudaError_t e = cudaGetLastError();
+  const long long cells = wb * planes;
+  int threads, group = 1;
+  if (cells <= 4096) {
+    threads = (int)std::max<long long>(32, std::min<long long>(1024, (cells + 31) / 32 * 32));
+  } else {
+    threads = 256;
+    group = (int)std::max<long long>(1, std::min<long long>(device_sms() / nmaps, (cells + 255) / 256));
+  }
+  a.group = group;
+  a.bar = bar;
+  a.status = status;
+  cudaError_t e = cudaSuccess;
+  if (group > 1) {
+    if (!bar || !status) return set_error(FG_ERR_INVALID_ARGUMENT, "toivanen: barrier counters missing");
+    e = cudaMemsetAsync(bar, 0, kToivMaps * sizeof(unsigned), s);
+    if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+    void *args[] = {&a};
+    const void *fn =
+        is3d ? (const void *)fg_toivanen_kernel<true, true> : (const void *)fg_toivanen_kernel<false, true>;
+    e = cudaLaunchCooperativeKernel(fn, dim3(nmaps * group), dim3(threads), args, 0, s);
+  } else if (is3d) {
+    fg_toivanen_kernel<true, false><<<nmaps, threads, 0, s>>>(a);
+  } else {
+    fg_toivanen_kernel<false, false><<<nmaps, threads, 0, s>>>(a);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   return FG_OK;
 }

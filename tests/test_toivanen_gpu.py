@@ -87,3 +87,18 @@ def test_toivanen_and_raster_scans_reach_the_same_fixed_point():
     a = fg.generalised_geodesic2d_toivanen(t(img), t(m), 1e10, 0.7, 40)
     b = fg.generalised_geodesic2d(t(img), t(m), 1e10, 0.7, 40)
     assert torch.allclose(a, b, rtol=1e-5, atol=1e-4)
+
+
+def test_large_volume_grouped_ctas():
+    # 6400 cells per wave: each map is swept by a group of CTAs ordered by a
+    # grid barrier; plain (one group), signed (two) and GSF (four at once)
+    rng = np.random.default_rng(12)
+    vol, vm = case(rng, (64, 200, 200), 1)
+    sp = [1.0, 0.8, 1.2]
+    got = fg.generalised_geodesic3d_toivanen(t(vol), t(vm), sp, 1e10, 0.5, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.toivanen3d(vol, vm, sp, 1e10, 0.5, 1))
+    got = fg.signed_generalised_geodesic3d_toivanen(t(vol), t(vm), sp, 1e10, 1.0, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.toivanen3d(vol, vm, sp, 1e10, 1.0, 1, signed=True))
+    got = fg.GSF3d_toivanen(t(vol), t(vm), 0.5, sp, 1e10, 0.7, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.gsf_toivanen3d(vol, vm, 0.5, sp, 1e10, 0.7, 1))
+    fg.check_status()
