@@ -186,6 +186,98 @@ __global__ void __launch_bounds__(1024, 1) fg_toivanen_kernel(const ToivArgs a) 
   }
 }
 
+// Images of at most 1024 rows: one thread per row.  Row h computes its cell
+// w = t - 2h at wave t (mirrored coordinates in the backward pass, whose
+// neighbour set is the mirror of the forward one).  The three neighbours in
+// the row above and the left neighbour come from 4-slot shared rings of the
+// rows' latest values (at wave t row h-1 writes slot (w+2) & 3 while row h
+// reads slots w-1 .. w+1 of it), so a wave needs no global reads of fresh
+// values; a row's own old distance and image values are loaded 4 cells ahead
+// into registers.  CT: 1 for one image channel, 0 for 2-4 channels.
+constexpr int kRowAhead = 4;
+
+template <int CT>
+__global__ void __launch_bounds__(1024, 1) fg_toivanen_rows_kernel(const ToivArgs a) {
+  extern __shared__ float rings[];
+  constexpr int NCH = CT == 1 ? 1 : 4;
+  const int C = CT == 1 ? 1 : a.C;
+  const int H = a.H, W = a.W;
+  float *dm = a.dist[blockIdx.x];
+  float *rd = rings;           // [H][4] latest distances of each row
+  float *ri = rings + 4 * H;   // [C][H][4] latest image values of each row
+  const int hm = threadIdx.x;  // this thread's row, in the pass's (mirrored) coordinates
+  const bool row = hm < H;
+  const int T = 2 * (H - 1) + W;
+  for (int it = 0; it < a.iterations; it++) {
+    for (int dir = 0; dir < 2; dir++) {
+      const bool bwd = dir == 1;
+      const int h = bwd ? H - 1 - hm : hm;  // the row in memory
+      auto at = [&](int wm) { return (long long)h * W + (bwd ? W - 1 - wm : wm); };
+      // own old values of cells wm .. wm + kRowAhead - 1, loaded ahead
+      float dpf[kRowAhead], ipf[kRowAhead][NCH];
+#pragma unroll
+      for (int k = 0; k < kRowAhead; k++) {
+        if (row && k < W) {
+          dpf[k] = dm[at(k)];
+#pragma unroll
+          for (int c = 0; c < NCH; c++)
+            if (c < C) ipf[k][c] = __ldg(a.img + c * a.img_cs + at(k));
+        }
+      }
+      // step lengths by relative position: above-left, above, above-right, left
+      const float r2 = a.ldf[0], one = a.ldf[1];
+      for (int t = 0; t < T; t++) {
+        const int wm = t - 2 * hm;
+        if (row && wm >= 0 && wm < W) {
+          const float dold = dpf[0];
+          float icur[NCH];
+#pragma unroll
+          for (int c = 0; c < NCH; c++)
+            if (c < C) icur[c] = ipf[0][c];
+          // next cell ahead
+#pragma unroll
+          for (int k = 0; k < kRowAhead - 1; k++) {
+            dpf[k] = dpf[k + 1];
+#pragma unroll
+            for (int c = 0; c < NCH; c++) ipf[k][c] = ipf[k + 1][c];
+          }
+          if (wm + kRowAhead < W) {
+            dpf[kRowAhead - 1] = dm[at(wm + kRowAhead)];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+              if (c < C) ipf[kRowAhead - 1][c] = __ldg(a.img + c * a.img_cs + at(wm + kRowAhead));
+          }
+          float nd = dold;
+          // candidates: (row above, wm-1 / wm / wm+1) and (this row, wm-1)
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const int r = j < 3 ? hm - 1 : hm, x = j < 3 ? wm - 1 + j : wm - 1;
+            if (r < 0 || x < 0 || x >= W) continue;
+            float l1;
+            if (CT == 1) {
+              l1 = fabsf(__fsub_rn(icur[0], ri[r * 4 + (x & 3)]));
+            } else {
+              l1 = 0.0f;
+#pragma unroll
+              for (int c = 0; c < NCH; c++)
+                if (c < C) l1 = __fadd_rn(l1, fabsf(__fsub_rn(icur[c], ri[(c * H + r) * 4 + (x & 3)])));
+            }
+            const float ld = (j == 0 || j == 2) ? r2 : one;
+            const float cur = __fadd_rn(__fadd_rn(rd[r * 4 + (x & 3)], __fmul_rn(a.le, ld)), __fmul_rn(a.lg, l1));
+            nd = cur < nd ? cur : nd;  // std::min(new_dist, cur_dist)
+          }
+          rd[hm * 4 + (wm & 3)] = nd;
+#pragma unroll
+          for (int c = 0; c < NCH; c++)
+            if (c < C) ri[(c * H + hm) * 4 + (wm & 3)] = icur[c];
+          dm[at(wm)] = nd;
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
 int device_sms() {
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -232,6 +324,21 @@ int launch_toivanen(const float *img, int C, int D, int H, int W, const float *s
       a.ldf[j] = sqrtf(vf);
       a.ldb[j] = sqrtf(vb);
     }
+  }
+  if (!is3d && H <= 1024 && C <= 4) {  // images: one thread per row
+    const int threads = std::max(32, (H + 31) / 32 * 32);
+    const size_t smem = (size_t)4 * H * (1 + C) * sizeof(float);
+    cudaError_t e;
+    if (C == 1) {
+      e = cudaFuncSetAttribute(fg_toivanen_rows_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) fg_toivanen_rows_kernel<1><<<nmaps, threads, smem, s>>>(a);
+    } else {
+      e = cudaFuncSetAttribute(fg_toivanen_rows_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) fg_toivanen_rows_kernel<0><<<nmaps, threads, smem, s>>>(a);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+    return FG_OK;
   }
   // threads: the most cells one wave can hold, in whole warps; beyond 4096
   // cells a group of 256-thread CTAs, at most one per SM for each map

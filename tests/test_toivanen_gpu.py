@@ -28,7 +28,9 @@ def t(a):
     return torch.from_numpy(np.ascontiguousarray(a))[None].cuda()
 
 
-@pytest.mark.parametrize("shape", [(1, 1), (1, 37), (29, 1), (2, 3), (130, 97), (64, 200), (257, 31)])
+# up to 1024 rows: one thread per row; taller images: the wave kernel
+@pytest.mark.parametrize("shape", [(1, 1), (1, 37), (29, 1), (2, 3), (130, 97), (64, 200), (257, 31), (1024, 9),
+                                   (1100, 23)])
 @pytest.mark.parametrize("C", [1, 3])
 def test_2d_vs_oracle(shape, C):
     rng = np.random.default_rng(sum(shape) * 7 + C)
