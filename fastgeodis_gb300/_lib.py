@@ -32,6 +32,7 @@ EXPORTED = (
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
     "fg_grad_geodesic2d_forward", "fg_grad_geodesic2d_backward",
+    "fg_grad_geodesic2d_forward_pass", "fg_grad_geodesic2d_backward_pass",
     "fg_generalised_geodesic2d_noalloc", "fg_click_mask",
     "fg_generalised_geodesic2d_toivanen", "fg_generalised_geodesic3d_toivanen",
     "fg_signed_generalised_geodesic2d_toivanen", "fg_signed_generalised_geodesic3d_toivanen",
@@ -86,6 +87,8 @@ def load():
     L.fg_batch_geodesic2d.argtypes = [vp, i, i, i, i, i, vp, vp, vp]
     L.fg_grad_geodesic2d_forward.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_grad_geodesic2d_backward.argtypes = [vp, i, i, i, i, vp, vp, vp]
+    L.fg_grad_geodesic2d_forward_pass.argtypes = [vp, i, i, i, i, vp, vp, vp]
+    L.fg_grad_geodesic2d_backward_pass.argtypes = [vp, i, i, i, i, i, i, vp, vp]
     L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
     for name in ("fg_generalised_geodesic2d", "fg_generalised_geodesic3d", "fg_signed_generalised_geodesic2d",
                  "fg_signed_generalised_geodesic3d", "fg_GSF2d", "fg_GSF3d"):

@@ -12,6 +12,12 @@ tape); the backward kernel walks the passes in reverse and routes
   (the derivative of ``l_grad * |I - I'|``, with sign(0) = 0).
 
 Forward values are bit-identical to :func:`generalised_geodesic2d`.
+
+When memory is short, ``recompute=True`` keeps the tape of a single pass (1
+byte per pixel instead of 4 per iteration) plus one scratch distance map, and
+the backward recomputes the forward up to each pass before applying that
+pass's adjoint (about (4 * iterations + 1) / 2 times the forward work); the
+gradients are the same bits.
 """
 from __future__ import annotations
 
@@ -32,17 +38,20 @@ assert GRAD_ITEM_DTYPE.itemsize == 128
 
 
 class _Buffers:
-    def __init__(self, image, softmask, v, lamb, iterations):
+    def __init__(self, image, softmask, v, lamb, iterations, recompute=False):
         B, C, H, W = image.shape
         dev = image.device
         self.shape = (B, C, H, W)
         self.iterations = int(iterations)
+        self.recompute = bool(recompute)
         self.image = image
         self.mask = softmask
         self.out = torch.empty((B, 1, H, W), device=dev)
         self.image_t = torch.empty((B, C, W, H), device=dev)
         self.t1 = torch.empty((B, W, H), device=dev)
-        self.tape = torch.empty((B, max(1, self.iterations) * 4 * H * W), dtype=torch.uint8, device=dev)
+        tape_passes = 1 if self.recompute else max(1, self.iterations) * 4
+        self.tape = torch.empty((B, tape_passes * H * W), dtype=torch.uint8, device=dev)
+        self.scratch = torch.empty((B, 1, H, W), device=dev) if self.recompute else None
         self.counter = torch.zeros(2, dtype=torch.int32, device=dev)
         self.items = np.zeros(B, dtype=GRAD_ITEM_DTYPE)
         P = H * W
@@ -64,13 +73,22 @@ class _Buffers:
         host = torch.from_numpy(self.items.view(np.uint8).copy())
         return host.to(self.dev, non_blocking=False)
 
+    @property
+    def npass(self):
+        return 4 * self.iterations
+
     def forward(self):
         B, C, H, W = self.shape
         L = _lib.load()
         items = self.upload()
         stream = torch.cuda.current_stream(self.dev).cuda_stream
-        rc = L.fg_grad_geodesic2d_forward(items.data_ptr(), B, C, max(H, W), self.iterations,
-                                          self.counter.data_ptr(), self.counter.data_ptr() + 4, stream)
+        if self.recompute and self.iterations > 0:
+            # all passes, recording only the last one's tape
+            rc = L.fg_grad_geodesic2d_forward_pass(items.data_ptr(), B, C, max(H, W), self.npass - 1,
+                                                   self.counter.data_ptr(), self.counter.data_ptr() + 4, stream)
+        else:
+            rc = L.fg_grad_geodesic2d_forward(items.data_ptr(), B, C, max(H, W), self.iterations,
+                                              self.counter.data_ptr(), self.counter.data_ptr() + 4, stream)
         _lib.check(rc)
         self._keep = items
         return self.out
@@ -96,10 +114,24 @@ class _Buffers:
         L = _lib.load()
         items = self.upload()
         stream = torch.cuda.current_stream(dev).cuda_stream
-        rc = L.fg_grad_geodesic2d_backward(items.data_ptr(), B, C, max(H, W), self.iterations,
-                                           self.counter.data_ptr(), self.counter.data_ptr() + 4, stream)
-        _lib.check(rc)
-        self._keep_b = (items, g_out, g_r, g_t, gi_t)
+        cnt, st = self.counter.data_ptr(), self.counter.data_ptr() + 4
+        if not self.recompute or self.iterations <= 0:
+            rc = L.fg_grad_geodesic2d_backward(items.data_ptr(), B, C, max(H, W), self.iterations, cnt, st, stream)
+            _lib.check(rc)
+            self._keep_b = (items, g_out, g_r, g_t, gi_t)
+            return g_image, g_mask
+        # recompute into scratch distance maps, so the forward output stays intact
+        re = self.items.copy()
+        for b in range(B):
+            re[b]["out"] = self.scratch.data_ptr() + b * H * W * 4
+        re_dev = torch.from_numpy(re.view(np.uint8).copy()).to(dev)
+        last = self.npass - 1
+        for p in range(last, -1, -1):
+            if p < last:  # the forward's tape holds the last pass; recompute the others
+                _lib.check(L.fg_grad_geodesic2d_forward_pass(re_dev.data_ptr(), B, C, max(H, W), p, cnt, st, stream))
+            _lib.check(L.fg_grad_geodesic2d_backward_pass(items.data_ptr(), B, C, max(H, W), p, int(p == last),
+                                                          int(p == 0), cnt, stream))
+        self._keep_b = (items, re_dev, g_out, g_r, g_t, gi_t)
         return g_image, g_mask
 
 
@@ -107,8 +139,8 @@ class GeneralisedGeodesic2dFunction(torch.autograd.Function):
     """autograd Function: (image [B,C,H,W], softmask [B,1,H,W]) -> D [B,1,H,W]."""
 
     @staticmethod
-    def forward(ctx, image, softmask, v, lamb, iterations):
-        buf = _Buffers(image, softmask, v, lamb, iterations)
+    def forward(ctx, image, softmask, v, lamb, iterations, recompute=False):
+        buf = _Buffers(image, softmask, v, lamb, iterations, recompute)
         out = buf.forward()
         ctx.buf = buf
         return out
@@ -116,17 +148,20 @@ class GeneralisedGeodesic2dFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g_out):
         g_image, g_mask = ctx.buf.backward(g_out)
-        return g_image, g_mask, None, None, None
+        return g_image, g_mask, None, None, None, None
 
 
 def generalised_geodesic2d_differentiable(image: torch.Tensor, softmask: torch.Tensor, v: float, lamb: float,
-                                          iter: int = 2) -> torch.Tensor:
+                                          iter: int = 2, recompute: bool = False) -> torch.Tensor:
     """Differentiable generalised geodesic distance of a batch of 2D images.
 
     Args:
         image: ``[B, C, H, W]`` float32 CUDA tensor (C <= 4, sides <= 2048).
         softmask: ``[B, 1, H, W]`` float32 CUDA tensor.
         v, lamb, iter: as in :func:`generalised_geodesic2d`.
+        recompute: keep one pass's argmin tape instead of all of them and
+            recompute the forward during the backward (less memory, more work,
+            the same gradients).
 
     Returns ``[B, 1, H, W]``; gradients flow to ``image`` and ``softmask``.
     """
@@ -142,4 +177,4 @@ def generalised_geodesic2d_differentiable(image: torch.Tensor, softmask: torch.T
         raise RuntimeError("differentiable transforms handle up to 4 channels and sides up to 2048")
     with torch.cuda.device(image.device):
         return GeneralisedGeodesic2dFunction.apply(image.contiguous(), softmask.contiguous(), float(v),
-                                                   float(lamb), int(iter))
+                                                   float(lamb), int(iter), bool(recompute))

@@ -230,10 +230,14 @@ __device__ fg_batch2d_item as_batch_item(const fg_grad2d_item &g) {
   return b;
 }
 
+// tape_pass < 0: record the tape of every pass at (iteration * 4 + pass) * H * W.
+// tape_pass >= 0: run the passes up to that one (numbered iteration * 4 + k)
+// and record only its tape, at the start of the item's tape buffer (the
+// memory-saving mode's recomputation).
 template <int CT>
 __global__ void __launch_bounds__(kThreads, 1)
-    fg_grad2d_forward_kernel(const fg_grad2d_item *items, int n, int iterations, int S, float r2, int *counter,
-                             int *status) {
+    fg_grad2d_forward_kernel(const fg_grad2d_item *items, int n, int iterations, int tape_pass, int S, float r2,
+                             int *counter, int *status) {
   extern __shared__ __align__(16) float sm[];
   __shared__ int s_item;
   __shared__ PassArgs s_args;
@@ -249,23 +253,32 @@ __global__ void __launch_bounds__(kThreads, 1)
       batch_prologue(it, false, sm);
       __threadfence();
       __syncthreads();
-      for (int iter = 0; iter < iterations; iter++) {
-        for (int k = 0; k < 4; k++) {
-          const int L = k >= 2 ? it.W : it.H;
-          const bool wt = k & 1;
-          if (L <= 1 && !wt) continue;
-          if (threadIdx.x == 0) {
-            batch_pass_args(it, 1, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), 1), r2, status, &s_args);
-            s_args.tape = g.tape + (long long)(iter * 4 + k) * P;
-          }
-          __syncthreads();
+      const int npass = tape_pass >= 0 ? tape_pass + 1 : 4 * iterations;
+      for (int pi = 0; pi < npass; pi++) {
+        const int k = pi & 3;
+        const int L = k >= 2 ? it.W : it.H;
+        const bool wt = k & 1;
+        if (L <= 1 && !wt) continue;
+        const bool rec = tape_pass < 0 || pi == tape_pass;
+        if (threadIdx.x == 0) {
+          batch_pass_args(it, 1, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), 1), r2, status, &s_args);
+          s_args.tape = rec ? g.tape + (tape_pass < 0 ? (long long)pi * P : 0) : nullptr;
+        }
+        __syncthreads();
+        // the tape-recording body gives the same distances as the plain one
+        if (rec) {
           if (wt)
             pass_body<1, CT, 1, MODE_GENERAL, true, true, false>(s_args, 0, sm);
           else
             pass_body<1, CT, 1, MODE_GENERAL, false, true, false>(s_args, 0, sm);
-          __threadfence();
-          __syncthreads();
+        } else {
+          if (wt)
+            pass_body<1, CT, 1, MODE_GENERAL, true, false, false>(s_args, 0, sm);
+          else
+            pass_body<1, CT, 1, MODE_GENERAL, false, false, false>(s_args, 0, sm);
         }
+        __threadfence();
+        __syncthreads();
       }
     }
     __syncthreads();
@@ -280,7 +293,7 @@ __device__ __forceinline__ float sgnf(float d) { return d > 0.0f ? 1.0f : (d < 0
 // either stays with Dold (the pass input) or moves to the predecessor
 // D[t-1][x+k] (and to the image through l_grad * |I - I'| of that step).
 template <int NCH>
-__device__ void adjoint_pass(const fg_grad2d_item &g, int k, int iter, int C, float *sm) {
+__device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char *tape, int C, float *sm) {
   const int tid = threadIdx.x, NT = blockDim.x;
   const int H = g.H, W = g.W;
   const long long P = (long long)H * W;
@@ -296,7 +309,6 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, int iter, int C, fl
   float *Gin = alongW ? g.g_t : g.g_r;
   const float *I = alongW ? g.image_t : g.image;
   float *gI = alongW ? g.gi_t : g.g_image;
-  const unsigned char *tape = g.tape + (long long)(iter * 4 + k) * P;
   const float lg = g.l_grad;
   float *gv = sm;                                   // [N] gradient handed to the previous row
   int *cd = reinterpret_cast<int *>(sm + N);        // [N] tape code of the row
@@ -372,9 +384,17 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, int iter, int C, fl
   }
 }
 
+// Adjoints of the passes pass_hi down to pass_lo (numbered iteration * 4 + k);
+// the tape of pass pi is at (pi - tape_base) * H * W.  kGradInit: the gradient
+// state starts from dLoss/dD; kGradFinal: dLoss/dmask and dLoss/dimage are
+// written at the end.  One call with both flags over every pass is the whole
+// backward; the memory-saving mode calls it once per pass.
+constexpr int kGradInit = 1, kGradFinal = 2;
+
 template <int NCH>
 __global__ void __launch_bounds__(kThreads, 1)
-    fg_grad2d_backward_kernel(const fg_grad2d_item *items, int n, int iterations, int *counter) {
+    fg_grad2d_backward_kernel(const fg_grad2d_item *items, int n, int pass_hi, int pass_lo, int tape_base,
+                              int flags, int *counter) {
   extern __shared__ __align__(16) float sm[];
   __shared__ int s_item;
   for (;;) {
@@ -386,24 +406,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int H = g.H, W = g.W, C = g.C;
     const long long P = (long long)H * W;
     if (P > 0) {
-      for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_r[p] = g.g_out[p];
-      for (long long p = threadIdx.x; p < C * P; p += blockDim.x) g.g_image[p] = 0.0f, g.gi_t[p] = 0.0f;
-      __threadfence();
-      __syncthreads();
-      for (int iter = iterations - 1; iter >= 0; iter--) {
-        for (int k = 3; k >= 0; k--) {
-          const int L = k >= 2 ? W : H;
-          if (L <= 1 && !(k & 1)) continue;  // the forward skipped this pass
-          adjoint_pass<NCH>(g, k, iter, C, sm);
-          __threadfence();
-          __syncthreads();
-        }
+      if (flags & kGradInit) {
+        for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_r[p] = g.g_out[p];
+        for (long long p = threadIdx.x; p < C * P; p += blockDim.x) g.g_image[p] = 0.0f, g.gi_t[p] = 0.0f;
+        __threadfence();
+        __syncthreads();
       }
-      // dLoss/dmask = v * dLoss/dD0 ; dLoss/dimage = its original-layout part + the transposed part
-      for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_mask[p] = __fmul_rn(g.v, g.g_r[p]);
-      for (long long q = threadIdx.x; q < C * P; q += blockDim.x) {
-        const long long c = q / P, r = q - c * P, h = r / W, w = r - h * W;
-        g.g_image[q] = __fadd_rn(g.g_image[q], g.gi_t[c * P + w * H + h]);
+      for (int pi = pass_hi; pi >= pass_lo; pi--) {
+        const int k = pi & 3;
+        const int L = k >= 2 ? W : H;
+        if (L <= 1 && !(k & 1)) continue;  // the forward skipped this pass
+        adjoint_pass<NCH>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
+        __threadfence();
+        __syncthreads();
+      }
+      if (flags & kGradFinal) {
+        // dLoss/dmask = v * dLoss/dD0 ; dLoss/dimage = its original-layout part + the transposed part
+        for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_mask[p] = __fmul_rn(g.v, g.g_r[p]);
+        for (long long q = threadIdx.x; q < C * P; q += blockDim.x) {
+          const long long c = q / P, r = q - c * P, h = r / W, w = r - h * W;
+          g.g_image[q] = __fadd_rn(g.g_image[q], g.gi_t[c * P + w * H + h]);
+        }
       }
     }
     __syncthreads();
@@ -413,9 +436,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 }  // namespace
 }  // namespace fgi
 
-extern "C" FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
-                                                 int iterations, int *counter, int *status, void *stream) {
-  using namespace fgi;
+namespace fgi {
+namespace {
+int grad_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent, int iterations, int tape_pass,
+                 int *counter, int *status, void *stream) {
   if (n < 0 || (n > 0 && (!items || !counter || !status)))
     return set_error(FG_ERR_INVALID_ARGUMENT, "grad: null descriptor, counter or status pointer");
   if (max_C < 1 || max_C > kMaxChannels) return set_error(FG_ERR_UNSUPPORTED, "grad: images need 1 to 4 channels");
@@ -435,17 +459,30 @@ extern "C" FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, in
   auto launch = [&](auto fn) -> int {
     cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
-    fn<<<grid, kThreads, smem, s>>>(items, n, std::max(iterations, 0), S, r2, counter, status);
+    fn<<<grid, kThreads, smem, s>>>(items, n, std::max(iterations, 0), tape_pass, S, r2, counter, status);
     e2 = cudaGetLastError();
     return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
   };
   return max_C == 1 ? launch(fg_grad2d_forward_kernel<1>) : launch(fg_grad2d_forward_kernel<0>);
 }
+}  // namespace
+}  // namespace fgi
 
-extern "C" FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
-                                                  int iterations, int *counter, int *status, void *stream) {
-  using namespace fgi;
-  (void)status;
+extern "C" FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                                 int iterations, int *counter, int *status, void *stream) {
+  return fgi::grad_forward(items, n, max_C, max_extent, iterations, -1, counter, status, stream);
+}
+
+extern "C" FG_API int fg_grad_geodesic2d_forward_pass(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                                      int pass, int *counter, int *status, void *stream) {
+  if (pass < 0) return fgi::set_error(FG_ERR_INVALID_ARGUMENT, "grad: negative pass index");
+  return fgi::grad_forward(items, n, max_C, max_extent, pass / 4 + 1, pass, counter, status, stream);
+}
+
+namespace fgi {
+namespace {
+int grad_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent, int pass_hi, int pass_lo,
+                  int tape_base, int flags, int *counter, void *stream) {
   if (n < 0 || (n > 0 && (!items || !counter)))
     return set_error(FG_ERR_INVALID_ARGUMENT, "grad: null descriptor or counter pointer");
   if (max_C < 1 || max_C > kMaxChannels) return set_error(FG_ERR_UNSUPPORTED, "grad: images need 1 to 4 channels");
@@ -463,9 +500,25 @@ extern "C" FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, i
   auto launch = [&](auto fn) -> int {
     cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
-    fn<<<grid, kThreads, smem, s>>>(items, n, std::max(iterations, 0), counter);
+    fn<<<grid, kThreads, smem, s>>>(items, n, pass_hi, pass_lo, tape_base, flags, counter);
     e2 = cudaGetLastError();
     return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
   };
   return max_C == 1 ? launch(fg_grad2d_backward_kernel<1>) : launch(fg_grad2d_backward_kernel<kMaxChannels>);
+}
+}  // namespace
+}  // namespace fgi
+
+extern "C" FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                                  int iterations, int *counter, int *status, void *stream) {
+  (void)status;
+  return fgi::grad_backward(items, n, max_C, max_extent, 4 * std::max(iterations, 0) - 1, 0, 0,
+                            fgi::kGradInit | fgi::kGradFinal, counter, stream);
+}
+
+extern "C" FG_API int fg_grad_geodesic2d_backward_pass(const fg_grad2d_item *items, int n, int max_C, int max_extent,
+                                                       int pass, int first, int last, int *counter, void *stream) {
+  if (pass < 0) return fgi::set_error(FG_ERR_INVALID_ARGUMENT, "grad: negative pass index");
+  return fgi::grad_backward(items, n, max_C, max_extent, pass, pass, pass,
+                            (first ? fgi::kGradInit : 0) | (last ? fgi::kGradFinal : 0), counter, stream);
 }

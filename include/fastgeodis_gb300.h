@@ -243,6 +243,22 @@ FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int ma
 FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
                                        int iterations, int *counter, int *status, void *stream);
 
+/* Memory-saving form of the two calls above (no counterpart in the reference):
+ * instead of every pass's tape (iterations * 4 * H * W bytes) an item's tape
+ * buffer holds one pass (H * W bytes), and the passes are recomputed.  Passes
+ * are numbered iteration * 4 + k (k: H forward, H backward, W forward, W
+ * backward).  _forward_pass runs passes 0 .. pass from the initial distances
+ * and records only that pass's tape; `out` receives the distances after it
+ * (point it at scratch when recomputing, to keep the real output).
+ * _backward_pass applies the adjoint of that one pass; first = 1 starts the
+ * gradient state from g_out, last = 1 writes g_mask and g_image.  Calling
+ * forward_pass(p) then backward_pass(p) for p from the last pass down to 0
+ * gives the same gradients, bit for bit, as fg_grad_geodesic2d_backward. */
+FG_API int fg_grad_geodesic2d_forward_pass(const fg_grad2d_item *items, int n, int max_C, int max_extent, int pass,
+                                           int *counter, int *status, void *stream);
+FG_API int fg_grad_geodesic2d_backward_pass(const fg_grad2d_item *items, int n, int max_C, int max_extent, int pass,
+                                            int first, int last, int *counter, void *stream);
+
 /* Soft mask of an interactive request from its clicks (no counterpart in the
  * reference, whose callers build masks on the host): writes mask[D][H][W]
  * (D = 1 for a 2D image) with 0.0 at every voxel within Euclidean distance

@@ -113,3 +113,23 @@ def test_gradients_vs_float64_finite_differences():
     # the derivative is piecewise constant; a sample may sit within eps of a
     # change of optimal path, so most (not all) samples must agree
     assert ok_i >= 14 and ok_m >= 14, (ok_i, ok_m)
+
+
+@pytest.mark.parametrize("iters,C,shape", [(1, 1, (40, 33)), (2, 1, (64, 64)), (3, 3, (37, 52))])
+def test_recompute_mode_gives_the_same_bits(iters, C, shape):
+    # one pass's tape plus recomputation instead of every pass's tape
+    g = torch.Generator().manual_seed(11 + iters)
+    B = 3
+    img = (torch.rand((B, C) + shape, generator=g) * 255).cuda()
+    msk = torch.sigmoid(torch.randn((B, 1) + shape, generator=g)).cuda()
+    w = torch.rand((B, 1) + shape, generator=g).cuda()
+    res = []
+    for rec in (False, True):
+        a = img.clone().requires_grad_(True)
+        m = msk.clone().requires_grad_(True)
+        d = fg.generalised_geodesic2d_differentiable(a, m, 10.0, 0.75, iters, recompute=rec)
+        (d * w).sum().backward()
+        res.append((d.detach(), a.grad, m.grad))
+    for x, y in zip(res[0], res[1]):
+        assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+    fg.check_status()
