@@ -124,6 +124,9 @@ def profile_launch_times():
     return [(float(ms[i]), int(st[i])) for i in range(n.value)]
 
 
+FG_PLAN_LEAN = 1      # plan flag: the 64-register kernel
+FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-section
+# the last field holds the plan flags (FG_PLAN_LEAN | FG_PLAN_CLUSTER)
 PLAN_FIELDS = ("S", "T1", "T2", "K1", "K2", "tiles1", "tiles2", "threads", "depth", "smem", "lean")
 
 

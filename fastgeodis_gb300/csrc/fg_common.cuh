@@ -28,6 +28,7 @@ __host__ __device__ constexpr int pass_max_threads(int cross, int cimg, int maps
 constexpr int kMaxMaps = 2;              // distance maps updated by one launch (they share the image)
 constexpr int kMaxChannels = 4;          // image channels held in registers
 constexpr int kMaxTiles = 2048;          // tiles of one pass (all co-resident)
+constexpr int kMaxCluster = 16;          // CTAs of a cluster plan (non-portable cluster size)
 constexpr unsigned kSpinLimit = 1u << 23; // polls of one halo word (each an L2 round trip, ~0.3-1 us) before FG_ERR_TIMEOUT
 
 // Arithmetic of one candidate.  GENERAL is the reference expression
@@ -109,6 +110,8 @@ constexpr int max_pass_depth(int nch, int m) { return (nch + m <= 4) ? 8 : 2; }
 // Launchers (one translation unit per cross-section rank).
 int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
+// Volume passes on a cluster plan (fg_pass3d_cluster.cu): c.tiles CTAs in one cluster.
+int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
 // in place; spacing_sq = nullptr for images.  bar: 4 counters (16 bytes) of

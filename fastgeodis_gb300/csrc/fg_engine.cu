@@ -185,7 +185,8 @@ DeviceInfo device_info() {
 struct Plan {
   int T1, T2, K1, K2, tiles1, tiles2, S, NT, B2, rowf, P;
   size_t smem;
-  bool lean;  // 64-register kernel
+  bool lean;     // 64-register kernel
+  bool cluster;  // one thread-block cluster of tiles1 strips of whole rows (fg_pass3d_cluster.cu)
 };
 
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
@@ -225,9 +226,37 @@ double cone_avg_runs(int cross, int R1, int R2, int K1, int K2, int S) {
   return sum / S;
 }
 
-// Plan overrides set by the autotuner (fg_plan_override): cross-section shape -> (S, T1, T2, lean).
+// Plan overrides set by the autotuner (fg_plan_override): cross-section shape
+// -> (S, T1, T2, flags); flags: FG_PLAN_LEAN, FG_PLAN_CLUSTER.
 std::mutex g_override_mu;
 std::map<std::tuple<int, int, int>, std::tuple<int, int, int, int>> g_overrides;
+
+// A cluster plan for a volume pass: ceil(N1 / T1) strips of T1 whole rows,
+// one CTA each, 2 to 16 CTAs in one cluster.  S is the transposed write's
+// flush period (halved until the rings fit; at least 2, the apron rings'
+// depth); the staging depth is the largest that fits one CTA per SM.
+bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1, bool want_lean, Plan *out) {
+  T1 = std::max(1, std::min(T1, N1));
+  const int G = (N1 + T1 - 1) / T1;
+  if (G < 2 || G > kMaxCluster) return false;
+  const int cimg = mode == MODE_EUCLID ? 0 : C;
+  const int runs = T1 * ((N2 + 3) / 4);
+  const int nt = std::max(32, (runs + 31) / 32 * 32);
+  if (nt > pass_max_threads(2, cimg, M)) return false;
+  const bool lean = nt > kThreads || (want_lean && pass_lean(2, cimg, M));
+  const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
+  for (int s2 = wt ? std::max(2, std::min(S, 8)) : 2; s2 >= 2; s2 /= 2) {
+    for (int depth = max_pass_depth(nch, M); depth >= 2; depth /= 2) {
+      int B2, rowf, nown;
+      const size_t sm = pass_smem_bytes(2, C, M, mode, wt, s2, T1, N2, &B2, &rowf, &nown, depth);
+      if (sm <= kSmemBudget) {
+        *out = Plan{T1, N2, 0, 0, G, 1, wt ? s2 : 8, nt, B2, rowf, depth, sm, lean, true};
+        return true;
+      }
+    }
+  }
+  return false;
+}
 std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older cache entries are stale
 
 bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int max_tiles, Plan *out) {
@@ -283,7 +312,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     // one CTA per SM (shared memory or registers): no room for a concurrent transform
     if (sm > kSmemBudget / 2 || nt > kThreads) cost *= 1.05;
     if (!found || cost < best_cost - 1e-9) {
-      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean};
+      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean, false};
       best_cost = cost;
       found = true;
     }
@@ -295,7 +324,13 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     auto it = g_overrides.find(std::make_tuple(cross, N1, N2));
     if (it != g_overrides.end()) std::tie(ovS, ovT1, ovT2, ovLean) = it->second;
   }
-  if (ovS > 0) {
+  if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
+    Plan cp;
+    if (cluster_plan(N1, N2, C, M, mode, wt, ovS, ovT1, (ovLean & FG_PLAN_LEAN) != 0, &cp)) {
+      best = cp;
+      found = true;
+    }
+  } else if (ovS > 0) {
     const int T1 = cross == 2 ? std::min(ovT1, N1) : 1, T2 = std::min(ovT2, N2);
     const int t1 = (N1 + T1 - 1) / T1, t2 = (N2 + T2 - 1) / T2;
     if ((long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, ovLean != 0);
@@ -331,9 +366,9 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (debug)
       fprintf(stderr,
               "[fg plan] cross=%d N=%dx%d C=%d M=%d mode=%d wt=%d -> T=%dx%d K=%d,%d tiles=%dx%d S=%d NT=%d "
-              "P=%d smem=%zu lean=%d cost=%.0f\n",
+              "P=%d smem=%zu lean=%d cluster=%d cost=%.0f\n",
               cross, N1, N2, C, M, mode, (int)wt, best.T1, best.T2, best.K1, best.K2, best.tiles1, best.tiles2,
-              best.S, best.NT, best.P, best.smem, (int)best.lean, best_cost);
+              best.S, best.NT, best.P, best.smem, (int)best.lean, (int)best.cluster, best_cost);
   }
   return found;
 }
@@ -461,6 +496,7 @@ int profiled_launch(cudaStream_t s, long long vp, int steps, Launch launch) {
 int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt, cudaStream_t s) {
   LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean};
   return profiled_launch(s, (long long)a.L * a.N1 * a.N2 * M, a.L, [&] {
+    if (p.cluster) return launch_pass_cluster(a, c, M, mode, wt, s);
     return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
   });
 }
@@ -812,7 +848,10 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
   } else {
     if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    g_overrides[key] = std::make_tuple(S, T1, T2, lean != 0 ? 1 : 0);
+    if (lean < 0 || lean > (FG_PLAN_LEAN | FG_PLAN_CLUSTER)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
+    if ((lean & FG_PLAN_CLUSTER) && (cross != 2 || S < 2))
+      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: cluster plans are for volume passes, with S >= 2");
+    g_overrides[key] = std::make_tuple(S, T1, T2, lean);
   }
   g_plan_epoch.fetch_add(1);
   return FG_OK;
@@ -827,7 +866,8 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
   const int c = mode == MODE_EUCLID ? 0 : C;
   if (!make_plan(cross, N1, N2, c, maps, mode, transposed_write != 0, std::min(sms, kMaxTiles), &p))
     return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
-  const int v[11] = {p.S, p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem, (int)p.lean};
+  const int v[11] = {p.S,  p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem,
+                     (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0)};
   for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }

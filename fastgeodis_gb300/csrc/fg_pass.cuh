@@ -28,6 +28,10 @@
 //     (held as NaN) never contribute a candidate, as in the reference.
 #pragma once
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "fg_common.cuh"
 
 namespace fgi {
@@ -67,6 +71,54 @@ __device__ __forceinline__ float ldg_nc_pinned(const float *p) {
   asm volatile("ld.global.nc.f32 %0, [%1];\n" : "=f"(v) : "l"(p));
   return v;
 }
+
+// --- thread-block cluster primitives (cluster plans) ---
+__device__ __forceinline__ unsigned cl_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+// address of the same shared-memory offset in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned cl_map(unsigned a, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cl_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_init(unsigned a, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+// one arrival that also expects `tx` bytes of asynchronous stores in this phase
+__device__ __forceinline__ void mbar_expect(unsigned a, unsigned tx) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(tx) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned a, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// stores into another CTA's shared memory that complete on its mbarrier `bar`
+__device__ __forceinline__ void st_async4(unsigned a, const float4 &v, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];\n" ::"r"(a),
+               "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
+               "r"(__float_as_uint(v.w)), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async1(unsigned a, float v, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];\n" ::"r"(a),
+               "r"(__float_as_uint(v)), "r"(bar)
+               : "memory");
+}
+constexpr unsigned kClusterSpinLimit = 1u << 16;  // failed mbarrier polls of one step before FG_ERR_TIMEOUT
 
 __device__ __forceinline__ float f4get(const float4 &v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
@@ -151,7 +203,18 @@ __device__ __forceinline__ void cp_async_wait() {
 // into registers first so the step loop never reloads its fields.
 // MULTI = false compiles a single-tile body (no halo exchange, no cone): the
 // batched kernels, whose CTA always owns a whole image.
-template <int CROSS, int CT, int M, int MODE, bool WT, bool TAPE = false, bool MULTI = true>
+//
+// CL = true: a cluster plan.  The CTAs of one thread-block cluster own strips
+// of whole rows of the cross-section (tiles1 = cluster size, tiles2 = 1, no
+// halo; `tile` is the CTA's rank).  After every step but the last, a strip's
+// first and last rows (distances and image values, with their edge slots) go
+// straight into the apron rows of the neighbour strips' rings with st.async,
+// which completes on the receiver's mbarrier of that step's parity.  The
+// receiver arms that mbarrier with the bytes it expects, and its apron
+// readers wait on it before the next step.  A sender cannot run more than one
+// step ahead of a receiver's reads (it needs the receiver's rows of the step
+// before), so rings of two steps suffice and no hand-off goes through L2.
+template <int CROSS, int CT, int M, int MODE, bool WT, bool TAPE = false, bool MULTI = true, bool CL = false>
 __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, float *sm) {
   const PassArgs a = ar;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
@@ -186,7 +249,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   int2 *otab = reinterpret_cast<int2 *>(oring + P * AR * NT);  // own cells (transposed flush)
 
   // --- set-up ---
-  const bool has_nb = MULTI && a.tiles1 * a.tiles2 > 1;
+  const bool has_nb = MULTI && !CL && a.tiles1 * a.tiles2 > 1;
   // run of this thread: with neighbours, runs ordered innermost first, so
   // the runs outside a step's cone are whole trailing warps
   int qrun = tid, cdist = S;
@@ -241,7 +304,31 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   // exchange words of this thread's run (cell (g1, g20) of the cross-section), parity 0, map 0
   const long long xplane = (long long)a.N1 * a.N2;
   unsigned long long *const xrun = has_nb ? a.xch + (long long)g1 * a.N2 + g20 : nullptr;
-  __syncthreads();
+
+  // cluster plan: two mbarriers after the own-cell table; every neighbour
+  // strip sends its boundary row each step, 24 bytes per run and array
+  unsigned cbar = 0, cl_bytes = 0, cl_sm[2] = {0, 0};
+  bool cl_push[2] = {false, false}, cl_waits = false, cl_dead = false;
+  if (CL) {
+    const int rank = tile, nr = a.tiles1;
+    cbar = smem_u32(otab + (WT ? R1 * R2 : 0));
+    cl_bytes = (unsigned)(((rank > 0 ? 1 : 0) + (rank < nr - 1 ? 1 : 0)) * rpr * 24 * (M + C));
+    cl_push[0] = active && r1 == 0 && rank > 0;           // first row -> the upper strip's lower apron
+    cl_push[1] = active && r1 == R1 - 1 && rank < nr - 1; // last row -> the lower strip's upper apron
+    if (cl_push[0]) cl_sm[0] = cl_map(smem_u32(sm), rank - 1);
+    if (cl_push[1]) cl_sm[1] = cl_map(smem_u32(sm), rank + 1);
+    cl_waits = tid == 0 || (active && (r1 == 0 || r1 == R1 - 1));  // apron readers, and the arming thread
+    if (tid == 0) {
+      mbar_init(cbar, 1);
+      mbar_init(cbar + 8, 1);
+      mbar_fence_init();
+      if (L >= 2) mbar_expect(cbar, cl_bytes);      // step 0
+      if (L >= 3) mbar_expect(cbar + 8, cl_bytes);  // step 1
+    }
+    cl_sync();  // rings filled and mbarriers armed in every CTA before the first push
+  } else {
+    __syncthreads();
+  }
 
   // running offsets: read layout of the next step to prefetch, write layout of the current step
   const long long rstep = a.dir > 0 ? a.s_str : -a.s_str;
@@ -293,6 +380,18 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
 
   for (int t = 0; t < L; t++) {
     const int slot = t & (P - 1);
+    if (CL && t > 0 && cl_waits) {
+      // the neighbour strips' rows of step t-1 have landed in the apron rows
+      const unsigned bar = cbar + ((t - 1) & 1) * 8, par = ((t - 1) >> 1) & 1;
+      unsigned spins = 0;
+      while (!cl_dead && !mbar_try_wait(bar, par)) {
+        if (++spins > kClusterSpinLimit || ((spins & 255u) == 0 && ld_status(a.status) != 0)) {
+          atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
+          cl_dead = true;  // results are void; later steps no longer wait
+        }
+      }
+      if (tid == 0 && !cl_dead && t + 1 <= L - 2) mbar_expect(bar, cl_bytes);  // the same parity's next step
+    }
     // exact halo values of the previous row from the neighbour tiles
     if (has_nb && t > 0 && (t & (S - 1)) == 0) {
       if (halo) {
@@ -451,6 +550,35 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
           for (int i = 0; i < 4; i++)
             if (own & (1u << i)) st_word(xw + m * xplane + i, ep | __float_as_uint(f4get(out[m], i)));
       }
+      if (CL && t + 1 < L && (cl_push[0] || cl_push[1])) {
+        // this strip's boundary row of step t into the neighbours' apron rows
+        const unsigned bar = cbar + (t & 1) * 8;
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+          if (!cl_push[side]) continue;
+          const int row = side == 0 ? R1 + 1 : 0;  // the receiver's apron row
+          const unsigned rsm = cl_sm[side], rbar = rsm + (bar - smem_u32(sm));
+          const unsigned lsm = smem_u32(sm);
+          const int pe = row * EP2 + (u + 1) * 2;
+#pragma unroll
+          for (int m = 0; m < M; m++) {
+            const unsigned d = rsm + (smem_u32(dring + (t & (SR - 1)) * M * rowf + m * rowf + row * B2 + 4 + 4 * u) - lsm);
+            const unsigned e = rsm + (smem_u32(dedge + (t & (SR - 1)) * M * edgef + m * edgef + pe) - lsm);
+            st_async4(d, out[m], rbar);
+            st_async1(e - 4, out[m].x, rbar);
+            st_async1(e + 8, out[m].w, rbar);
+          }
+#pragma unroll
+          for (int c = 0; c < NCH; c++)
+            if (c < C) {
+              const unsigned d = rsm + (smem_u32(iring + (t & 1) * C * rowf + c * rowf + row * B2 + 4 + 4 * u) - lsm);
+              const unsigned e = rsm + (smem_u32(iedge + (t & 1) * C * edgef + c * edgef + pe) - lsm);
+              st_async4(d, icur[c], rbar);
+              st_async1(e - 4, icur[c].x, rbar);
+              st_async1(e + 8, icur[c].w, rbar);
+            }
+        }
+      }
       float *dc = dring + (t & (SR - 1)) * M * rowf + cb;
       float *dce = dedge + (t & (SR - 1)) * M * edgef;
 #pragma unroll
@@ -517,6 +645,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     }
   }
   cp_async_wait<0>();
+  if (CL) cl_sync();  // no CTA leaves while a neighbour may still address its shared memory
 }
 
 // Register budget: 128 (CTAs up to 512 threads), or 64 for the lean kernel
@@ -528,50 +657,100 @@ __global__ void __maxnreg__((LEAN ? 64 : 128)) fg_pass_kernel(const PassArgs a) 
   pass_body<CROSS, CT, M, MODE, WT>(a, blockIdx.x, sm);
 }
 
+// The same pass on a cluster plan: one cluster of tiles1 CTAs, one strip each.
 template <int CROSS, int CT, int M, int MODE, bool WT, bool LEAN>
+__global__ void __maxnreg__((LEAN ? 64 : 128)) fg_pass_cluster_kernel(const PassArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  pass_body<CROSS, CT, M, MODE, WT, false, true, true>(a, (int)cl_rank(), sm);
+}
+
+// Whether one cluster of this launch configuration can be co-scheduled on
+// the device (cached per kernel, cluster size, CTA size and shared memory).
+inline bool cluster_fits(const void *fn, const cudaLaunchConfig_t &cfg, int dev) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void *, unsigned, unsigned, size_t, int>, bool> cache;
+  const auto key = std::make_tuple(fn, cfg.gridDim.x, cfg.blockDim.x, cfg.dynamicSmemBytes, dev);
+  std::lock_guard<std::mutex> g(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, fn, &cfg);
+  if (e != cudaSuccess) (void)cudaGetLastError();
+  const bool ok = e == cudaSuccess && n > 0;
+  cache[key] = ok;
+  return ok;
+}
+
+// Launch of one variant.  CLU: the cluster plan (one cluster of c.tiles CTAs);
+// otherwise a cooperative launch of c.tiles CTAs.
+template <int CROSS, int CT, int M, int MODE, bool WT, bool LEAN, bool CLU>
 int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
-  auto fn = fg_pass_kernel<CROSS, CT, M, MODE, WT, LEAN>;
+  void (*fn)(const PassArgs);
+  if constexpr (CLU) fn = fg_pass_cluster_kernel<CROSS, CT, M, MODE, WT, LEAN>;
+  else fn = fg_pass_kernel<CROSS, CT, M, MODE, WT, LEAN>;
   static unsigned long long configured = 0;  // bit per device (set under the engine's launch lock)
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 64 && !(configured & (1ull << dev))) {
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess && CLU) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
     configured |= 1ull << dev;
   }
   void *args[] = {const_cast<PassArgs *>(&a)};
-  if (c.tiles > 1)
-    e = cudaLaunchCooperativeKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
-  else
-    e = cudaLaunchKernel((const void *)fn, dim3(1), dim3(c.threads), args, c.smem, s);
+  if constexpr (CLU) {
+    if (c.tiles < 2 || c.tiles > kMaxCluster) return set_error(FG_ERR_UNSUPPORTED, "a cluster plan has 2 to 16 CTAs");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c.tiles);
+    cfg.blockDim = dim3(c.threads);
+    cfg.dynamicSmemBytes = c.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c.tiles;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (!cluster_fits(reinterpret_cast<const void *>(fn), cfg, dev))
+      return set_error(FG_ERR_UNSUPPORTED, "the device cannot co-schedule this cluster plan");
+    e = cudaLaunchKernelExC(&cfg, (const void *)fn, args);
+  } else {
+    if (c.tiles > 1)
+      e = cudaLaunchCooperativeKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
+    else
+      e = cudaLaunchKernel((const void *)fn, dim3(1), dim3(c.threads), args, c.smem, s);
+  }
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   return FG_OK;
 }
 
-template <int CROSS, int CT, int M, int MODE, bool WT>
+template <int CROSS, int CT, int M, int MODE, bool WT, bool CLU>
 int launch_regs(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
   if constexpr (pass_lean(CROSS, CT == 0 ? kMaxChannels : CT, M)) {  // CT = 0: up to 4 channels
-    if (c.lean) return launch_variant<CROSS, CT, M, MODE, WT, true>(a, c, s);
+    if (c.lean) return launch_variant<CROSS, CT, M, MODE, WT, true, CLU>(a, c, s);
   }
   if (c.threads > kThreads) return set_error(FG_ERR_UNSUPPORTED, "a 128-register sweep CTA has at most 512 threads");
-  return launch_variant<CROSS, CT, M, MODE, WT, false>(a, c, s);
+  return launch_variant<CROSS, CT, M, MODE, WT, false, CLU>(a, c, s);
 }
 
-template <int CROSS, int M, bool WT>
+template <int CROSS, int M, bool WT, bool CLU>
 int launch_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStream_t s) {
   const bool one = a.C == 1;
-  if (mode == MODE_EUCLID) return launch_regs<CROSS, 1, M, MODE_EUCLID, WT>(a, c, s);
+  if (mode == MODE_EUCLID) return launch_regs<CROSS, 1, M, MODE_EUCLID, WT, CLU>(a, c, s);
   if (mode == MODE_GEO)
-    return one ? launch_regs<CROSS, 1, M, MODE_GEO, WT>(a, c, s) : launch_regs<CROSS, 0, M, MODE_GEO, WT>(a, c, s);
-  return one ? launch_regs<CROSS, 1, M, MODE_GENERAL, WT>(a, c, s)
-             : launch_regs<CROSS, 0, M, MODE_GENERAL, WT>(a, c, s);
+    return one ? launch_regs<CROSS, 1, M, MODE_GEO, WT, CLU>(a, c, s) : launch_regs<CROSS, 0, M, MODE_GEO, WT, CLU>(a, c, s);
+  return one ? launch_regs<CROSS, 1, M, MODE_GENERAL, WT, CLU>(a, c, s)
+             : launch_regs<CROSS, 0, M, MODE_GENERAL, WT, CLU>(a, c, s);
 }
 
-template <int CROSS>
+template <int CROSS, bool CLU = false>
 int launch_cross(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
-  if (M == 1) return wt ? launch_mode<CROSS, 1, true>(a, c, mode, s) : launch_mode<CROSS, 1, false>(a, c, mode, s);
-  if (M == 2) return wt ? launch_mode<CROSS, 2, true>(a, c, mode, s) : launch_mode<CROSS, 2, false>(a, c, mode, s);
+  if (M == 1)
+    return wt ? launch_mode<CROSS, 1, true, CLU>(a, c, mode, s) : launch_mode<CROSS, 1, false, CLU>(a, c, mode, s);
+  if (M == 2)
+    return wt ? launch_mode<CROSS, 2, true, CLU>(a, c, mode, s) : launch_mode<CROSS, 2, false, CLU>(a, c, mode, s);
   return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
 }
 

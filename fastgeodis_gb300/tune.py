@@ -13,7 +13,9 @@ A workload of several transforms of one shape that run at the same time
 tuned as such: the timed unit is all of them, launched on their own streams,
 and the candidates include plans with fewer, larger tiles (a fraction of the
 SMs per transform), which waste less work on halos while the transforms
-share the GPU.
+share the GPU.  Volume passes also try cluster plans: one thread-block
+cluster of up to 16 CTAs owns the whole cross-section (no halo, no hand-off
+through global memory), so concurrent transforms each take a few SMs.
 
 Every plan computes the same bits; only the time changes.  Pinned plans hold
 for the process (all calls with that cross-section) until `clear`.
@@ -36,8 +38,8 @@ THREADS_LEAN = 1024
 
 Key = Tuple[int, int, int]        # (cross, N1, N2)
 Choice = Tuple[int, int, int]     # (S, T1, T2)
-# A pinned plan: (S, T1, T2, lean); lean = 1 asks for the 64-register kernel
-# (fg_plan_override), 0 leaves it to the planner.
+# A pinned plan: (S, T1, T2, flags); flags FG_PLAN_LEAN asks for the
+# 64-register kernel, FG_PLAN_CLUSTER for a cluster plan (fg_plan_override).
 
 
 def _ceil(a: int, b: int) -> int:
@@ -87,6 +89,28 @@ def candidates(cross: int, N1: int, N2: int, sms: int, steps=(4, 8), max_per_ste
                     n += 1
                 if n >= max_per_step:
                     break
+    return out
+
+
+def cluster_candidates(cross: int, N1: int, N2: int, lean_capable: bool = True,
+                       sizes: Sequence[int] = (16, 12, 8, 6, 4)) -> List[Tuple[int, int, int, int]]:
+    """Cluster plans of a volume cross-section: (S, T1, N2, flags) for about
+    `sizes` strips of T1 whole rows, one CTA each (2 to 16 per cluster, one
+    thread per run of 4 cells: at most 1024 threads with the 64-register
+    kernel, 512 without)."""
+    if cross != 2:
+        return []
+    max_threads = THREADS_LEAN if lean_capable else THREADS
+    out = []
+    for G in sizes:
+        T1 = _ceil(N1, G)
+        g = _ceil(N1, T1)
+        threads = T1 * _ceil(N2, 4)
+        if g < 2 or g > 16 or threads > max_threads:
+            continue
+        c = (8, T1, N2, _lib.FG_PLAN_CLUSTER | (_lib.FG_PLAN_LEAN if threads > THREADS else 0))
+        if c not in out:
+            out.append(c)
     return out
 
 
@@ -184,9 +208,20 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
                 small = (c[1] + 2 * c[0]) * _ceil(c[2] + 2 * c[0], 4) <= THREADS
                 if lean and cross == 2 and len(lambs) > 1 and small:
                     trials.append(c + (1,))  # 64-register kernel: two CTAs per SM
+            # cluster plans (one thread-block cluster per transform): they pay
+            # off when several transforms share the GPU
+            trials += cluster_candidates(cross, N1, N2, lean_capable=lean)
             for c in trials:
                 _lib.check(L.fg_plan_override(cross, N1, N2, *c))
-                t = measure()
+                try:
+                    t = measure()
+                except _lib.EngineError:
+                    # a cluster plan the device cannot co-schedule: the launch is
+                    # refused before anything runs
+                    if not c[3] & _lib.FG_PLAN_CLUSTER:
+                        raise
+                    torch.cuda.synchronize(dev)
+                    continue
                 if verbose:
                     print(f"[tune] {key} S={c[0]} T={c[1]}x{c[2]} lean={c[3]}: {t:.3f} ms")
                 if t < best_t:

@@ -65,15 +65,26 @@ FG_API size_t fg_workspace_bytes(int op, int C, int D, int H, int W);
  * these values; they exist to tune and to exercise multi-tile plans. */
 FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 
+/* Plan flags (fg_plan_override's `lean` argument, fg_plan_describe's last field). */
+#define FG_PLAN_LEAN 1    /* the 64-register kernel */
+#define FG_PLAN_CLUSTER 2 /* a cluster plan: one thread-block cluster owns the cross-section */
+
 /* Plan override (no counterpart in the reference): for passes whose
  * cross-section is N1 x N2 (cross = 1 for 2D images, N1 = 1; cross = 2 for
  * volumes), use tiles of T1 x T2 cells with S steps per halo hand-off
- * (S in {1,2,4,8}, halo S).  lean = 1 asks for the 64-register kernel where
- * the variant has one (volumes, one image channel or none, one map: two CTAs
- * of up to 512 threads per SM); 0 leaves it to the planner (the 128-register
- * kernel up to 512 threads).  S = 0 removes the override.  Used by the
+ * (S in {1,2,4,8}, halo S).  Flag FG_PLAN_LEAN asks for the 64-register
+ * kernel where the variant has one (volumes, one image channel or none, one
+ * map: two CTAs of up to 512 threads per SM); without it the planner decides
+ * (the 128-register kernel up to 512 threads).  Flag FG_PLAN_CLUSTER (volumes
+ * only, S >= 2) asks for a cluster plan instead: ceil(N1 / T1) CTAs (2 to
+ * 16) of one thread-block cluster each own T1 whole rows, and exchange their
+ * boundary rows every step through distributed shared memory, with no halo
+ * and no hand-off through global memory; T2 is ignored and S is the
+ * transposed write's flush period.  S = 0 removes the override.  Used by the
  * autotuner (fastgeodis_gb300.tune); results do not depend on it.  A plan
- * that does not fit the device falls back to the planner's choice. */
+ * that does not fit the device falls back to the planner's choice, and a
+ * cluster plan that the device cannot co-schedule fails with
+ * FG_ERR_UNSUPPORTED at launch. */
 FG_API int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean);
 
 /* The plan the engine uses for one pass (no counterpart in the reference):
@@ -81,8 +92,8 @@ FG_API int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, in
  * C image channels, `maps` distance maps (1 or 2), arithmetic mode (0
  * general, 1 l_grad == 0, 2 l_eucl == 0 and l_grad == 1), transposed write
  * or not, on a GPU of `sms` SMs.  Writes 11 ints to `plan`: S, T1, T2, K1,
- * K2, tiles1, tiles2, threads, staging depth, shared-memory bytes, lean
- * (1: the 64-register kernel).  Needs no GPU; honours fg_set_tuning and
+ * K2, tiles1, tiles2, threads, staging depth, shared-memory bytes, flags
+ * (FG_PLAN_LEAN, FG_PLAN_CLUSTER).  Needs no GPU; honours fg_set_tuning and
  * fg_plan_override. */
 FG_API int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int transposed_write, int sms,
                             int *plan);

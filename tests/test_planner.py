@@ -119,3 +119,38 @@ def test_bad_queries():
         _lib.plan_describe(3, 4, 4)
     with pytest.raises(ValueError):
         _lib.plan_describe(2, 4, 4, maps=3)
+
+
+@pytest.mark.parametrize("N1,N2", [(256, 256), (128, 256), (20, 27), (64, 64), (9, 100), (2, 8)])
+@pytest.mark.parametrize("C,maps,mode", [(1, 1, 0), (1, 1, 1), (3, 1, 0), (1, 2, 2)])
+@pytest.mark.parametrize("wt", [False, True])
+@pytest.mark.parametrize("G", [2, 4, 16])
+def test_cluster_plans(N1, N2, C, maps, mode, wt, G):
+    L = _lib.load()
+    T1 = -(-N1 // G)
+    _lib.check(L.fg_plan_override(2, N1, N2, 8, T1, N2, _lib.FG_PLAN_CLUSTER))
+    try:
+        p = _lib.plan_describe(2, N1, N2, C, maps, mode, wt)
+    finally:
+        _lib.check(L.fg_plan_override(2, N1, N2, 0, 0, 0, 0))
+    runs = T1 * -(-N2 // 4)
+    g = -(-N1 // T1)
+    mt = max_threads(2, C, maps, mode)
+    if not p["lean"] & _lib.FG_PLAN_CLUSTER:
+        # no cluster plan: one strip too many threads, or a single strip
+        assert runs > mt or g < 2
+        return
+    assert (p["tiles1"], p["tiles2"], p["K1"], p["K2"], p["T1"], p["T2"]) == (g, 1, 0, 0, T1, N2)
+    assert 2 <= g <= 16 and runs <= p["threads"] <= mt and p["threads"] % 32 == 0
+    assert p["smem"] <= SMEM_LIMIT and p["depth"] in (2, 4, 8)
+    if wt:
+        assert p["S"] in (2, 4, 8)  # the apron rings hold two steps at least
+    if p["threads"] > 512:
+        assert p["lean"] & _lib.FG_PLAN_LEAN
+
+
+def test_cluster_override_validation():
+    L = _lib.load()
+    assert L.fg_plan_override(1, 1, 256, 8, 1, 256, _lib.FG_PLAN_CLUSTER) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_plan_override(2, 64, 64, 1, 8, 64, _lib.FG_PLAN_CLUSTER) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_plan_override(2, 64, 64, 4, 8, 64, 4) == _lib.FG_ERR_INVALID_ARGUMENT

@@ -45,6 +45,20 @@ def test_fewer_tile_candidates_for_concurrent_transforms():
     assert min(tiles(c) for c in conc) <= 52 < min(tiles(c) for c in one)
 
 
+@pytest.mark.parametrize("N1,N2", [(256, 256), (128, 256), (20, 27), (2, 8), (1, 64), (300, 300)])
+def test_cluster_candidates_fit_the_kernel(N1, N2):
+    for lean in (False, True):
+        for S, T1, T2, flags in tune.cluster_candidates(2, N1, N2, lean_capable=lean):
+            assert flags & _lib.FG_PLAN_CLUSTER and T2 == N2
+            g = -(-N1 // T1)
+            threads = T1 * -(-N2 // 4)
+            assert 2 <= g <= 16 and threads <= (1024 if lean else 512)
+            assert bool(flags & _lib.FG_PLAN_LEAN) == (threads > 512)
+    assert tune.cluster_candidates(1, 1, 512) == []
+    if N1 * -(-N2 // 4) > 16 * 1024:
+        assert tune.cluster_candidates(2, N1, N2) == []
+
+
 def test_pass_keys():
     assert tune.pass_keys((5, 7)) == [(1, 1, 7), (1, 1, 5)]
     assert tune.pass_keys((6, 6)) == [(1, 1, 6)]
@@ -120,7 +134,7 @@ def test_autotune_pins_plans_and_keeps_results():
         res = tune.autotune(shape, channels=1, lambs=[0.0, 0.5], iterations=1, repeats=2, max_per_step=4)
         assert set(res) == set(tune.pass_keys(shape))
         for S, T1, T2, lean, ms in res.values():
-            assert ms > 0 and S in (0, 4, 8) and lean in (0, 1)
+            assert ms > 0 and S in (0, 4, 8) and lean in (0, 1, 2, 3)  # flags: lean, cluster
         img, m = _case(shape, 1, 5)
         got = fg.generalised_geodesic3d(torch.from_numpy(img)[None].cuda(), torch.from_numpy(m)[None].cuda(),
                                         [1.0, 1.0, 1.0], 1e10, 0.5, 2)[0].cpu().numpy()
