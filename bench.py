@@ -644,15 +644,26 @@ def run_gpu_arm(args, w, rank, world):
         d_in.append(cache[id(im_np)])
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     tuned = None
-    if args.tune and w.get("method") != "toivanen":  # untimed: plans of the step's transforms run together
+    if args.plans and w.get("method") != "toivanen":
+        # plans tuned by an earlier run (--save-plans): a profiler serialises
+        # the kernels, so plans tuned under it would be tuned for no concurrency
+        from fastgeodis_gb300 import tune
+
+        res = tune.load(args.plans)
+        tuned = {"plans": {",".join(map(str, k)): [int(x) for x in v[:4]] for k, v in res.items()},
+                 "note": f"loaded from {os.path.basename(args.plans)} (--plans)"}
+    elif args.tune and w.get("method") != "toivanen":  # untimed: plans of the step's transforms run together
         from fastgeodis_gb300 import tune
 
         shape = tuple(w["image"].shape[2:])
         t_tune = time.perf_counter()
-        tuned = tune.autotune(shape, channels=int(w["image"].shape[1]), lambs=w["lambs"],
-                              spacing=w.get("spacing", (1.0, 1.0, 1.0)), iterations=1)
-        tuned = {"plans": {",".join(map(str, k)): [v[0], v[1], v[2], v[3]] for k, v in tuned.items()},
-                 "note": "(cross, N1, N2): (S, T1, T2, lean); S = 0 keeps the cost model's plan",
+        res = tune.autotune(shape, channels=int(w["image"].shape[1]), lambs=w["lambs"],
+                            spacing=w.get("spacing", (1.0, 1.0, 1.0)), iterations=1)
+        if args.save_plans and rank == 0:
+            tune.save(res, args.save_plans)
+        tuned = {"plans": {",".join(map(str, k)): [v[0], v[1], v[2], v[3]] for k, v in res.items()},
+                 "note": "(cross, N1, N2): (S, T1, T2, flags: 1 = 64-register kernel, 2 = cluster plan); "
+                         "S = 0 keeps the cost model's plan",
                  "seconds": round(time.perf_counter() - t_tune, 2)}
 
     # the step's transforms are independent: one CUDA stream each, so their
@@ -821,6 +832,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="use the cost model's plans instead of autotuning the workload's shape before warm-up")
+    ap.add_argument("--save-plans", default=None, help="write the autotuned plans to this JSON file")
+    ap.add_argument("--plans", default=None, help="pin plans from this JSON file (from --save-plans) instead of tuning")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run warm-up and timed GPU steps only (no end-to-end or CPU legs): for profiler captures")
     args = ap.parse_args()

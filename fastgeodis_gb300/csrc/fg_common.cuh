@@ -81,6 +81,7 @@ struct LaunchCfg {
   int threads;
   size_t smem;
   bool lean;  // the 64-register kernel (required above 512 threads)
+  int rpt;    // cluster sweep kernel: 4-cell runs per thread (0: the pass kernel)
 };
 
 // Pitch of the shared rings' rows: at least `floats`, a multiple of 4 (float4
@@ -101,6 +102,35 @@ __host__ __device__ constexpr int pass_edge_floats(int cross, int R1, int R2) {
   return cross == 2 ? ring_pitch((R1 + 2) * (((R2 + 3) / 4) + 2) * 2) : 0;
 }
 
+// Shared memory of a cluster sweep CTA (fg_cluster.cuh), a strip of T1 rows
+// of N2 cells: offsets in floats, except `bar` (bytes).  Rows are stored
+// with an apron row above and below (the neighbour strips' boundary rows)
+// and a 4-cell apron left and right, as in the pass kernel.
+struct ClusterLayout {
+  int rpr, B2, rowf, edgef;               // runs per row, floats per ring row, ring and edge-array pitches
+  int dring, iring, dedge, iedge, oring;  // distances [SR][M], image [2][C], their edge arrays, staging [P][M+C][RPT][NT]
+  int otab;                               // own-cell table of the transposed write (int2 per cell)
+  int bar;                                // two mbarriers (bytes)
+  int bytes;
+};
+__host__ __device__ inline ClusterLayout cluster_layout(int C, int M, int SR, int T1, int N2, int NT, int RPT, int P,
+                                                        bool wt) {
+  ClusterLayout l;
+  l.rpr = (N2 + 3) / 4;
+  l.B2 = 4 * l.rpr + 8;
+  l.rowf = ring_pitch((T1 + 2) * l.B2);
+  l.edgef = ring_pitch((T1 + 2) * (l.rpr + 2) * 2);
+  l.dring = 0;
+  l.iring = SR * M * l.rowf;
+  l.dedge = l.iring + 2 * C * l.rowf;
+  l.iedge = l.dedge + SR * M * l.edgef;
+  l.oring = l.iedge + 2 * C * l.edgef;  // every pitch is a multiple of 4 floats: 16-byte aligned
+  l.otab = l.oring + P * (M + C) * RPT * NT * 4;
+  l.bar = (l.otab + (wt ? 2 * T1 * N2 : 0)) * 4;
+  l.bytes = l.bar + 16;
+  return l;
+}
+
 // Shared-memory bytes of a pass kernel for a region of R1 x R2 cells.
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2, int *rowf,
                        int *nown_max, int depth);
@@ -110,8 +140,10 @@ constexpr int max_pass_depth(int nch, int m) { return (nch + m <= 4) ? 8 : 2; }
 // Launchers (one translation unit per cross-section rank).
 int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
-// Volume passes on a cluster plan (fg_pass3d_cluster.cu): c.tiles CTAs in one cluster.
+// Volume passes on a cluster plan (fg_pass3d_cluster.cu): c.tiles CTAs in one
+// cluster; c.rpt > 0 selects the cluster sweep kernel with c.rpt runs per thread.
 int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
+int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
 // in place; spacing_sq = nullptr for images.  bar: 4 counters (16 bytes) of

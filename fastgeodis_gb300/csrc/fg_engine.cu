@@ -187,6 +187,7 @@ struct Plan {
   size_t smem;
   bool lean;     // 64-register kernel
   bool cluster;  // one thread-block cluster of tiles1 strips of whole rows (fg_pass3d_cluster.cu)
+  int rpt;       // cluster plans: runs per thread of the cluster sweep kernel (0: the pass kernel)
 };
 
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
@@ -235,22 +236,36 @@ std::map<std::tuple<int, int, int>, std::tuple<int, int, int, int>> g_overrides;
 // one CTA each, 2 to 16 CTAs in one cluster.  S is the transposed write's
 // flush period (halved until the rings fit; at least 2, the apron rings'
 // depth); the staging depth is the largest that fits one CTA per SM.
-bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1, bool want_lean, Plan *out) {
+// rpt = 2 or 4: the cluster sweep kernel, rpt vertically adjacent runs per
+// thread (T1 rounded up to a multiple of rpt, at most 512 threads, at most
+// one image channel read); rpt = 0: the pass kernel, one run per thread.
+bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1, int rpt, bool want_lean, Plan *out) {
+  const int cimg = mode == MODE_EUCLID ? 0 : C;
+  if (rpt != 0 && (cimg > 1 || (rpt != 2 && rpt != 4))) return false;
+  const int step = std::max(rpt, 1);
   T1 = std::max(1, std::min(T1, N1));
+  T1 = (T1 + step - 1) / step * step;
   const int G = (N1 + T1 - 1) / T1;
   if (G < 2 || G > kMaxCluster) return false;
-  const int cimg = mode == MODE_EUCLID ? 0 : C;
-  const int runs = T1 * ((N2 + 3) / 4);
-  const int nt = std::max(32, (runs + 31) / 32 * 32);
-  if (nt > pass_max_threads(2, cimg, M)) return false;
-  const bool lean = nt > kThreads || (want_lean && pass_lean(2, cimg, M));
+  const int rpr = (N2 + 3) / 4;
+  const int nt = std::max(32, ((T1 + step - 1) / step * rpr + 31) / 32 * 32);
+  if (nt > (rpt ? kThreads : pass_max_threads(2, cimg, M))) return false;
+  const bool lean = rpt == 0 && (nt > kThreads || (want_lean && pass_lean(2, cimg, M)));
   const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
   for (int s2 = wt ? std::max(2, std::min(S, 8)) : 2; s2 >= 2; s2 /= 2) {
     for (int depth = max_pass_depth(nch, M); depth >= 2; depth /= 2) {
       int B2, rowf, nown;
-      const size_t sm = pass_smem_bytes(2, C, M, mode, wt, s2, T1, N2, &B2, &rowf, &nown, depth);
+      size_t sm;
+      if (rpt) {
+        const ClusterLayout ly = cluster_layout(cimg, M, wt ? s2 : 2, T1, N2, nt, rpt, depth, wt);
+        sm = (size_t)ly.bytes;
+        B2 = ly.B2;
+        rowf = ly.rowf;
+      } else {
+        sm = pass_smem_bytes(2, C, M, mode, wt, s2, T1, N2, &B2, &rowf, &nown, depth);
+      }
       if (sm <= kSmemBudget) {
-        *out = Plan{T1, N2, 0, 0, G, 1, wt ? s2 : 8, nt, B2, rowf, depth, sm, lean, true};
+        *out = Plan{T1, N2, 0, 0, G, 1, wt ? s2 : 8, nt, B2, rowf, depth, sm, lean, true, rpt};
         return true;
       }
     }
@@ -312,7 +327,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     // one CTA per SM (shared memory or registers): no room for a concurrent transform
     if (sm > kSmemBudget / 2 || nt > kThreads) cost *= 1.05;
     if (!found || cost < best_cost - 1e-9) {
-      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean, false};
+      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean, false, 0};
       best_cost = cost;
       found = true;
     }
@@ -326,7 +341,8 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   }
   if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
     Plan cp;
-    if (cluster_plan(N1, N2, C, M, mode, wt, ovS, ovT1, (ovLean & FG_PLAN_LEAN) != 0, &cp)) {
+    const int rpt = (ovLean & FG_PLAN_RUNS4) ? 4 : ((ovLean & FG_PLAN_RUNS2) ? 2 : 0);
+    if (cluster_plan(N1, N2, C, M, mode, wt, ovS, ovT1, rpt, (ovLean & FG_PLAN_LEAN) != 0, &cp)) {
       best = cp;
       found = true;
     }
@@ -494,7 +510,7 @@ int profiled_launch(cudaStream_t s, long long vp, int steps, Launch launch) {
 }
 
 int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt, cudaStream_t s) {
-  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean};
+  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean, p.rpt};
   return profiled_launch(s, (long long)a.L * a.N1 * a.N2 * M, a.L, [&] {
     if (p.cluster) return launch_pass_cluster(a, c, M, mode, wt, s);
     return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
@@ -848,7 +864,11 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
   } else {
     if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    if (lean < 0 || lean > (FG_PLAN_LEAN | FG_PLAN_CLUSTER)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
+    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_RUNS4;
+    if (lean < 0 || (lean & ~all) || ((lean & FG_PLAN_RUNS2) && (lean & FG_PLAN_RUNS4)))
+      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
+    if ((lean & (FG_PLAN_RUNS2 | FG_PLAN_RUNS4)) && !(lean & FG_PLAN_CLUSTER))
+      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: runs per thread apply to cluster plans");
     if ((lean & FG_PLAN_CLUSTER) && (cross != 2 || S < 2))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: cluster plans are for volume passes, with S >= 2");
     g_overrides[key] = std::make_tuple(S, T1, T2, lean);
@@ -867,7 +887,8 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
   if (!make_plan(cross, N1, N2, c, maps, mode, transposed_write != 0, std::min(sms, kMaxTiles), &p))
     return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
   const int v[11] = {p.S,  p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem,
-                     (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0)};
+                     (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0) |
+                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0) | (p.rpt == 4 ? FG_PLAN_RUNS4 : 0)};
   for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }

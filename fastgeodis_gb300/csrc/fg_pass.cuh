@@ -488,10 +488,13 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
             const int k = r * 3 + (d2 + 1);  // candidate number 0 .. 3 * NR - 1
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-              float l1 = 0.0f;
+              // one image channel: d = I(x) - I(y); the reference's l_grad * |d|
+              // equals |l_grad * d| bit for bit (round to nearest is symmetric in sign)
+              float d = 0.0f, l1 = 0.0f;
               if (USE_IMG) {
                 if (CT == 1) {
-                  l1 = fabsf(__fsub_rn(f4get(icur[0], i), ip[0][i + 1 + d2]));
+                  d = __fsub_rn(f4get(icur[0], i), ip[0][i + 1 + d2]);
+                  l1 = fabsf(d);
                 } else {
 #pragma unroll
                   for (int c = 0; c < NCH; c++)
@@ -501,7 +504,9 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
 #pragma unroll
               for (int m = 0; m < M; m++) {
                 float cand;
-                if (MODE == MODE_GENERAL)
+                if (MODE == MODE_GENERAL && CT == 1)
+                  cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), fabsf(__fmul_rn(a.lg[m], d)));
+                else if (MODE == MODE_GENERAL)
                   cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], l1));
                 else if (MODE == MODE_EUCLID)
                   cand = __fadd_rn(dp[m][i + 1 + d2], a.e[m][n]);
@@ -681,6 +686,40 @@ inline bool cluster_fits(const void *fn, const cudaLaunchConfig_t &cfg, int dev)
   return ok;
 }
 
+// One cluster of c.tiles CTAs running `fn` (cudaLaunchKernelEx with a cluster
+// dimension).  `configured`: per-device bits of the caller's kernel whose
+// attributes are set (under the engine's launch lock).
+inline int launch_one_cluster(const void *fn, unsigned long long &configured, const PassArgs &a, const LaunchCfg &c,
+                              cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 64 && !(configured & (1ull << dev))) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+    configured |= 1ull << dev;
+  }
+  if (c.tiles < 2 || c.tiles > kMaxCluster) return set_error(FG_ERR_UNSUPPORTED, "a cluster plan has 2 to 16 CTAs");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c.tiles);
+  cfg.blockDim = dim3(c.threads);
+  cfg.dynamicSmemBytes = c.smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = c.tiles;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (!cluster_fits(fn, cfg, dev)) return set_error(FG_ERR_UNSUPPORTED, "the device cannot co-schedule this cluster plan");
+  void *args[] = {const_cast<PassArgs *>(&a)};
+  e = cudaLaunchKernelExC(&cfg, fn, args);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  return FG_OK;
+}
+
 // Launch of one variant.  CLU: the cluster plan (one cluster of c.tiles CTAs);
 // otherwise a cooperative launch of c.tiles CTAs.
 template <int CROSS, int CT, int M, int MODE, bool WT, bool LEAN, bool CLU>
@@ -689,39 +728,20 @@ int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
   if constexpr (CLU) fn = fg_pass_cluster_kernel<CROSS, CT, M, MODE, WT, LEAN>;
   else fn = fg_pass_kernel<CROSS, CT, M, MODE, WT, LEAN>;
   static unsigned long long configured = 0;  // bit per device (set under the engine's launch lock)
+  if constexpr (CLU) return launch_one_cluster((const void *)fn, configured, a, c, s);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 64 && !(configured & (1ull << dev))) {
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e == cudaSuccess && CLU) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
     configured |= 1ull << dev;
   }
   void *args[] = {const_cast<PassArgs *>(&a)};
-  if constexpr (CLU) {
-    if (c.tiles < 2 || c.tiles > kMaxCluster) return set_error(FG_ERR_UNSUPPORTED, "a cluster plan has 2 to 16 CTAs");
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(c.tiles);
-    cfg.blockDim = dim3(c.threads);
-    cfg.dynamicSmemBytes = c.smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = c.tiles;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    if (!cluster_fits(reinterpret_cast<const void *>(fn), cfg, dev))
-      return set_error(FG_ERR_UNSUPPORTED, "the device cannot co-schedule this cluster plan");
-    e = cudaLaunchKernelExC(&cfg, (const void *)fn, args);
-  } else {
-    if (c.tiles > 1)
-      e = cudaLaunchCooperativeKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
-    else
-      e = cudaLaunchKernel((const void *)fn, dim3(1), dim3(c.threads), args, c.smem, s);
-  }
+  if (c.tiles > 1)
+    e = cudaLaunchCooperativeKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
+  else
+    e = cudaLaunchKernel((const void *)fn, dim3(1), dim3(c.threads), args, c.smem, s);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   return FG_OK;
 }

@@ -92,25 +92,32 @@ def candidates(cross: int, N1: int, N2: int, sms: int, steps=(4, 8), max_per_ste
     return out
 
 
-def cluster_candidates(cross: int, N1: int, N2: int, lean_capable: bool = True,
+def cluster_candidates(cross: int, N1: int, N2: int, lean_capable: bool = True, one_channel: bool = True,
                        sizes: Sequence[int] = (16, 12, 8, 6, 4)) -> List[Tuple[int, int, int, int]]:
     """Cluster plans of a volume cross-section: (S, T1, N2, flags) for about
-    `sizes` strips of T1 whole rows, one CTA each (2 to 16 per cluster, one
-    thread per run of 4 cells: at most 1024 threads with the 64-register
-    kernel, 512 without)."""
+    `sizes` strips of T1 whole rows, one CTA each (2 to 16 per cluster).  On
+    the pass kernel a thread owns one run of 4 cells (at most 1024 threads
+    with the 64-register kernel, 512 without); on the cluster sweep kernel
+    (passes that read at most one image channel) 2 or 4 vertically adjacent
+    runs, T1 a multiple of them, at most 512 threads."""
     if cross != 2:
         return []
-    max_threads = THREADS_LEAN if lean_capable else THREADS
     out = []
-    for G in sizes:
-        T1 = _ceil(N1, G)
-        g = _ceil(N1, T1)
-        threads = T1 * _ceil(N2, 4)
-        if g < 2 or g > 16 or threads > max_threads:
+    rpr = _ceil(N2, 4)
+    for rpt, flag in ((1, 0), (2, _lib.FG_PLAN_RUNS2), (4, _lib.FG_PLAN_RUNS4)):
+        if rpt > 1 and not one_channel:
             continue
-        c = (8, T1, N2, _lib.FG_PLAN_CLUSTER | (_lib.FG_PLAN_LEAN if threads > THREADS else 0))
-        if c not in out:
-            out.append(c)
+        max_threads = (THREADS_LEAN if lean_capable else THREADS) if rpt == 1 else THREADS
+        for G in sizes:
+            T1 = _ceil(_ceil(N1, G), rpt) * rpt
+            g = _ceil(N1, T1)
+            threads = (T1 // rpt) * rpr
+            if g < 2 or g > 16 or threads > max_threads:
+                continue
+            lean = _lib.FG_PLAN_LEAN if rpt == 1 and threads > THREADS else 0
+            c = (8, T1, N2, _lib.FG_PLAN_CLUSTER | lean | flag)
+            if c not in out:
+                out.append(c)
     return out
 
 
@@ -210,7 +217,7 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
                     trials.append(c + (1,))  # 64-register kernel: two CTAs per SM
             # cluster plans (one thread-block cluster per transform): they pay
             # off when several transforms share the GPU
-            trials += cluster_candidates(cross, N1, N2, lean_capable=lean)
+            trials += cluster_candidates(cross, N1, N2, lean_capable=lean, one_channel=channels <= 1)
             for c in trials:
                 _lib.check(L.fg_plan_override(cross, N1, N2, *c))
                 try:

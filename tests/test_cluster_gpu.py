@@ -25,17 +25,21 @@ def case(shape, C, seed):
     return img, m
 
 
-def pin_cluster(shape, G, lean=False):
-    """Pins a cluster plan of about G strips on every pass of a volume shape."""
+RUNS = {1: 0, 2: _lib.FG_PLAN_RUNS2, 4: _lib.FG_PLAN_RUNS4}
+
+
+def pin_cluster(shape, G, lean=False, rpt=1, S=4):
+    """Pins a cluster plan of about G strips on every pass of a volume shape
+    (rpt runs per thread: 1 the pass kernel, 2 or 4 the cluster sweep kernel)."""
     L = _lib.load()
     for cross, N1, N2 in tune.pass_keys(shape):
         T1 = -(-N1 // G)
-        flags = _lib.FG_PLAN_CLUSTER | (_lib.FG_PLAN_LEAN if lean else 0)
-        _lib.check(L.fg_plan_override(cross, N1, N2, 4, T1, N2, flags))
+        flags = _lib.FG_PLAN_CLUSTER | (_lib.FG_PLAN_LEAN if lean else 0) | RUNS[rpt]
+        _lib.check(L.fg_plan_override(cross, N1, N2, S, T1, N2, flags))
 
 
-def uses_cluster(shape, C=1, maps=1, mode=0):
-    return all(_lib.plan_describe(*k, C, maps, mode)["lean"] & _lib.FG_PLAN_CLUSTER for k in tune.pass_keys(shape))
+def uses_cluster(shape, C=1, maps=1, mode=0, flag=_lib.FG_PLAN_CLUSTER):
+    return all(_lib.plan_describe(*k, C, maps, mode)["lean"] & flag for k in tune.pass_keys(shape))
 
 
 def t(a):
@@ -114,6 +118,52 @@ def test_concurrent_cluster_transforms():
         torch.cuda.synchronize()
         for lamb, o in zip(lambs, outs):
             assert bits_equal(o[0].cpu().numpy(), oracle.geodesic3d(img, m, sp, 1e10, lamb, 2)), lamb
+        fg.check_status()
+    finally:
+        tune.clear(shape)
+
+
+@pytest.mark.parametrize("shape", [(20, 33, 27), (24, 64, 64), (7, 18, 40), (13, 100, 36)])
+@pytest.mark.parametrize("G", [2, 5, 16])
+@pytest.mark.parametrize("rpt", [2, 4])
+def test_cluster_sweep_kernel_gives_the_oracle_bits(shape, G, rpt):
+    img, m = case(shape, 1, sum(shape) * rpt + G)
+    sp = [1.5, 0.8, 1.1]
+    try:
+        pin_cluster(shape, G, rpt=rpt, S=8)
+        for mode in (0, 1, 2):
+            assert uses_cluster(shape, mode=mode, flag=RUNS[rpt]), mode
+        for lamb in (0.0, 0.6, 1.0):
+            got = fg.generalised_geodesic3d(t(img), t(m), sp, 1e10, lamb, 2)[0].cpu().numpy()
+            want = oracle.geodesic3d(img, m, sp, 1e10, lamb, 2)
+            assert bits_equal(got, want), (shape, G, rpt, lamb, np.abs(got - want).max())
+        fg.check_status()
+    finally:
+        tune.clear(shape)
+
+
+@pytest.mark.parametrize("rpt", [2, 4])
+def test_cluster_sweep_kernel_full_strips_signed_gsf_channels(rpt):
+    shape = (20, 256, 256)
+    img, m = case(shape, 1, 77 + rpt)
+    sp = [1.0, 1.0, 1.0]
+    try:
+        pin_cluster(shape, 16, rpt=rpt, S=8)
+        assert uses_cluster(shape, flag=RUNS[rpt])
+        # two maps: the 20 x 256 sections on the sweep kernel (256 x 256 ones do not fit its rings)
+        assert _lib.plan_describe(2, 20, 256, 1, 2, 0)["lean"] & RUNS[rpt]
+        for lamb in (0.0, 0.5):
+            got = fg.generalised_geodesic3d(t(img), t(m), sp, 1e10, lamb, 1)[0].cpu().numpy()
+            assert bits_equal(got, oracle.geodesic3d(img, m, sp, 1e10, lamb, 1)), lamb
+        m2 = np.random.default_rng(5).random(m.shape).astype(np.float32)
+        got = fg.signed_generalised_geodesic3d(t(img), t(m2), sp, 1e10, 0.5, 1)[0].cpu().numpy()
+        assert bits_equal(got, oracle.signed3d(img, m2, sp, 1e10, 0.5, 1))
+        got = fg.GSF3d(t(img), t(m2), 0.5, sp, 1e10, 1.0, 1)[0].cpu().numpy()
+        assert bits_equal(got, oracle.gsf3d(img, m2, 0.5, sp, 1e10, 1.0, 1))
+        # three image channels: these passes keep a plan of the pass kernel
+        img3, _ = case(shape, 3, 5)
+        got = fg.generalised_geodesic3d(t(img3), t(m), sp, 1e10, 0.5, 1)[0].cpu().numpy()
+        assert bits_equal(got, oracle.geodesic3d(img3, m, sp, 1e10, 0.5, 1))
         fg.check_status()
     finally:
         tune.clear(shape)

@@ -18,6 +18,20 @@ def max_threads(cross, C, maps, mode):
     return 1024 if (cross == 2 and cimg <= 1 and maps == 1) else 512
 
 
+def ring_pitch(f):
+    f = (f + 3) // 4 * 4
+    return f + (36 - f % 32) % 32
+
+
+def cluster_smem(C, M, SR, T1, N2, NT, rpt, depth, wt):
+    """Shared-memory bytes of a cluster sweep CTA (the layout of ClusterLayout)."""
+    rpr = -(-N2 // 4)
+    rowf = ring_pitch((T1 + 2) * (4 * rpr + 8))
+    edgef = ring_pitch((T1 + 2) * (rpr + 2) * 2)
+    floats = (SR * M + 2 * C) * (rowf + edgef) + depth * (M + C) * rpt * NT * 4 + (2 * T1 * N2 if wt else 0)
+    return floats * 4 + 16
+
+
 def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
     S, T1, T2, K1, K2, t1, t2, nt, depth, smem, lean = (p[k] for k in _lib.PLAN_FIELDS)
     assert S in (1, 2, 4, 8) and depth in (2, 4, 8)
@@ -154,3 +168,40 @@ def test_cluster_override_validation():
     assert L.fg_plan_override(1, 1, 256, 8, 1, 256, _lib.FG_PLAN_CLUSTER) == _lib.FG_ERR_INVALID_ARGUMENT
     assert L.fg_plan_override(2, 64, 64, 1, 8, 64, _lib.FG_PLAN_CLUSTER) == _lib.FG_ERR_INVALID_ARGUMENT
     assert L.fg_plan_override(2, 64, 64, 4, 8, 64, 4) == _lib.FG_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("N1,N2", [(256, 256), (128, 256), (20, 27), (100, 64), (9, 100)])
+@pytest.mark.parametrize("C,maps,mode", [(1, 1, 0), (1, 1, 1), (1, 2, 2), (3, 1, 1), (3, 1, 0)])
+@pytest.mark.parametrize("wt", [False, True])
+@pytest.mark.parametrize("rpt,flag", [(2, 4), (4, 8)])
+def test_cluster_sweep_plans(N1, N2, C, maps, mode, wt, rpt, flag):
+    L = _lib.load()
+    G = 16
+    _lib.check(L.fg_plan_override(2, N1, N2, 8, -(-N1 // G), N2, _lib.FG_PLAN_CLUSTER | flag))
+    try:
+        p = _lib.plan_describe(2, N1, N2, C, maps, mode, wt)
+    finally:
+        _lib.check(L.fg_plan_override(2, N1, N2, 0, 0, 0, 0))
+    cimg = 0 if mode == 1 else C
+    T1 = -(-(-(-N1 // G)) // rpt) * rpt
+    g = -(-N1 // T1)
+    threads = T1 // rpt * -(-N2 // 4)
+    nt = -(-threads // 32) * 32
+    fits = any(cluster_smem(cimg, maps, s2 if wt else 2, T1, N2, nt, rpt, 2, wt) <= 227 * 1024 - 1024
+               for s2 in (8, 4, 2))
+    if cimg > 1 or g < 2 or threads > 512 or not fits:
+        assert not p["lean"] & (_lib.FG_PLAN_RUNS2 | _lib.FG_PLAN_RUNS4)  # the planner's own plan
+        return
+    assert p["lean"] == _lib.FG_PLAN_CLUSTER | flag
+    assert (p["tiles1"], p["tiles2"], p["T1"], p["T2"], p["K1"], p["K2"]) == (g, 1, T1, N2, 0, 0)
+    assert threads <= p["threads"] <= 512 and p["threads"] % 32 == 0
+    assert p["smem"] <= SMEM_LIMIT and p["depth"] in (2, 4, 8)
+    S = p["S"] if wt else 2
+    assert p["smem"] == cluster_smem(cimg, maps, S, T1, N2, p["threads"], rpt, p["depth"], wt)
+
+
+def test_runs_flags_validation():
+    L = _lib.load()
+    assert L.fg_plan_override(2, 64, 64, 8, 8, 64, _lib.FG_PLAN_RUNS2) == _lib.FG_ERR_INVALID_ARGUMENT
+    both = _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2 | _lib.FG_PLAN_RUNS4
+    assert L.fg_plan_override(2, 64, 64, 8, 8, 64, both) == _lib.FG_ERR_INVALID_ARGUMENT
