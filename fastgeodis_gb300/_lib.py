@@ -127,7 +127,6 @@ def profile_launch_times():
 FG_PLAN_LEAN = 1      # plan flag: the 64-register kernel
 FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-section
 FG_PLAN_RUNS2 = 4     # plan flag: cluster sweep kernel, 2 runs of 4 cells per thread
-FG_PLAN_RUNS4 = 8     # plan flag: cluster sweep kernel, 4 runs of 4 cells per thread
 # the last field holds the plan flags (FG_PLAN_LEAN | FG_PLAN_CLUSTER)
 PLAN_FIELDS = ("S", "T1", "T2", "K1", "K2", "tiles1", "tiles2", "threads", "depth", "smem", "lean")
 

@@ -8,7 +8,7 @@
 //   * One thread-block cluster of G <= 16 CTAs owns the whole cross-section;
 //     CTA `rank` owns the strip of T1 whole rows starting at rank * T1 (T1 a
 //     multiple of RPT).  No halo, no hand-off through global memory.
-//   * A thread owns the same 4-cell run u of RPT consecutive rows.  The
+//   * A thread owns the same 4-cell run u of RPT (2) consecutive rows.  The
 //     previous step's rows it reads (rows rf-1 .. rf+RPT of the shared ring)
 //     pass through a sliding window of three rows, so RPT runs load RPT + 2
 //     rows instead of 3 * RPT, and the per-step overhead (waits, staging,

@@ -141,7 +141,7 @@ constexpr int max_pass_depth(int nch, int m) { return (nch + m <= 4) ? 8 : 2; }
 int launch_pass_cross1(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 // Volume passes on a cluster plan (fg_pass3d_cluster.cu): c.tiles CTAs in one
-// cluster; c.rpt > 0 selects the cluster sweep kernel with c.rpt runs per thread.
+// cluster; c.rpt = 2 selects the cluster sweep kernel (2 runs per thread).
 int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 

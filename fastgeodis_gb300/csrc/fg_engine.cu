@@ -236,12 +236,12 @@ std::map<std::tuple<int, int, int>, std::tuple<int, int, int, int>> g_overrides;
 // one CTA each, 2 to 16 CTAs in one cluster.  S is the transposed write's
 // flush period (halved until the rings fit; at least 2, the apron rings'
 // depth); the staging depth is the largest that fits one CTA per SM.
-// rpt = 2 or 4: the cluster sweep kernel, rpt vertically adjacent runs per
-// thread (T1 rounded up to a multiple of rpt, at most 512 threads, at most
-// one image channel read); rpt = 0: the pass kernel, one run per thread.
+// rpt = 2: the cluster sweep kernel, 2 vertically adjacent runs per thread
+// (T1 rounded up to an even number, at most 512 threads, at most one image
+// channel read); rpt = 0: the pass kernel, one run per thread.
 bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1, int rpt, bool want_lean, Plan *out) {
   const int cimg = mode == MODE_EUCLID ? 0 : C;
-  if (rpt != 0 && (cimg > 1 || (rpt != 2 && rpt != 4))) return false;
+  if (rpt != 0 && (cimg > 1 || rpt != 2)) return false;
   const int step = std::max(rpt, 1);
   T1 = std::max(1, std::min(T1, N1));
   T1 = (T1 + step - 1) / step * step;
@@ -341,7 +341,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   }
   if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
     Plan cp;
-    const int rpt = (ovLean & FG_PLAN_RUNS4) ? 4 : ((ovLean & FG_PLAN_RUNS2) ? 2 : 0);
+    const int rpt = (ovLean & FG_PLAN_RUNS2) ? 2 : 0;
     if (cluster_plan(N1, N2, C, M, mode, wt, ovS, ovT1, rpt, (ovLean & FG_PLAN_LEAN) != 0, &cp)) {
       best = cp;
       found = true;
@@ -864,10 +864,9 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
   } else {
     if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_RUNS4;
-    if (lean < 0 || (lean & ~all) || ((lean & FG_PLAN_RUNS2) && (lean & FG_PLAN_RUNS4)))
-      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
-    if ((lean & (FG_PLAN_RUNS2 | FG_PLAN_RUNS4)) && !(lean & FG_PLAN_CLUSTER))
+    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2;
+    if (lean < 0 || (lean & ~all)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
+    if ((lean & FG_PLAN_RUNS2) && !(lean & FG_PLAN_CLUSTER))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: runs per thread apply to cluster plans");
     if ((lean & FG_PLAN_CLUSTER) && (cross != 2 || S < 2))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: cluster plans are for volume passes, with S >= 2");
@@ -888,7 +887,7 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
     return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
   const int v[11] = {p.S,  p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem,
                      (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0) |
-                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0) | (p.rpt == 4 ? FG_PLAN_RUNS4 : 0)};
+                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0)};
   for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }

@@ -1,7 +1,7 @@
 // Volume passes on cluster plans: one thread-block cluster owns the whole
 // cross-section and neighbour rows travel through distributed shared memory.
 // Runs per thread 0: the pass kernel's body (one run per thread, up to 1024
-// threads); 2 or 4: the cluster sweep kernel (fg_sweep3d_cluster.cu).
+// threads); 2: the cluster sweep kernel (fg_sweep3d_cluster.cu).
 #include "fg_pass.cuh"
 
 namespace fgi {

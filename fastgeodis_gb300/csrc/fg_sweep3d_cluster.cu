@@ -1,5 +1,5 @@
 // The cluster sweep kernel's variants (fg_cluster.cuh): volume passes that
-// read at most one image channel, 2 or 4 runs of 4 cells per thread.
+// read at most one image channel, 2 runs of 4 cells per thread.
 #include "fg_cluster.cuh"
 
 namespace fgi {
@@ -15,8 +15,7 @@ int launch_sweep(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
 template <int CT, int M, int MODE, bool WT>
 int launch_rpt(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
   if (c.rpt == 2) return launch_sweep<CT, M, MODE, WT, 2>(a, c, s);
-  if (c.rpt == 4) return launch_sweep<CT, M, MODE, WT, 4>(a, c, s);
-  return set_error(FG_ERR_UNSUPPORTED, "a cluster sweep thread owns 2 or 4 runs");
+  return set_error(FG_ERR_UNSUPPORTED, "a cluster sweep thread owns 2 runs");
 }
 
 // one image channel (or none read): images with more channels take the pass

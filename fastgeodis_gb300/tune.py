@@ -98,13 +98,13 @@ def cluster_candidates(cross: int, N1: int, N2: int, lean_capable: bool = True, 
     `sizes` strips of T1 whole rows, one CTA each (2 to 16 per cluster).  On
     the pass kernel a thread owns one run of 4 cells (at most 1024 threads
     with the 64-register kernel, 512 without); on the cluster sweep kernel
-    (passes that read at most one image channel) 2 or 4 vertically adjacent
-    runs, T1 a multiple of them, at most 512 threads."""
+    (passes that read at most one image channel) 2 vertically adjacent runs,
+    T1 even, at most 512 threads."""
     if cross != 2:
         return []
     out = []
     rpr = _ceil(N2, 4)
-    for rpt, flag in ((1, 0), (2, _lib.FG_PLAN_RUNS2), (4, _lib.FG_PLAN_RUNS4)):
+    for rpt, flag in ((1, 0), (2, _lib.FG_PLAN_RUNS2)):
         if rpt > 1 and not one_channel:
             continue
         max_threads = (THREADS_LEAN if lean_capable else THREADS) if rpt == 1 else THREADS

@@ -69,7 +69,6 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 #define FG_PLAN_LEAN 1    /* the 64-register kernel */
 #define FG_PLAN_CLUSTER 2 /* a cluster plan: one thread-block cluster owns the cross-section */
 #define FG_PLAN_RUNS2 4   /* cluster plan on the cluster sweep kernel, 2 runs of 4 cells per thread */
-#define FG_PLAN_RUNS4 8   /* cluster plan on the cluster sweep kernel, 4 runs of 4 cells per thread */
 
 /* Plan override (no counterpart in the reference): for passes whose
  * cross-section is N1 x N2 (cross = 1 for 2D images, N1 = 1; cross = 2 for
@@ -82,10 +81,10 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * 16) of one thread-block cluster each own T1 whole rows, and exchange their
  * boundary rows every step through distributed shared memory, with no halo
  * and no hand-off through global memory; T2 is ignored and S is the
- * transposed write's flush period.  With FG_PLAN_RUNS2 or FG_PLAN_RUNS4 (and
- * at most one image channel read) the strips run on the cluster sweep kernel,
- * each thread owning 2 or 4 vertically adjacent runs (T1 is rounded up to a
- * multiple), at most 512 threads per CTA.  S = 0 removes the override.  Used by the
+ * transposed write's flush period.  With FG_PLAN_RUNS2 (and at most one image
+ * channel read) the strips run on the cluster sweep kernel, each thread
+ * owning 2 vertically adjacent runs (T1 is rounded up to an even number), at
+ * most 512 threads per CTA.  S = 0 removes the override.  Used by the
  * autotuner (fastgeodis_gb300.tune); results do not depend on it.  A plan
  * that does not fit the device falls back to the planner's choice, and a
  * cluster plan that the device cannot co-schedule fails with

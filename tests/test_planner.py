@@ -173,7 +173,7 @@ def test_cluster_override_validation():
 @pytest.mark.parametrize("N1,N2", [(256, 256), (128, 256), (20, 27), (100, 64), (9, 100)])
 @pytest.mark.parametrize("C,maps,mode", [(1, 1, 0), (1, 1, 1), (1, 2, 2), (3, 1, 1), (3, 1, 0)])
 @pytest.mark.parametrize("wt", [False, True])
-@pytest.mark.parametrize("rpt,flag", [(2, 4), (4, 8)])
+@pytest.mark.parametrize("rpt,flag", [(2, 4)])
 def test_cluster_sweep_plans(N1, N2, C, maps, mode, wt, rpt, flag):
     L = _lib.load()
     G = 16
@@ -190,7 +190,7 @@ def test_cluster_sweep_plans(N1, N2, C, maps, mode, wt, rpt, flag):
     fits = any(cluster_smem(cimg, maps, s2 if wt else 2, T1, N2, nt, rpt, 2, wt) <= 227 * 1024 - 1024
                for s2 in (8, 4, 2))
     if cimg > 1 or g < 2 or threads > 512 or not fits:
-        assert not p["lean"] & (_lib.FG_PLAN_RUNS2 | _lib.FG_PLAN_RUNS4)  # the planner's own plan
+        assert not p["lean"] & _lib.FG_PLAN_RUNS2  # the planner's own plan
         return
     assert p["lean"] == _lib.FG_PLAN_CLUSTER | flag
     assert (p["tiles1"], p["tiles2"], p["T1"], p["T2"], p["K1"], p["K2"]) == (g, 1, T1, N2, 0, 0)
@@ -203,5 +203,4 @@ def test_cluster_sweep_plans(N1, N2, C, maps, mode, wt, rpt, flag):
 def test_runs_flags_validation():
     L = _lib.load()
     assert L.fg_plan_override(2, 64, 64, 8, 8, 64, _lib.FG_PLAN_RUNS2) == _lib.FG_ERR_INVALID_ARGUMENT
-    both = _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2 | _lib.FG_PLAN_RUNS4
-    assert L.fg_plan_override(2, 64, 64, 8, 8, 64, both) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_plan_override(2, 64, 64, 8, 8, 64, _lib.FG_PLAN_CLUSTER | 8) == _lib.FG_ERR_INVALID_ARGUMENT

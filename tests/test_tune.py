@@ -50,16 +50,16 @@ def test_cluster_candidates_fit_the_kernel(N1, N2):
     for lean in (False, True):
         for S, T1, T2, flags in tune.cluster_candidates(2, N1, N2, lean_capable=lean):
             assert flags & _lib.FG_PLAN_CLUSTER and T2 == N2
-            rpt = 4 if flags & _lib.FG_PLAN_RUNS4 else (2 if flags & _lib.FG_PLAN_RUNS2 else 1)
+            rpt = 2 if flags & _lib.FG_PLAN_RUNS2 else 1
             assert T1 % rpt == 0
             g = -(-N1 // T1)
             threads = T1 // rpt * -(-N2 // 4)
             assert 2 <= g <= 16 and threads <= (1024 if lean and rpt == 1 else 512)
             assert bool(flags & _lib.FG_PLAN_LEAN) == (threads > 512)
     for c in tune.cluster_candidates(2, N1, N2, one_channel=False):
-        assert not c[3] & (_lib.FG_PLAN_RUNS2 | _lib.FG_PLAN_RUNS4)
+        assert not c[3] & _lib.FG_PLAN_RUNS2
     assert tune.cluster_candidates(1, 1, 512) == []
-    if N1 * -(-N2 // 4) > 16 * 512 * 4:  # 16 CTAs of 512 threads with 4 runs each
+    if N1 * -(-N2 // 4) > 16 * 512 * 2:  # 16 CTAs of 512 threads with 2 runs each
         assert tune.cluster_candidates(2, N1, N2) == []
 
 
