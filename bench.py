@@ -604,6 +604,20 @@ def run_reference_arm(args, w, rank):
     print(json.dumps(line), flush=True)
 
 
+def sweep_kernel_name(w, tuned):
+    """The kernel of the workload's sweep passes: the pinned plans' kind."""
+    if w.get("method") == "toivanen":
+        return "fg_toivanen_kernel"
+    flags = [int(v[3]) for v in (tuned or {}).get("plans", {}).values() if int(v[0]) > 0]
+    from fastgeodis_gb300 import _lib
+
+    if any(f & _lib.FG_PLAN_RUNS2 for f in flags):
+        return "fg_sweep_cluster_kernel"
+    if any(f & _lib.FG_PLAN_CLUSTER for f in flags):
+        return "fg_pass_cluster_kernel"
+    return "fg_pass_kernel"
+
+
 def metric_name(w):
     name = "generalised_geodesic3d" if w["dims"] == 3 else "generalised_geodesic2d"
     return name + ("_toivanen" if w.get("method") == "toivanen" else "") + " throughput"
@@ -803,7 +817,7 @@ def run_gpu_arm(args, w, rank, world):
                    "wall_s_timed_region": round(wall, 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "fg_toivanen_kernel" if w.get("method") == "toivanen" else "fg_pass_kernel",
+                     "kernel": sweep_kernel_name(w, tuned),
                      "avg_launch_ms": round(avg_launch_ms, 5),
                      "alg_bytes_per_launch": int(alg_bytes_launch), "peak_source": peak_kind,
                      "pass_time_share": round(pass_ms / (ms * args.steps), 4),
