@@ -745,6 +745,30 @@ def run_gpu_arm(args, w, rank, world):
         if rank == 0:
             print(json.dumps({"kernels_only": True, "ms_per_step": round(ms, 4), "pass_launches": pass_launches}))
         return
+    graph_batch = None
+    if w.get("images") and w["dims"] == 3 and w.get("method") != "toivanen":
+        # the same batch through the batched API, replayed from one CUDA graph
+        # (the plans pinned above stay in force)
+        b = fg.GeodesicBatch3d([tuple(int(x) for x in im.shape[1:]) for im, _ in d_in], iterations=w["iters"],
+                               use_graph=True, streams=len(d_in), inputs=([im for im, _ in d_in], [mk for _, mk in d_in]),
+                               plans=None, device=dev)
+        b.v, b.lambs, b.spacings = w["v"], list(w["lambs"]), [tuple(w["spacing"])] * len(d_in)
+        for _ in range(args.warmup):
+            b.run()
+        torch.cuda.synchronize()
+        g_ms = []
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.run()
+            e1.record(stream)
+            e1.synchronize()
+            g_ms.append(e0.elapsed_time(e1))
+        b.check()
+        gm = float(np.mean(g_ms))
+        graph_batch = {"api": f"GeodesicBatch3d, {len(d_in)} streams, one CUDA graph per step",
+                       "ms_per_step": round(gm, 4), "value": round(world * vp_step / (gm * 1e-3) / 1e9, 4)}
     # end to end through the public API with host buffers (pinned): every call
     # copies its inputs to the device and returns its result in host memory.
     # The step's calls are independent, so each is issued from its own host
@@ -814,7 +838,8 @@ def run_gpu_arm(args, w, rank, world):
                    "plans": ({"autotuned": tuned} if tuned else
                              "wavefront, no plan" if w.get("method") == "toivanen" else "cost model"),
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)",
-                   "wall_s_timed_region": round(wall, 4)},
+                   "wall_s_timed_region": round(wall, 4),
+                   **({"graph_batch": graph_batch} if graph_batch else {})},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": sweep_kernel_name(w, tuned),

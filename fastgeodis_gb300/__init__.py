@@ -34,6 +34,9 @@ __all__ = [
     "GeodesicBatch2d",
     "generalised_geodesic2d_batch",
     "signed_generalised_geodesic2d_batch",
+    "GeodesicBatch3d",
+    "generalised_geodesic3d_batch",
+    "signed_generalised_geodesic3d_batch",
     "generalised_geodesic2d",
     "generalised_geodesic3d",
     "signed_generalised_geodesic2d",
@@ -326,4 +329,5 @@ def GSF3d_toivanen(image: torch.Tensor, softmask: torch.Tensor, theta: float, sp
 
 
 from .batch import GeodesicBatch2d, generalised_geodesic2d_batch, signed_generalised_geodesic2d_batch  # noqa: E402
+from .batch3d import GeodesicBatch3d, generalised_geodesic3d_batch, signed_generalised_geodesic3d_batch  # noqa: E402
 from .autograd import generalised_geodesic2d_differentiable  # noqa: E402
