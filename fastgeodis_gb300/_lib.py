@@ -27,7 +27,7 @@ FG_OP_GSF = 2
 EXPORTED = (
     "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override", "fg_plan_describe",
     "fg_profile_begin", "fg_profile_end", "fg_profile_launch_times",
-    "fg_workspace_bytes", "fg_workspace_status",
+    "fg_workspace_bytes", "fg_workspace_status", "fg_selftest_wait",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
@@ -75,6 +75,7 @@ def load():
     L.fg_plan_override.restype = i
     L.fg_set_tuning.restype = i
     L.fg_workspace_status.argtypes = [vp, vp]
+    L.fg_selftest_wait.argtypes = [i, vp, sz, vp]
     L.fg_workspace_status.restype = i
     L.fg_generalised_geodesic2d.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp, sz, vp]
     L.fg_signed_generalised_geodesic2d.argtypes = L.fg_generalised_geodesic2d.argtypes

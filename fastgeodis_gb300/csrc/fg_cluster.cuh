@@ -168,14 +168,7 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
     if (t > 0 && waits && !dead) {
       // the neighbour strips' rows of step t-1 have landed in the apron rows
       const unsigned bar = cbar + ((t - 1) & 1) * 8, par = ((t - 1) >> 1) & 1;
-      unsigned spins = 0;
-      while (!mbar_try_wait(bar, par)) {
-        if (++spins > kClusterSpinLimit || ((spins & 255u) == 0 && ld_status(a.status) != 0)) {
-          atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
-          dead = true;  // results are void; later steps no longer wait
-          break;
-        }
-      }
+      if (!wait_phase(bar, par, a.status, kClusterSpinLimit)) dead = true;  // results are void; later steps no longer wait
       if (tid == 0 && !dead && t + 1 <= L - 2) mbar_expect(bar, cl_bytes);  // the same parity's next step
     }
     // this thread's inputs of step t have landed (P - 1 younger groups may still be in flight)

@@ -33,21 +33,12 @@
 #include <tuple>
 
 #include "fg_common.cuh"
+#include "fg_wait.cuh"
 
 namespace fgi {
 
-__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];\n" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
 __device__ __forceinline__ void st_word(unsigned long long *p, unsigned long long v) {
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ int ld_status(const int *p) {
-  int v;
-  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
-  return v;
 }
 // Global loads pinned where they are written (asm volatile), so that the
 // prefetch of step t+P is issued at step t and not moved next to its use.
@@ -95,16 +86,6 @@ __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier
 // one arrival that also expects `tx` bytes of asynchronous stores in this phase
 __device__ __forceinline__ void mbar_expect(unsigned a, unsigned tx) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(tx) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned a, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(a), "r"(parity)
-      : "memory");
-  return ok != 0;
 }
 // stores into another CTA's shared memory that complete on its mbarrier `bar`
 __device__ __forceinline__ void st_async4(unsigned a, const float4 &v, unsigned bar) {
@@ -383,13 +364,8 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
     if (CL && t > 0 && cl_waits) {
       // the neighbour strips' rows of step t-1 have landed in the apron rows
       const unsigned bar = cbar + ((t - 1) & 1) * 8, par = ((t - 1) >> 1) & 1;
-      unsigned spins = 0;
-      while (!cl_dead && !mbar_try_wait(bar, par)) {
-        if (++spins > kClusterSpinLimit || ((spins & 255u) == 0 && ld_status(a.status) != 0)) {
-          atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
-          cl_dead = true;  // results are void; later steps no longer wait
-        }
-      }
+      if (!cl_dead && !wait_phase(bar, par, a.status, kClusterSpinLimit))
+        cl_dead = true;  // results are void; later steps no longer wait
       if (tid == 0 && !cl_dead && t + 1 <= L - 2) mbar_expect(bar, cl_bytes);  // the same parity's next step
     }
     // exact halo values of the previous row from the neighbour tiles
@@ -409,14 +385,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
 #pragma unroll
           for (int i = 0; i < 4; i++)
             if (halo & (1u << i)) {
-              unsigned spins = 0;
-              while ((unsigned)(wd[m][i] >> 32) != want) {
-                if (++spins > kSpinLimit || ((spins & 1023u) == 0 && ld_status(a.status) != 0)) {
-                  atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
-                  break;
-                }
-                wd[m][i] = ld_word(xw + m * xplane + i);
-              }
+              wd[m][i] = wait_word(xw + m * xplane + i, want, wd[m][i], a.status, kSpinLimit);
               const float hv = __uint_as_float((unsigned)wd[m][i]);
               pr[m * rowf + i] = hv;
               // a run's first and last cells also live in its neighbours' edge slots

@@ -32,6 +32,7 @@
 #include <cmath>
 
 #include "fg_common.cuh"
+#include "fg_wait.cuh"
 
 namespace fgi {
 namespace {
@@ -52,17 +53,6 @@ struct ToivArgs {
   int *status;             // FG_ERR_TIMEOUT if a barrier wait expired
 };
 
-__device__ __forceinline__ unsigned toiv_ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ int toiv_ld_status(const int *p) {
-  int v;
-  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
 // Barrier of the `group` CTAs of one map: the n-th call returns once all of
 // them have arrived n times.  Bounded: after kSpinLimit polls (or once another
 // CTA has recorded a timeout) it records FG_ERR_TIMEOUT and returns.
@@ -72,13 +62,7 @@ __device__ __forceinline__ void toiv_group_sync(const ToivArgs &a, unsigned *bar
     arrivals += (unsigned)a.group;
     __threadfence();  // this CTA's cell writes (ordered by the barrier above) before the arrival
     atomicAdd(bar, 1u);
-    unsigned spins = 0;
-    while (toiv_ld_acquire(bar) < arrivals) {
-      if (++spins > kSpinLimit || ((spins & 1023u) == 0 && toiv_ld_status(a.status) != 0)) {
-        atomicCAS(a.status, 0, FG_ERR_TIMEOUT);
-        break;
-      }
-    }
+    wait_count(bar, arrivals, a.status, kSpinLimit);
   }
   __syncthreads();
 }

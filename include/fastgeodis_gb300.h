@@ -119,6 +119,15 @@ FG_API int fg_profile_launch_times(float *ms, int *steps, int cap, int *n);
  * synchronising `stream`: FG_OK, or FG_ERR_TIMEOUT if a kernel gave up. */
 FG_API int fg_workspace_status(void *workspace, void *stream);
 
+/* Self-test of failure detection (no counterpart in the reference): runs the
+ * engine's bounded wait routine on something that never happens -- kind 0
+ * an exchange word nobody publishes, kind 1 an mbarrier phase whose bytes
+ * never arrive, kind 2 a group counter that never reaches its target -- with
+ * a limit well under a second.  The kernel records FG_ERR_TIMEOUT in the
+ * workspace status word (read it with fg_workspace_status) and returns; the
+ * context stays usable.  Uses the first 256 bytes of the workspace. */
+FG_API int fg_selftest_wait(int kind, void *workspace, size_t workspace_bytes, void *stream);
+
 /* Replaces FastGeodis.generalised_geodesic2d
  * (reference: FastGeodis/__init__.py:37-65 -> FastGeodis/fastgeodis.cpp:44-90
  *  -> FastGeodis/fastgeodis_cuda.cu:278-318).
