@@ -292,7 +292,7 @@ __device__ __forceinline__ float sgnf(float d) { return d > 0.0f ? 1.0f : (d < 0
 // the tape holds which term won.  Walking t downwards, the gradient of a cell
 // either stays with Dold (the pass input) or moves to the predecessor
 // D[t-1][x+k] (and to the image through l_grad * |I - I'| of that step).
-template <int NCH>
+template <int NCH, int J>
 __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char *tape, int C, float *sm) {
   const int tid = threadIdx.x, NT = blockDim.x;
   const int H = g.H, W = g.W;
@@ -310,10 +310,45 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
   const float *I = alongW ? g.image_t : g.image;
   float *gI = alongW ? g.gi_t : g.g_image;
   const float lg = g.l_grad;
-  float *gv = sm;                                   // [N] gradient handed to the previous row
-  int *cd = reinterpret_cast<int *>(sm + N);        // [N] tape code of the row
-  float *irow = sm + 2 * N;                         // [NCH][N] image values of the row
-  constexpr int J = 4;                              // cells per thread (N <= 4 * kThreads)
+  // the gradient each cell of a row hands to the previous row and its tape
+  // code, double-buffered by step parity (one barrier per step)
+  float *gvb = sm;                                   // [2][N]
+  int *cdb = reinterpret_cast<int *>(sm + 2 * N);    // [2][N]
+  // J cells per thread, x = tid + j * NT: N <= J * NT (J is chosen from the
+  // batch's widest image, so no thread carries empty cells)
+  auto pos = [&](int t) -> long long { return dir > 0 ? (long long)t : (long long)(L - 1 - t); };
+  // Per cell x = tid + j * NT: the step's inputs, loaded one step ahead so
+  // that no global load sits on a step's critical path.  Image rows are kept
+  // at x-1, x, x+1 (row s of the step and row sp before it); each step loads
+  // one new row, the next step's sp.
+  float go[J], gi[J][NCH], is_[J][NCH][3], isp[J][NCH][3];
+  int cd[J];
+  float go_n[J], gi_n[J][NCH], isp_n[J][NCH][3];
+  int cd_n[J];
+  auto load_row = [&](float (&dst)[J][NCH][3], long long r) {
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const int x = tid + j * NT;
+#pragma unroll
+      for (int c = 0; c < NCH; c++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const int xx = x + q - 1;
+          dst[j][c][q] = (c < C && x < N && xx >= 0 && xx < N) ? I[c * P + r * s_str + xx] : 0.0f;
+        }
+    }
+  };
+  auto load_step = [&](float (&go_)[J], int (&cd_)[J], float (&gi_)[J][NCH], int t) {
+    const long long s = pos(t);
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const int x = tid + j * NT;
+      go_[j] = x < N ? Gout[s * ws_str + x * wc] : 0.0f;
+      cd_[j] = (x < N && t > 0) ? (int)tape[s * s_str + x] : 0;
+#pragma unroll
+      for (int c = 0; c < NCH; c++) gi_[j][c] = (c < C && x < N) ? gI[c * P + s * s_str + x] : 0.0f;
+    }
+  };
   float racc[J], gip[J][NCH];
 #pragma unroll
   for (int j = 0; j < J; j++) {
@@ -321,15 +356,22 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
 #pragma unroll
     for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
   }
-  auto pos = [&](int t) -> long long { return dir > 0 ? (long long)t : (long long)(L - 1 - t); };
+  load_step(go, cd, gi, L - 1);
+  load_row(is_, pos(L - 1));
+  if (L > 1) load_row(isp, pos(L - 2));
   for (int t = L - 1; t >= 0; t--) {
-    const long long s = pos(t), sp = t > 0 ? pos(t - 1) : 0;
+    const long long s = pos(t);
+    // the next step's inputs, in flight during this step
+    if (t > 0) load_step(go_n, cd_n, gi_n, t - 1);
+    if (t > 1) load_row(isp_n, pos(t - 2));
+    float *gv = gvb + (t & 1) * N;
+    int *cdr = cdb + (t & 1) * N;
 #pragma unroll
     for (int j = 0; j < J; j++) {
       const int x = tid + j * NT;
       if (x >= N) continue;
-      const float G = __fadd_rn(Gout[s * ws_str + x * wc], racc[j]);
-      const int code = t > 0 ? (int)tape[s * s_str + x] : 0;
+      const float G = __fadd_rn(go[j], racc[j]);
+      const int code = cd[j];
       float gself[NCH];
 #pragma unroll
       for (int c = 0; c < NCH; c++) gself[c] = 0.0f;
@@ -338,23 +380,20 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
         gv[x] = 0.0f;
       } else {
         Gin[s * s_str + x] = 0.0f;
-        const int xp = x + code - 2;
 #pragma unroll
         for (int c = 0; c < NCH; c++)
           if (c < C) {
-            const float d = __fsub_rn(I[c * P + s * s_str + x], I[c * P + sp * s_str + xp]);
+            // the predecessor x + code - 2 of row sp
+            const float ip = code == 1 ? isp[j][c][0] : (code == 2 ? isp[j][c][1] : isp[j][c][2]);
+            const float d = __fsub_rn(is_[j][c][1], ip);
             gself[c] = __fmul_rn(__fmul_rn(G, lg), sgnf(d));
           }
         gv[x] = G;
       }
-      cd[x] = code;
+      cdr[x] = code;
 #pragma unroll
       for (int c = 0; c < NCH; c++)
-        if (c < C) {
-          const long long o = c * P + s * s_str + x;
-          irow[c * N + x] = I[o];
-          gI[o] = __fadd_rn(gI[o], __fadd_rn(gself[c], gip[j][c]));
-        }
+        if (c < C) gI[c * P + s * s_str + x] = __fadd_rn(gi[j][c], __fadd_rn(gself[c], gip[j][c]));
     }
     __syncthreads();
     if (t > 0) {
@@ -368,20 +407,32 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
 #pragma unroll
         for (int d = -1; d <= 1; d++) {
           const int x = xq - d;  // a cell of row t whose step came from xq
-          if (x < 0 || x >= N || cd[x] != d + 2) continue;
+          if (x < 0 || x >= N || cdr[x] != d + 2) continue;
           const float gx = gv[x];
           racc[j] = __fadd_rn(racc[j], gx);
 #pragma unroll
           for (int c = 0; c < NCH; c++)
             if (c < C) {
-              const float dd = __fsub_rn(irow[c * N + x], I[c * P + sp * s_str + xq]);
+              const float dd = __fsub_rn(is_[j][c][1 - d], isp[j][c][1]);
               gip[j][c] = __fsub_rn(gip[j][c], __fmul_rn(__fmul_rn(gx, lg), sgnf(dd)));
             }
         }
       }
+      // rows and inputs move down one step
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        go[j] = go_n[j];
+        cd[j] = cd_n[j];
+#pragma unroll
+        for (int c = 0; c < NCH; c++) {
+          gi[j][c] = gi_n[j][c];
+#pragma unroll
+          for (int q = 0; q < 3; q++) is_[j][c][q] = isp[j][c][q], isp[j][c][q] = isp_n[j][c][q];
+        }
+      }
     }
-    __syncthreads();
   }
+  __syncthreads();  // the next pass reuses the exchange rows
 }
 
 // Adjoints of the passes pass_hi down to pass_lo (numbered iteration * 4 + k);
@@ -391,7 +442,7 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
 // backward; the memory-saving mode calls it once per pass.
 constexpr int kGradInit = 1, kGradFinal = 2;
 
-template <int NCH>
+template <int NCH, int J>
 __global__ void __launch_bounds__(kThreads, 1)
     fg_grad2d_backward_kernel(const fg_grad2d_item *items, int n, int pass_hi, int pass_lo, int tape_base,
                               int flags, int *counter) {
@@ -416,7 +467,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int k = pi & 3;
         const int L = k >= 2 ? W : H;
         if (L <= 1 && !(k & 1)) continue;  // the forward skipped this pass
-        adjoint_pass<NCH>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
+        adjoint_pass<NCH, J>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
         __threadfence();
         __syncthreads();
       }
@@ -494,8 +545,7 @@ int grad_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int nch = max_C == 1 ? 1 : kMaxChannels;
-  const size_t smem = (size_t)(2 + nch) * max_extent * 4 + 64;
+  const size_t smem = (size_t)4 * max_extent * 4 + 64;  // adjoint_pass: gradient and code rows, two of each
   const int grid = std::max(1, std::min(n, sms));
   auto launch = [&](auto fn) -> int {
     cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -504,7 +554,12 @@ int grad_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
     e2 = cudaGetLastError();
     return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
   };
-  return max_C == 1 ? launch(fg_grad2d_backward_kernel<1>) : launch(fg_grad2d_backward_kernel<kMaxChannels>);
+  // cells per thread: the fewest that cover the widest image's rows and columns
+  if (max_extent <= kThreads)
+    return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 1>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 1>);
+  if (max_extent <= 2 * kThreads)
+    return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 2>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 2>);
+  return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 4>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 4>);
 }
 }  // namespace
 }  // namespace fgi
