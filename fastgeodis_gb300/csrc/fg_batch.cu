@@ -14,6 +14,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "fg_pass.cuh"
 
@@ -435,6 +436,136 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
   __syncthreads();  // the next pass reuses the exchange rows
 }
 
+// Ring of the staged adjoint (adjoint_pass_ring): a step's image row is read
+// again as the previous row of the next step, so a slot is refilled two
+// steps after its own and the loads run kAdjRing - 2 steps ahead.
+constexpr int kAdjRing = 8;
+// floats of one ring slot: upstream gradients, image-gradient row, image row
+// (C channels each where it applies) and the tape row as 4-byte words
+__host__ __device__ inline int adj_slot_floats(int N, int C) { return N * (1 + 2 * C) + (N + 3) / 4; }
+
+// The adjoint of one pass as adjoint_pass, with every global input of a step
+// (upstream gradient and image-gradient rows, image row, tape row) staged
+// into a shared ring by cp.async kAdjRing - 2 steps ahead; same arithmetic,
+// same order, same bits.
+template <int NCH, int J>
+__device__ void adjoint_pass_ring(const fg_grad2d_item &g, int k, const unsigned char *tape, int C, float *sm) {
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const int H = g.H, W = g.W;
+  const long long P = (long long)H * W;
+  const bool alongW = k >= 2;
+  const int dir = (k & 1) ? -1 : 1;
+  const int L = alongW ? W : H, N = alongW ? H : W;
+  const long long s_str = alongW ? H : W;
+  long long ws_str, wc;
+  if (k == 1) ws_str = 1, wc = H;
+  else if (k == 3) ws_str = 1, wc = W;
+  else ws_str = s_str, wc = 1;
+  const float *Gout = (k == 0 || k == 3) ? g.g_r : g.g_t;
+  float *Gin = alongW ? g.g_t : g.g_r;
+  const float *I = alongW ? g.image_t : g.image;
+  float *gI = alongW ? g.gi_t : g.g_image;
+  const float lg = g.l_grad;
+  float *gvb = sm;                                   // [2][N] by step parity
+  int *cdb = reinterpret_cast<int *>(sm + 2 * N);    // [2][N]
+  float *ring = sm + 4 * N;                          // [kAdjRing][slot]
+  const int SLOT = adj_slot_floats(N, C);
+  // tape rows as 4-byte words where every row starts on one
+  const bool tw = N % 4 == 0 && s_str % 4 == 0 && (reinterpret_cast<uintptr_t>(tape) & 3) == 0;
+  auto pos = [&](int t) -> long long { return dir > 0 ? (long long)t : (long long)(L - 1 - t); };
+  auto slot = [&](int t) -> float * { return ring + (t & (kAdjRing - 1)) * SLOT; };
+  auto stage = [&](int u) {  // step u's inputs into its slot: one commit group, possibly empty
+    if (u >= 0) {
+      float *sl = slot(u);
+      const long long s = pos(u);
+      for (int x = tid; x < N; x += NT) {
+        cp_async4(sl + x, Gout + s * ws_str + x * wc);
+        for (int c = 0; c < C; c++) {
+          cp_async4(sl + (1 + c) * N + x, gI + c * P + s * s_str + x);
+          cp_async4(sl + (1 + C + c) * N + x, I + c * P + s * s_str + x);
+        }
+      }
+      if (tw && u > 0)
+        for (int w = tid; w < N / 4; w += NT) cp_async4(sl + (1 + 2 * C) * N + w, tape + s * s_str + 4 * w);
+    }
+    cp_async_commit();
+  };
+  float racc[J], gip[J][NCH];
+#pragma unroll
+  for (int j = 0; j < J; j++) {
+    racc[j] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
+  }
+  for (int u = L - 1; u >= L - (kAdjRing - 2); u--) stage(u);
+  cp_async_wait<kAdjRing - 4>();  // steps L-1 and L-2 have landed
+  __syncthreads();
+  for (int t = L - 1; t >= 0; t--) {
+    const long long s = pos(t);
+    const float *sl = slot(t), *slp = slot(t - 1);
+    float *gv = gvb + (t & 1) * N;
+    int *cdr = cdb + (t & 1) * N;
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const int x = tid + j * NT;
+      if (x >= N) continue;
+      const float G = __fadd_rn(sl[x], racc[j]);
+      const int code = t == 0 ? 0
+                              : (tw ? (int)reinterpret_cast<const unsigned char *>(sl + (1 + 2 * C) * N)[x]
+                                    : (int)tape[s * s_str + x]);
+      float gself[NCH];
+#pragma unroll
+      for (int c = 0; c < NCH; c++) gself[c] = 0.0f;
+      if (code == kTapeSelf) {
+        Gin[s * s_str + x] = G;
+        gv[x] = 0.0f;
+      } else {
+        Gin[s * s_str + x] = 0.0f;
+        const int xp = x + code - 2;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+          if (c < C) {
+            const float d = __fsub_rn(sl[(1 + C + c) * N + x], slp[(1 + C + c) * N + xp]);
+            gself[c] = __fmul_rn(__fmul_rn(G, lg), sgnf(d));
+          }
+        gv[x] = G;
+      }
+      cdr[x] = code;
+#pragma unroll
+      for (int c = 0; c < NCH; c++)
+        if (c < C) gI[c * P + s * s_str + x] = __fadd_rn(sl[(1 + c) * N + x], __fadd_rn(gself[c], gip[j][c]));
+    }
+    cp_async_wait<kAdjRing - 5>();  // step t-2 has landed (read after the barrier)
+    __syncthreads();
+    stage(t + 2 - kAdjRing);         // into the slot of step t+2, whose last reader (step t+1) is done
+    if (t > 0) {
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        const int xq = tid + j * NT;  // cell of row t-1
+        racc[j] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
+        if (xq >= N) continue;
+#pragma unroll
+        for (int d = -1; d <= 1; d++) {
+          const int x = xq - d;  // a cell of row t whose step came from xq
+          if (x < 0 || x >= N || cdr[x] != d + 2) continue;
+          const float gx = gv[x];
+          racc[j] = __fadd_rn(racc[j], gx);
+#pragma unroll
+          for (int c = 0; c < NCH; c++)
+            if (c < C) {
+              const float dd = __fsub_rn(sl[(1 + C + c) * N + x], slp[(1 + C + c) * N + xq]);
+              gip[j][c] = __fsub_rn(gip[j][c], __fmul_rn(__fmul_rn(gx, lg), sgnf(dd)));
+            }
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();  // the next pass reuses the ring and the exchange rows
+}
+
 // Adjoints of the passes pass_hi down to pass_lo (numbered iteration * 4 + k);
 // the tape of pass pi is at (pi - tape_base) * H * W.  kGradInit: the gradient
 // state starts from dLoss/dD; kGradFinal: dLoss/dmask and dLoss/dimage are
@@ -442,7 +573,7 @@ __device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char
 // backward; the memory-saving mode calls it once per pass.
 constexpr int kGradInit = 1, kGradFinal = 2;
 
-template <int NCH, int J>
+template <int NCH, int J, bool RING>
 __global__ void __launch_bounds__(kThreads, 1)
     fg_grad2d_backward_kernel(const fg_grad2d_item *items, int n, int pass_hi, int pass_lo, int tape_base,
                               int flags, int *counter) {
@@ -467,7 +598,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int k = pi & 3;
         const int L = k >= 2 ? W : H;
         if (L <= 1 && !(k & 1)) continue;  // the forward skipped this pass
-        adjoint_pass<NCH, J>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
+        if (RING)
+          adjoint_pass_ring<NCH, J>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
+        else
+          adjoint_pass<NCH, J>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
         __threadfence();
         __syncthreads();
       }
@@ -545,7 +679,11 @@ int grad_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = (size_t)4 * max_extent * 4 + 64;  // adjoint_pass: gradient and code rows, two of each
+  // adjoint_pass: gradient and code rows, two of each; the staged form adds its ring
+  const size_t smem_reg = (size_t)4 * max_extent * 4 + 64;
+  const size_t smem_ring = smem_reg + (size_t)kAdjRing * adj_slot_floats(max_extent, max_C) * 4;
+  const bool ring = smem_ring <= kBatchSmemLimit;
+  const size_t smem = ring ? smem_ring : smem_reg;
   const int grid = std::max(1, std::min(n, sms));
   auto launch = [&](auto fn) -> int {
     cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -554,12 +692,17 @@ int grad_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
     e2 = cudaGetLastError();
     return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
   };
-  // cells per thread: the fewest that cover the widest image's rows and columns
-  if (max_extent <= kThreads)
-    return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 1>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 1>);
-  if (max_extent <= 2 * kThreads)
-    return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 2>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 2>);
-  return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 4>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 4>);
+  // cells per thread: the fewest that cover the widest image's rows and columns;
+  // the staged adjoint where its ring fits shared memory
+  auto by_j = [&](auto ring_tag) -> int {
+    constexpr bool R = decltype(ring_tag)::value;
+    if (max_extent <= kThreads)
+      return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 1, R>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 1, R>);
+    if (max_extent <= 2 * kThreads)
+      return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 2, R>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 2, R>);
+    return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 4, R>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 4, R>);
+  };
+  return ring ? by_j(std::true_type{}) : by_j(std::false_type{});
 }
 }  // namespace
 }  // namespace fgi

@@ -133,3 +133,25 @@ def test_recompute_mode_gives_the_same_bits(iters, C, shape):
     for x, y in zip(res[0], res[1]):
         assert torch.equal(x.view(torch.int32), y.view(torch.int32))
     fg.check_status()
+
+
+def test_wide_multichannel_images_use_the_register_adjoint():
+    # 1400-wide rows with three channels: the staged adjoint's ring does not
+    # fit shared memory, so the backward takes the register-prefetch path
+    torch.manual_seed(9)
+    B, C, H, W = 2, 3, 6, 1400
+    img = (torch.rand(B, C, H, W) * 10).cuda().requires_grad_(True)
+    msk = torch.sigmoid(torch.randn(B, 1, H, W) * 2).cuda().requires_grad_(True)
+    v, lamb, it = 3.0, 0.6, 1
+    d = fg.generalised_geodesic2d_differentiable(img, msk, v, lamb, it)
+    w = torch.rand(B, 1, H, W).cuda()
+    (d * w).sum().backward()
+    for b in range(B):
+        ib = img[b:b + 1].detach().cpu().requires_grad_(True)
+        mb = msk[b:b + 1].detach().cpu().requires_grad_(True)
+        db = torch_scan(ib, mb, v, lamb, it)
+        assert torch.equal(db.detach(), d[b, 0].detach().cpu())
+        (db * w[b, 0].cpu()).sum().backward()
+        torch.testing.assert_close(img.grad[b].cpu(), ib.grad[0], rtol=1e-5, atol=1e-5)
+        torch.testing.assert_close(msk.grad[b].cpu(), mb.grad[0], rtol=1e-5, atol=1e-5)
+    fg.check_status()
