@@ -604,10 +604,18 @@ def run_reference_arm(args, w, rank):
     print(json.dumps(line), flush=True)
 
 
+def _one_launch_side():
+    from fastgeodis_gb300 import _lib
+
+    return _lib.FG_ONE_LAUNCH_SIDE
+
+
 def sweep_kernel_name(w, tuned):
     """The kernel of the workload's sweep passes: the pinned plans' kind."""
     if w.get("method") == "toivanen":
         return "fg_toivanen_kernel"
+    if w["dims"] == 2 and max(w["image"].shape[2:]) <= _one_launch_side():
+        return "fg_batch2d_one_kernel"
     flags = [int(v[3]) for v in (tuned or {}).get("plans", {}).values() if int(v[0]) > 0]
     from fastgeodis_gb300 import _lib
 
@@ -666,7 +674,10 @@ def run_gpu_arm(args, w, rank, world):
         res = tune.load(args.plans)
         tuned = {"plans": {",".join(map(str, k)): [int(x) for x in v[:4]] for k, v in res.items()},
                  "note": f"loaded from {os.path.basename(args.plans)} (--plans)"}
-    elif args.tune and w.get("method") != "toivanen":  # untimed: plans of the step's transforms run together
+    elif (args.tune and w.get("method") != "toivanen"
+          and not (w["dims"] == 2 and max(w["image"].shape[2:]) <= _lib.FG_ONE_LAUNCH_SIDE)):
+        # untimed: plans of the step's transforms run together (small images
+        # run in one launch and have no pass plans to tune)
         from fastgeodis_gb300 import tune
 
         shape = tuple(w["image"].shape[2:])

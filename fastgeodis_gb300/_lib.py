@@ -125,6 +125,7 @@ def profile_launch_times():
     return [(float(ms[i]), int(st[i])) for i in range(n.value)]
 
 
+FG_ONE_LAUNCH_SIDE = 512  # plain / signed 2D transforms of images up to this side run in one launch
 FG_PLAN_LEAN = 1      # plan flag: the 64-register kernel
 FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-section
 FG_PLAN_RUNS2 = 4     # plan flag: cluster sweep kernel, 2 runs of 4 cells per thread

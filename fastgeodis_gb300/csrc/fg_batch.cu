@@ -102,6 +102,39 @@ __device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, 
   *pa = a;
 }
 
+// One image's whole transform by one CTA: initial distances and the image
+// transpose, `iterations` x 4 passes, and the signed difference.
+template <int CT, int M>
+__device__ __forceinline__ void batch_item(const fg_batch2d_item &it, int iterations, int S, float r2, int *status,
+                                           float *sm, PassArgs &s_args) {
+  if ((long long)it.H * it.W > 0) {
+    batch_prologue(it, M == 2, sm);
+    __threadfence();
+    __syncthreads();
+    for (int iter = 0; iter < iterations; iter++) {
+      for (int k = 0; k < 4; k++) {
+        const int L = k >= 2 ? it.W : it.H;
+        const bool wt = k & 1;
+        if (L <= 1 && !wt) continue;
+        if (threadIdx.x == 0)
+          batch_pass_args(it, M, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), M), r2, status, &s_args);
+        __syncthreads();
+        if (wt)
+          pass_body<1, CT, M, MODE_GENERAL, true, false, false>(s_args, 0, sm);
+        else
+          pass_body<1, CT, M, MODE_GENERAL, false, false, false>(s_args, 0, sm);
+        __threadfence();
+        __syncthreads();
+      }
+    }
+    if (M == 2) {
+      const long long P = (long long)it.H * it.W;
+      for (long long p = threadIdx.x; p < P; p += blockDim.x) it.out[p] = __fsub_rn(it.out[p], it.d2[p]);
+    }
+  }
+  __syncthreads();
+}
+
 template <int CT, int M>
 __global__ void __launch_bounds__(kThreads, 1)
     fg_batch2d_kernel(const fg_batch2d_item *items, int n, int iterations, int S, float r2, int *counter,
@@ -114,34 +147,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     const int i = s_item;
     if (i >= n) break;
-    const fg_batch2d_item it = items[i];
-    if ((long long)it.H * it.W > 0) {
-      batch_prologue(it, M == 2, sm);
-      __threadfence();
-      __syncthreads();
-      for (int iter = 0; iter < iterations; iter++) {
-        for (int k = 0; k < 4; k++) {
-          const int L = k >= 2 ? it.W : it.H;
-          const bool wt = k & 1;
-          if (L <= 1 && !wt) continue;
-          if (threadIdx.x == 0)
-            batch_pass_args(it, M, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), M), r2, status, &s_args);
-          __syncthreads();
-          if (wt)
-            pass_body<1, CT, M, MODE_GENERAL, true, false, false>(s_args, 0, sm);
-          else
-            pass_body<1, CT, M, MODE_GENERAL, false, false, false>(s_args, 0, sm);
-          __threadfence();
-          __syncthreads();
-        }
-      }
-      if (M == 2) {
-        const long long P = (long long)it.H * it.W;
-        for (long long p = threadIdx.x; p < P; p += blockDim.x) it.out[p] = __fsub_rn(it.out[p], it.d2[p]);
-      }
-    }
-    __syncthreads();
+    batch_item<CT, M>(items[i], iterations, S, r2, status, sm, s_args);
   }
+}
+
+// One image (the descriptor as a kernel parameter): the single-call form.
+template <int CT, int M>
+__global__ void __launch_bounds__(kThreads, 1)
+    fg_batch2d_one_kernel(const fg_batch2d_item it, int iterations, int S, float r2, int *status) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ PassArgs s_args;
+  batch_item<CT, M>(it, iterations, S, r2, status, sm, s_args);
 }
 
 template <int CT, int M>
@@ -180,6 +196,27 @@ int batch_flush_steps(int max_C, int max_extent, int is_signed) {
   return batch_smem(max_C, max_extent, is_signed, 8) <= kBatchSmemLimit ? 8 : 4;
 }
 }  // namespace
+}  // namespace fgi
+
+namespace fgi {
+int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, int *status, cudaStream_t s) {
+  const int ext = std::max(it.H, it.W);
+  if (it.C < 1 || it.C > kMaxChannels || ext > 4 * kThreads)
+    return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: 1 to 4 channels, sides up to 2048");
+  const int S = batch_flush_steps(it.C, ext, is_signed);
+  const size_t smem = batch_smem(it.C, ext, is_signed, S);
+  if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: shared memory");
+  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
+  auto launch = [&](auto fn) -> int {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+    fn<<<1, kThreads, smem, s>>>(it, std::max(iterations, 0), S, r2, status);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  };
+  if (it.C == 1) return is_signed ? launch(fg_batch2d_one_kernel<1, 2>) : launch(fg_batch2d_one_kernel<1, 1>);
+  return is_signed ? launch(fg_batch2d_one_kernel<0, 2>) : launch(fg_batch2d_one_kernel<0, 1>);
+}
 }  // namespace fgi
 
 extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed) {

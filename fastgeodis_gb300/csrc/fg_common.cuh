@@ -145,6 +145,12 @@ int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, b
 int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 
+// A whole 2D transform (plain, or signed) of one image by one CTA in one
+// launch (fg_batch.cu, the batched kernel's per-image body): initial
+// distances, the image transpose, every pass and the signed difference.
+int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, int *status, cudaStream_t s);
+constexpr int kOneLaunchSide = FG_ONE_LAUNCH_SIDE;  // images up to this side (measured faster than per-pass launches)
+
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
 // in place; spacing_sq = nullptr for images.  bar: 4 counters (16 bytes) of
 // scratch the launch clears, status: the workspace status word.

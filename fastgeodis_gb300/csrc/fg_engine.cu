@@ -722,6 +722,20 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
     fg_unswept_kernel<<<ew_grid(n), 256, 0, s>>>(out + P, mask + P, n, v, theta, op);
     FG_CUDA(cudaGetLastError());
   }
+  if (!g.is3d && !toivanen && op != FG_OP_GSF && std::max(g.H, g.W) <= kOneLaunchSide) {
+    // small images: the whole transform in one launch (its CTA runs the passes
+    // back to back), with the workspace's buffers as scratch
+    fg_batch2d_item it{};
+    it.image = image, it.mask = mask, it.out = out, it.image_t = img_t;
+    it.t1 = xt[0];
+    it.d2 = op == FG_OP_SIGNED ? xr[0] : nullptr;
+    it.t2 = op == FG_OP_SIGNED ? xt[1] : nullptr;
+    it.C = g.C, it.H = g.H, it.W = g.W;
+    it.v = v, it.l_grad = lg, it.l_eucl = le;
+    const int M = op == FG_OP_SIGNED ? 2 : 1;
+    return profiled_launch(s, 4LL * std::max(iterations, 0) * P * M, 2 * std::max(iterations, 0) * (g.H + g.W),
+                           [&] { return launch_image_one(it, op == FG_OP_SIGNED, iterations, w.status, s); });
+  }
   if (iterations > 0 && !toivanen) {
     dim3 tg((g.W + 31) / 32, (g.H + 31) / 32, g.C * g.D);
     fg_transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(image, img_t, g.D, g.H, g.W);

@@ -128,6 +128,11 @@ FG_API int fg_workspace_status(void *workspace, void *stream);
  * context stays usable.  Uses the first 256 bytes of the workspace. */
 FG_API int fg_selftest_wait(int kind, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Images whose sides are all at most this run their whole plain or signed
+ * transform in one launch (one CTA: initial distances, transpose, every pass);
+ * larger ones run one launch per pass on the planned tiles. */
+#define FG_ONE_LAUNCH_SIDE 512
+
 /* Replaces FastGeodis.generalised_geodesic2d
  * (reference: FastGeodis/__init__.py:37-65 -> FastGeodis/fastgeodis.cpp:44-90
  *  -> FastGeodis/fastgeodis_cuda.cu:278-318).
