@@ -847,7 +847,9 @@ def run_gpu_arm(args, w, rank, world):
         "config": {"workload": w["desc"], "parallelism": f"replicas x{world}",
                    "streams": f"{len(w['lambs'])} transforms per step on {len(w['lambs'])} CUDA streams",
                    "plans": ({"autotuned": tuned} if tuned else
-                             "wavefront, no plan" if w.get("method") == "toivanen" else "cost model"),
+                             "wavefront, no plan" if w.get("method") == "toivanen" else
+                             "the whole transform in one launch, no pass plans"
+                             if sweep_kernel_name(w, None) == "fg_batch2d_one_kernel" else "cost model"),
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)",
                    "wall_s_timed_region": round(wall, 4),
                    **({"graph_batch": graph_batch} if graph_batch else {})},
