@@ -9,7 +9,9 @@
 // ever waits for another, so any number of images and any grid size is safe,
 // and the launch can be captured in a CUDA graph (memset of the counter +
 // one kernel).  Each image's arithmetic is exactly that of the per-call path:
-// results are bit-identical, alone or in a batch.
+// results are bit-identical, alone or in a batch.  The per-call path itself
+// runs small images (sides up to FG_ONE_LAUNCH_SIDE) through the same
+// per-image body in a one-CTA launch (fg_batch2d_one_kernel).
 
 #include <math.h>
 

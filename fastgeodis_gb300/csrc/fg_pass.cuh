@@ -19,6 +19,11 @@
 //     that row by the words of its neighbours, re-polling (bounded) only words
 //     that do not yet carry the wanted epoch.  One L2 round trip per hand-off,
 //     no fences, no flags.  Halo cells are never written back.
+//   * Cluster plans (volumes, CL = true): one thread-block cluster owns the
+//     whole cross-section as strips of whole rows and the strips exchange
+//     their boundary rows every step through distributed shared memory (see
+//     pass_body); fg_cluster.cuh holds the cluster sweep kernel, which runs
+//     the same plans with two runs per thread.
 //   * Layout: the swept axis is never the contiguous one in the read layout.
 //     The pass that hands over to a sweep along the contiguous axis writes
 //     its result transposed (step innermost), through an S-row shared ring
