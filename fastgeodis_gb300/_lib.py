@@ -27,7 +27,7 @@ FG_OP_GSF = 2
 EXPORTED = (
     "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override", "fg_plan_describe",
     "fg_profile_begin", "fg_profile_end", "fg_profile_launch_times",
-    "fg_workspace_bytes", "fg_workspace_status", "fg_selftest_wait",
+    "fg_workspace_bytes", "fg_workspace_status", "fg_selftest_wait", "fg_cluster_capacity",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
@@ -76,6 +76,7 @@ def load():
     L.fg_set_tuning.restype = i
     L.fg_workspace_status.argtypes = [vp, vp]
     L.fg_selftest_wait.argtypes = [i, vp, sz, vp]
+    L.fg_cluster_capacity.argtypes = [i, i, sz, ctypes.POINTER(ctypes.c_int)]
     L.fg_workspace_status.restype = i
     L.fg_generalised_geodesic2d.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp, sz, vp]
     L.fg_signed_generalised_geodesic2d.argtypes = L.fg_generalised_geodesic2d.argtypes
@@ -138,6 +139,13 @@ def plan_describe(cross, N1, N2, C=1, maps=1, mode=0, transposed_write=False, sm
     out = (ctypes.c_int * len(PLAN_FIELDS))()
     check(load().fg_plan_describe(cross, N1, N2, C, maps, mode, int(transposed_write), sms, out))
     return dict(zip(PLAN_FIELDS, list(out)))
+
+
+def cluster_capacity(cluster_size: int, threads: int, smem: int) -> int:
+    """Clusters of this shape of the cluster sweep kernel the current device runs at once."""
+    n = ctypes.c_int()
+    check(load().fg_cluster_capacity(cluster_size, threads, smem, ctypes.byref(n)))
+    return n.value
 
 
 def last_error() -> str:

@@ -144,6 +144,7 @@ int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, b
 // cluster; c.rpt = 2 selects the cluster sweep kernel (2 runs per thread).
 int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
+int cluster_capacity(int size, int threads, size_t smem, int *out);
 
 // A whole 2D transform (plain, or signed) of one image by one CTA in one
 // launch (fg_batch.cu, the batched kernel's per-image body): initial

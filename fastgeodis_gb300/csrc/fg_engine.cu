@@ -906,6 +906,12 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
   return FG_OK;
 }
 
+int fg_cluster_capacity(int cluster_size, int threads, size_t smem, int *clusters) {
+  if (cluster_size < 1 || cluster_size > kMaxCluster || threads < 32 || threads > kThreads || !clusters)
+    return fail(FG_ERR_INVALID_ARGUMENT, "cluster capacity: bad arguments");
+  return cluster_capacity(cluster_size, threads, smem, clusters);
+}
+
 int fg_set_tuning(int max_region_cells, int max_tiles) {
   if (max_region_cells < 0 || max_region_cells > kMaxRegion || max_tiles < 0 || max_tiles > kMaxTiles)
     return fail(FG_ERR_INVALID_ARGUMENT, "tuning values out of range");

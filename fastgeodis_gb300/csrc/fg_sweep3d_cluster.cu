@@ -30,6 +30,34 @@ int launch_sweep_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStrea
 
 }  // namespace
 
+// How many clusters of `size` CTAs (threads, smem each) of the cluster sweep
+// kernel the current device co-schedules (cudaOccupancyMaxActiveClusters).
+int cluster_capacity(int size, int threads, size_t smem, int *out) {
+  const void *fn = (const void *)fg_sweep_cluster_kernel<1, 1, MODE_GENERAL, false, 2>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(size);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = size;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  e = cudaOccupancyMaxActiveClusters(&n, fn, &cfg);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  }
+  *out = n;
+  return FG_OK;
+}
+
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
   if (M == 1) return wt ? launch_sweep_mode<1, true>(a, c, mode, s) : launch_sweep_mode<1, false>(a, c, mode, s);
   if (M == 2) return wt ? launch_sweep_mode<2, true>(a, c, mode, s) : launch_sweep_mode<2, false>(a, c, mode, s);

@@ -91,6 +91,12 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * FG_ERR_UNSUPPORTED at launch. */
 FG_API int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean);
 
+/* How many clusters of `cluster_size` CTAs (2-16) of `threads` threads and
+ * `smem` bytes of dynamic shared memory each the current device runs at once
+ * (cudaOccupancyMaxActiveClusters for the cluster sweep kernel): the
+ * concurrency of cluster plans (no counterpart in the reference). */
+FG_API int fg_cluster_capacity(int cluster_size, int threads, size_t smem, int *clusters);
+
 /* The plan the engine uses for one pass (no counterpart in the reference):
  * cross-section rank `cross` (1: a 2D row, 2: a 3D plane) of N1 x N2 cells,
  * C image channels, `maps` distance maps (1 or 2), arithmetic mode (0

@@ -167,3 +167,11 @@ def test_cluster_sweep_kernel_full_strips_signed_gsf_channels(rpt):
         fg.check_status()
     finally:
         tune.clear(shape)
+
+
+def test_cluster_capacity_matches_what_runs():
+    # 16-CTA clusters of the b256 plan: the device runs at least one, at most 152 / 16
+    n = _lib.cluster_capacity(16, 512, 188 * 1024)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert 1 <= n <= sms // 16
+    assert _lib.cluster_capacity(2, 512, 188 * 1024) >= n

@@ -204,3 +204,13 @@ def test_runs_flags_validation():
     L = _lib.load()
     assert L.fg_plan_override(2, 64, 64, 8, 8, 64, _lib.FG_PLAN_RUNS2) == _lib.FG_ERR_INVALID_ARGUMENT
     assert L.fg_plan_override(2, 64, 64, 8, 8, 64, _lib.FG_PLAN_CLUSTER | 8) == _lib.FG_ERR_INVALID_ARGUMENT
+
+
+def test_cluster_capacity_arguments():
+    import ctypes
+    L = _lib.load()
+    n = ctypes.c_int()
+    assert L.fg_cluster_capacity(0, 512, 1024, ctypes.byref(n)) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_cluster_capacity(17, 512, 1024, ctypes.byref(n)) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_cluster_capacity(16, 1024, 1024, ctypes.byref(n)) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_cluster_capacity(16, 512, 1024, None) == _lib.FG_ERR_INVALID_ARGUMENT
