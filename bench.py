@@ -205,6 +205,12 @@ def run_batch_arm(args, rank, world):
     d2h = 2 * sum(o.numel() * 4 for o in plans[0].outputs)
     if rank != 0:
         return
+    i0 = min(range(len(items)), key=lambda i: shapes[i][1] * shapes[i][2])  # the smallest image of the batch
+    batched()
+    torch.cuda.synchronize()
+    f64 = fp64_check(plans[0].outputs[i0][0].cpu().numpy(), items[i0][0][0].cpu().numpy(),
+                     items[i0][1][0].cpu().numpy(), 1e10, items[i0][2], 2)
+    f64["image"] = "the smallest of the batch, plain transform"
     line = {
         "metric": "generalised_geodesic2d uneven batch throughput", "value": round(vp / ms_b / 1e6, 4),
         "unit": "Gvoxel-passes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -215,7 +221,8 @@ def run_batch_arm(args, rank, world):
                    "path": "GeodesicBatch2d (one persistent launch per variant, CUDA graph)",
                    "per_call_value": round(vp / ms_p / 1e6, 4), "per_call_ms_per_step": round(ms_p, 3),
                    "speedup_vs_per_call": round(ms_p / ms_b, 2),
-                   "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)"},
+                   "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)",
+                   "fp64_check": f64},
         "e2e": {"value": round(vp / e2e_s / 1e9, 4), "unit": "Gvoxel-passes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "clocks": clk, "gpu_launches": 2,
@@ -486,6 +493,24 @@ class ClockSampler:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def fp64_check(got, image, mask, v, lamb, iters, spacing=None):
+    """Error of one float32 transform against the oracle's float64 scan of
+    the same inputs (the same raster scan in double precision)."""
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    if spacing is None:
+        ref = oracle.geodesic2d_f64(image, mask, v, lamb, iters)
+    else:
+        ref = oracle.geodesic3d_f64(image, mask, spacing, v, lamb, iters)
+    got = np.asarray(got, np.float64)
+    err = np.abs(got - ref)
+    rel = err / np.maximum(np.abs(ref), 1e-30)
+    return {"lamb": lamb, "max_abs_err": float(err.max()), "max_rel_err": float(rel.max()),
+            "within_1e-5_rel_1e-4_abs": bool(np.all(err <= 1e-4 + 1e-5 * np.abs(ref))),
+            "reference": "oracle float64 scan of the same inputs", "seconds": round(time.perf_counter() - t0, 2)}
 
 
 def measured_peak_hbm():
@@ -839,6 +864,16 @@ def run_gpu_arm(args, w, rank, world):
     traffic = committed_traffic(w["name"])
     init_launches = n_calls * args.steps  # v*mask initialisation, one per transform
     cpu_val, cpu_kind, cpu_cores, cpu_sample = time_cpu_sample(w, "port", budget_s=args.cpu_budget)
+    f64 = None
+    if w.get("method") != "toivanen":
+        # the transform of the step with the middle lamb, against the float64 scan
+        k = len(w["lambs"]) // 2
+        im, mk = d_in[k]
+        lamb = w["lambs"][k]
+        out = (f3(im, mk, w["spacing"], w["v"], lamb, w["iters"]) if w["dims"] == 3
+               else f2(im, mk, w["v"], lamb, w["iters"]))
+        f64 = fp64_check(out[0].cpu().numpy(), im[0].cpu().numpy(), mk[0].cpu().numpy(), w["v"], lamb, w["iters"],
+                         spacing=w["spacing"] if w["dims"] == 3 else None)
     line = {
         "metric": metric_name(w), "value": round(value, 4), "unit": "Gvoxel-passes/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -852,7 +887,8 @@ def run_gpu_arm(args, w, rank, world):
                              if sweep_kernel_name(w, None) == "fg_batch2d_one_kernel" else "cost model"),
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)",
                    "wall_s_timed_region": round(wall, 4),
-                   **({"graph_batch": graph_batch} if graph_batch else {})},
+                   **({"graph_batch": graph_batch} if graph_batch else {}),
+                   **({"fp64_check": f64} if f64 else {})},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": sweep_kernel_name(w, tuned),
