@@ -227,6 +227,11 @@ double cone_avg_runs(int cross, int R1, int R2, int K1, int K2, int S) {
   return sum / S;
 }
 
+// Whether an image of H x W takes the one-launch path (launch_image_one):
+// small enough, and no plan pinned or planner limit set for its passes (so
+// that fg_plan_override and fg_set_tuning still reach the pass kernel).
+bool one_launch_image(int H, int W);
+
 // Plan overrides set by the autotuner (fg_plan_override): cross-section shape
 // -> (S, T1, T2, flags); flags: FG_PLAN_LEAN, FG_PLAN_CLUSTER.
 std::mutex g_override_mu;
@@ -273,6 +278,13 @@ bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1
   return false;
 }
 std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older cache entries are stale
+
+bool one_launch_image(int H, int W) {
+  if (std::max(H, W) > kOneLaunchSide || g_tune_region.load() < kMaxRegion || g_tune_tiles.load() > 0) return false;
+  std::lock_guard<std::mutex> g(g_override_mu);
+  return g_overrides.find(std::make_tuple(1, 1, W)) == g_overrides.end() &&
+         g_overrides.find(std::make_tuple(1, 1, H)) == g_overrides.end();
+}
 
 bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int max_tiles, Plan *out) {
   static std::mutex mu;
@@ -722,7 +734,7 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
     fg_unswept_kernel<<<ew_grid(n), 256, 0, s>>>(out + P, mask + P, n, v, theta, op);
     FG_CUDA(cudaGetLastError());
   }
-  if (!g.is3d && !toivanen && op != FG_OP_GSF && std::max(g.H, g.W) <= kOneLaunchSide) {
+  if (!g.is3d && !toivanen && op != FG_OP_GSF && one_launch_image(g.H, g.W)) {
     // small images: the whole transform in one launch (its CTA runs the passes
     // back to back), with the workspace's buffers as scratch
     fg_batch2d_item it{};

@@ -136,7 +136,9 @@ FG_API int fg_selftest_wait(int kind, void *workspace, size_t workspace_bytes, v
 
 /* Images whose sides are all at most this run their whole plain or signed
  * transform in one launch (one CTA: initial distances, transpose, every pass);
- * larger ones run one launch per pass on the planned tiles. */
+ * larger ones, and any image whose passes have a pinned plan
+ * (fg_plan_override) or planner limits (fg_set_tuning), run one launch per
+ * pass on the planned tiles. */
 #define FG_ONE_LAUNCH_SIDE 512
 
 /* Replaces FastGeodis.generalised_geodesic2d

@@ -252,3 +252,39 @@ def test_float64_error_report_2d():
     got = fg.generalised_geodesic2d(t(img), t(m), 1e10, 1.0, 2)[0].cpu().numpy().astype(np.float64)
     ref64 = oracle.geodesic2d_f64(img, m, 1e10, 1.0, 2)
     np.testing.assert_allclose(got, ref64, rtol=1e-5, atol=1e-4)
+
+
+def test_small_images_run_in_one_launch_unless_plans_are_pinned():
+    L = _lib.load()
+    rng = np.random.default_rng(21)
+    img = rng.random((1, 64, 96)).astype(np.float32)
+    m = np.ones((1, 64, 96), np.float32)
+    m[0, 10, 20] = 0
+    ti, tm = t(img), t(m)
+    want = oracle.geodesic2d(img, m, 1e10, 0.5, 2)
+
+    def launches(fn):
+        torch.cuda.synchronize()
+        _lib.profile_begin()
+        out = fn()
+        torch.cuda.synchronize()
+        _, n, _ = _lib.profile_end()
+        return n, out
+
+    n, out = launches(lambda: fg.generalised_geodesic2d(ti, tm, 1e10, 0.5, 2))
+    assert n == 1 and bits_equal(out[0].cpu().numpy(), want)  # the whole transform in one launch
+    n, out = launches(lambda: fg.signed_generalised_geodesic2d(ti, tm, 1e10, 0.5, 2))
+    assert n == 1
+    _lib.check(L.fg_plan_override(1, 1, 96, 8, 1, 96, 0))  # a pinned plan: one launch per pass
+    try:
+        n, out = launches(lambda: fg.generalised_geodesic2d(ti, tm, 1e10, 0.5, 2))
+        assert n == 8 and bits_equal(out[0].cpu().numpy(), want)
+    finally:
+        _lib.check(L.fg_plan_override(1, 1, 96, 0, 0, 0, 0))
+    _lib.check(L.fg_set_tuning(64, 0))  # planner limits: one launch per pass too
+    try:
+        n, out = launches(lambda: fg.generalised_geodesic2d(ti, tm, 1e10, 0.5, 2))
+        assert n == 8 and bits_equal(out[0].cpu().numpy(), want)
+    finally:
+        _lib.check(L.fg_set_tuning(0, 0))
+    fg.check_status()
