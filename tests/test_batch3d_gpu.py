@@ -86,3 +86,21 @@ def test_functional_batch_api():
         assert torch.equal(outs[i], want)
         want = fg.signed_generalised_geodesic3d(imgs[i], msks[i], [1.0, 1.0, 1.0], 1e10, 0.5, 2)
         assert torch.equal(souts[i], want)
+
+
+def test_batch_with_tuned_plans():
+    shapes = [(1, 12, 40, 48)] * 3 + [(1, 8, 24, 32)]
+    vols = [volume(s, 70 + i) for i, s in enumerate(shapes)]
+    b = fg.GeodesicBatch3d(shapes, iterations=1, use_graph=True, streams=4, plans="tune")
+    try:
+        for i, (img, m) in enumerate(vols):
+            b.images[i].copy_(torch.from_numpy(img))
+            b.masks[i].copy_(torch.from_numpy(m))
+        b.lambs = [0.0, 0.5, 1.0, 0.7]
+        outs = [o.clone() for o in b.run()]
+        b.check()
+        for i, (img, m) in enumerate(vols):
+            assert bits_equal(outs[i][0].cpu().numpy(), oracle.geodesic3d(img[0], m[0], [1.0, 1.0, 1.0], 1e10,
+                                                                         b.lambs[i], 1)), i
+    finally:
+        b.release_plans()
