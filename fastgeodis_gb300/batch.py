@@ -2,10 +2,12 @@
 
 The reference computes one image per call (its C++ layer rejects batch != 1,
 FastGeodis/common.h:89-95).  Here a list of images -- each ``[1, C, H, W]``
-with its own soft mask ``[1, 1, H, W]`` and its own ``lamb`` -- goes into a
-single kernel launch whose CTAs pull images from a work queue, largest first,
-and run each image's whole transform.  Per image the result is bit-identical
-to :func:`fastgeodis_gb300.generalised_geodesic2d` /
+with its own soft mask ``[1, 1, H, W]``, its own ``lamb`` and its own form
+(plain or signed) -- goes into a single kernel launch whose CTAs pull jobs
+from a work queue, largest first, and run each job whole.  A signed image is
+one job (both distance maps in one CTA) or, when that job would set the
+batch's critical path, two (one map each, on two CTAs).  Per image the result
+is bit-identical to :func:`fastgeodis_gb300.generalised_geodesic2d` /
 :func:`fastgeodis_gb300.signed_generalised_geodesic2d`.
 
 :class:`GeodesicBatch2d` fixes the shapes once, owns the buffers and replays
@@ -13,7 +15,7 @@ the launch from a captured CUDA graph.
 """
 from __future__ import annotations
 
-from typing import List, Optional, Sequence, Union
+from typing import List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 import torch
@@ -24,13 +26,74 @@ from . import _lib
 ITEM_DTYPE = np.dtype([
     ("image", np.uint64), ("mask", np.uint64), ("out", np.uint64), ("image_t", np.uint64),
     ("d2", np.uint64), ("t1", np.uint64), ("t2", np.uint64),
-    ("C", np.int32), ("H", np.int32), ("W", np.int32), ("reserved0", np.int32),
+    ("C", np.int32), ("H", np.int32), ("W", np.int32), ("flags", np.int32),
     ("v", np.float32), ("l_grad", np.float32), ("l_eucl", np.float32), ("reserved1", np.float32),
 ])
 assert ITEM_DTYPE.itemsize == 88
+FG_BATCH_SIGNED, FG_BATCH_SPLIT, FG_BATCH_SECOND = 1, 2, 4
 
 MAX_SIDE = 2048
 MAX_CHANNELS = 4
+
+# Microseconds per raster step of one job (one CTA sweeps a whole row per
+# step) by (channels, maps), at rows of STEP_ROWS cells: measured on a GB300
+# with square images, 2 iterations.
+STEP_ROWS = (256, 512, 1024, 2048)
+STEP_US = {
+    (1, 1): (0.3233, 0.372, 0.5249, 0.9472),
+    (1, 2): (0.4022, 0.5079, 0.7557, 1.816),
+    (2, 1): (0.3736, 0.4618, 0.6804, 1.4291),
+    (2, 2): (0.4768, 0.5912, 0.9409, 2.4003),
+    (3, 1): (0.4197, 0.5257, 0.8414, 2.1059),
+    (3, 2): (0.5349, 0.6739, 1.0994, 2.834),
+    (4, 1): (0.4881, 0.6244, 1.0118, 2.5494),
+    (4, 2): (0.6061, 0.7746, 1.2716, 3.8427),
+}
+
+
+def step_us(C: int, maps: int, row: int) -> float:
+    """Estimated microseconds of one step over a row of `row` cells."""
+    t = STEP_US[(min(max(C, 1), MAX_CHANNELS), maps)]
+    return float(np.interp(row, STEP_ROWS, t))
+
+
+def job_cost(C: int, H: int, W: int, maps: int, iterations: int) -> float:
+    """Estimated microseconds of one job: per iteration two passes of H steps
+    over rows of W cells and two of W steps over rows of H cells."""
+    return 2.0 * max(iterations, 1) * (H * step_us(C, maps, W) + W * step_us(C, maps, H))
+
+
+def plan_jobs(shapes: Sequence[Tuple[int, int, int]], signed: Sequence[bool], iterations: int, sms: int,
+              split: Union[str, bool] = "auto") -> List[Tuple[int, int]]:
+    """Queue order of the batch's jobs, largest first: ``(image, part)`` with
+    part 0 for a whole image (plain, or signed with both maps in one CTA) and
+    1 / 2 for the halves of a split signed image (adjacent, first first).
+
+    ``split="auto"`` splits a signed image only when its one-CTA job would
+    outlast the batch's lower bound on time, max(longest job, total work / SMs)
+    with every signed image split: the others keep both maps in one CTA,
+    which reads the image once for both."""
+    n = len(shapes)
+    whole = [job_cost(C, H, W, 2 if signed[i] else 1, iterations) for i, (C, H, W) in enumerate(shapes)]
+    half = [job_cost(C, H, W, 1, iterations) for (C, H, W) in shapes]
+    sgn = [i for i in range(n) if signed[i]]
+    if split is True or split == "always":
+        halves = set(sgn)
+    elif split is False or split == "never":
+        halves = set()
+    else:
+        halves = set(sgn)
+        costs = [half[i] if i in halves else whole[i] for i in range(n)]
+        total = sum(whole[i] for i in range(n) if not signed[i]) + sum(2 * half[i] for i in sgn)
+        bound = max(max(costs, default=0.0), total / max(1, sms))
+        for i in sorted(sgn, key=lambda k: whole[k]):
+            if whole[i] <= bound:
+                halves.discard(i)
+    units = sorted(range(n), key=lambda i: -(half[i] if i in halves else whole[i]))
+    jobs: List[Tuple[int, int]] = []
+    for i in units:
+        jobs.extend([(i, 1), (i, 2)] if i in halves else [(i, 0)])
+    return jobs
 
 
 def _check_item(image: torch.Tensor, mask: torch.Tensor, device) -> None:
@@ -56,21 +119,32 @@ class GeodesicBatch2d:
 
     Args:
         shapes: list of ``(C, H, W)``.
-        signed: compute ``D(M) - D(1 - M)`` instead of ``D(M)``.
+        signed: compute ``D(M) - D(1 - M)`` instead of ``D(M)``: one value for
+            every image, or one per image (plain and signed in one launch).
         iterations: raster-scan iterations (the reference's ``iter``).
         device: CUDA device.
         use_graph: replay the launch from a captured CUDA graph.
+        inputs: optional caller-owned ``(images, masks)`` lists, used in place.
+        split: ``"auto"`` (see :func:`plan_jobs`), ``True`` (every signed image
+            as two jobs) or ``False`` (every signed image as one job).
 
     Fill ``images[i]`` / ``masks[i]`` (in place), set ``v`` / ``lambs``, call
     :meth:`run`; results are in ``outputs[i]``.
     """
 
-    def __init__(self, shapes: Sequence[Sequence[int]], signed: bool = False, iterations: int = 2,
-                 device=None, use_graph: bool = True, inputs=None):
+    def __init__(self, shapes: Sequence[Sequence[int]], signed: Union[bool, Sequence[bool]] = False,
+                 iterations: int = 2, device=None, use_graph: bool = True, inputs=None,
+                 split: Union[str, bool] = "auto"):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-        self.signed = bool(signed)
         self.iterations = int(iterations)
         self.shapes = [tuple(int(x) for x in s) for s in shapes]
+        n = len(self.shapes)
+        if isinstance(signed, (list, tuple)):
+            if len(signed) != n:
+                raise ValueError("signed must be one value or one per image")
+            self.signed = [bool(x) for x in signed]
+        else:
+            self.signed = [bool(signed)] * n
         for C, H, W in self.shapes:
             if C < 1 or C > MAX_CHANNELS or max(H, W) > MAX_SIDE or min(H, W) < 0:
                 raise RuntimeError(f"unsupported batch item shape {(C, H, W)}")
@@ -82,19 +156,19 @@ class GeodesicBatch2d:
             self.masks = [torch.ones((1, 1, H, W), device=dev) for _, H, W in self.shapes]
         self.outputs = [torch.empty((1, 1, H, W), device=dev) for _, H, W in self.shapes]
         self._scratch = []
-        for C, H, W in self.shapes:
+        for (C, H, W), sg in zip(self.shapes, self.signed):
             s = {"image_t": torch.empty((C, W, H), device=dev), "t1": torch.empty((W, H), device=dev)}
-            if self.signed:
+            if sg:
                 s["d2"] = torch.empty((H, W), device=dev)
                 s["t2"] = torch.empty((W, H), device=dev)
             self._scratch.append(s)
-        n = len(self.shapes)
-        # largest first: the queue then finishes with the short jobs
-        self.order = sorted(range(n), key=lambda i: -(self.shapes[i][1] + self.shapes[i][2]) *
-                            max(self.shapes[i][1], self.shapes[i][2]))
-        self._items_host = np.zeros(n, dtype=ITEM_DTYPE)
-        self._items_dev = torch.empty(max(1, n * ITEM_DTYPE.itemsize), dtype=torch.uint8, device=dev)
-        self._counter = torch.zeros(2, dtype=torch.int32, device=dev)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        self.jobs = plan_jobs(self.shapes, self.signed, self.iterations, sms, split)
+        nj = len(self.jobs)
+        self._items_host = np.zeros(nj, dtype=ITEM_DTYPE)
+        self._items_dev = torch.empty(max(1, nj * ITEM_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+        self._counter = torch.zeros(1 + nj, dtype=torch.int32, device=dev)  # queue + one word per split image
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.max_C = max([s[0] for s in self.shapes], default=1)
         self.max_extent = max([max(s[1], s[2]) for s in self.shapes], default=1)
         self.v = 1e10
@@ -105,18 +179,21 @@ class GeodesicBatch2d:
 
     def _fill_items(self):
         it = self._items_host
-        for slot, i in enumerate(self.order):
+        for slot, (i, part) in enumerate(self.jobs):
             C, H, W = self.shapes[i]
             s = self._scratch[i]
             lamb = float(self.lambs[i])
+            sg = self.signed[i]
             it[slot]["image"] = self.images[i].data_ptr()
             it[slot]["mask"] = self.masks[i].data_ptr()
             it[slot]["out"] = self.outputs[i].data_ptr()
             it[slot]["image_t"] = s["image_t"].data_ptr()
             it[slot]["t1"] = s["t1"].data_ptr()
-            it[slot]["d2"] = s["d2"].data_ptr() if self.signed else 0
-            it[slot]["t2"] = s["t2"].data_ptr() if self.signed else 0
+            it[slot]["d2"] = s["d2"].data_ptr() if sg else 0
+            it[slot]["t2"] = s["t2"].data_ptr() if sg else 0
             it[slot]["C"], it[slot]["H"], it[slot]["W"] = C, H, W
+            it[slot]["flags"] = (FG_BATCH_SIGNED if sg else 0) | (FG_BATCH_SPLIT if part else 0) | \
+                (FG_BATCH_SECOND if part == 2 else 0)
             it[slot]["v"] = np.float32(self.v)
             it[slot]["l_grad"] = np.float32(lamb)
             it[slot]["l_eucl"] = np.float32(1.0 - lamb)  # FastGeodis/__init__.py:63-65
@@ -126,10 +203,8 @@ class GeodesicBatch2d:
     def _launch(self):
         L = _lib.load()
         stream = torch.cuda.current_stream(self.device).cuda_stream
-        cnt = self._counter
-        rc = L.fg_batch_geodesic2d(self._items_dev.data_ptr(), len(self.shapes), self.max_C, self.max_extent,
-                                   1 if self.signed else 0, self.iterations, cnt.data_ptr(),
-                                   cnt.data_ptr() + 4, stream)
+        rc = L.fg_batch_geodesic2d(self._items_dev.data_ptr(), len(self.jobs), self.max_C, self.max_extent, 0,
+                                   self.iterations, self._counter.data_ptr(), self._status.data_ptr(), stream)
         _lib.check(rc)
 
     def run(self):
@@ -157,6 +232,14 @@ class GeodesicBatch2d:
                 self._graph = g
             self._graph.replay()
             return self.outputs
+
+    def check(self) -> None:
+        """Synchronise and raise if a launch recorded an error (a wait that
+        timed out, or a malformed split pair)."""
+        code = int(self._status.item())
+        if code:
+            self._status.zero_()
+            raise _lib.EngineError(f"fastgeodis_gb300 batch error {code}")
 
 
 def _as_list(x, n, name) -> List[float]:

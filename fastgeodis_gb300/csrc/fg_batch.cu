@@ -1,202 +1,190 @@
-// Batched 2D transforms: many images of uneven size (and channel count) in
-// one persistent launch.
+// Batched 2D transforms: many images of uneven size, channel count and form
+// (plain or signed) in one persistent launch.
 //
-// Each CTA repeatedly claims the next image from a work queue (an atomic
-// counter; the caller orders the images largest first) and runs that image's
-// whole transform by itself: transposed image copy, initial distances, every
-// pass of every iteration (through pass_body, one tile covering the whole
-// cross-section), and for the signed form the final subtraction.  No CTA
-// ever waits for another, so any number of images and any grid size is safe,
-// and the launch can be captured in a CUDA graph (memset of the counter +
-// one kernel).  Each image's arithmetic is exactly that of the per-call path:
-// results are bit-identical, alone or in a batch.  The per-call path itself
-// runs small images (sides up to FG_ONE_LAUNCH_SIDE) through the same
-// per-image body in a one-CTA launch (fg_batch2d_one_kernel).
+// Each CTA repeatedly claims the next job from a work queue (an atomic
+// counter; the caller orders the jobs largest first) and runs it by itself
+// (pass_body, one tile covering the whole cross-section, no halo exchange).
+// A job is one descriptor: a plain image (initial distances, image transpose,
+// `iterations` x 4 passes), a signed image with both distance maps in one
+// CTA (they share the image reads), or one half of a signed image split over
+// two consecutive descriptors (half the latency).  The first half transposes
+// the image and computes D(mask); the second computes D(1 - mask) and reads
+// the transposed image after the first half has published it (a bounded wait
+// on a per-pair word: the first half was claimed earlier by a running CTA and
+// waits for nothing); whichever half finishes second writes the difference.
+// No other CTA waits for another, so any number of jobs and any grid size is
+// safe, and the launch can be captured in a CUDA graph (memset of the
+// counters + one kernel).
+//
+// Every job runs the pass body compiled for its image's channel count (1 to
+// 4), so a mixed batch costs what its images cost alone; with the count a
+// run-time value the general body spilled registers beside the others in
+// this kernel.  Each image's arithmetic is exactly that of the per-call path:
+// results are bit-identical, alone, in a batch, split or not.  The per-call
+// path itself runs small images (sides up to FG_ONE_LAUNCH_SIDE) through the
+// same per-image body in a one-CTA launch (fg_batch2d_one_kernel).
 
 #include <math.h>
 
 #include <algorithm>
-#include <type_traits>
 
-#include "fg_pass.cuh"
+#include "fg_batch.cuh"
+#include "fg_wait.cuh"
 
 namespace fgi {
 namespace {
 
-
-__device__ void batch_prologue(const fg_batch2d_item &it, bool is_signed, float *sm) {
-  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
-  const int H = it.H, W = it.W;
-  const long long P = (long long)H * W;
-  // image [C][H][W] -> [C][W][H], 32x32 tiles through shared memory, one per warp
-  float *tb = sm + warp * 32 * 33;
-  const int th = (H + 31) / 32, tw = (W + 31) / 32;
-  for (int job = warp; job < it.C * th * tw; job += nwarps) {
-    const int c = job / (th * tw), r = job - c * th * tw, h0 = (r / tw) * 32, w0 = (r % tw) * 32;
-    const float *src = it.image + c * P;
-    float *dst = it.image_t + c * P;
-    for (int y = 0; y < 32; y++) {
-      int h = h0 + y, w = w0 + lane;
-      if (h < H && w < W) tb[y * 33 + lane] = src[(long long)h * W + w];
-    }
-    __syncwarp();
-    for (int y = 0; y < 32; y++) {
-      int w = w0 + y, h = h0 + lane;
-      if (h < H && w < W) dst[(long long)w * H + h] = tb[lane * 33 + y];
-    }
-    __syncwarp();
-  }
-  // initial distances v*M (and v*(1-M) for the signed form)
-  for (long long i = tid; i < P; i += NT) {
-    const float m = it.mask[i];
-    it.out[i] = __fmul_rn(it.v, m);
-    if (is_signed) it.d2[i] = __fmul_rn(it.v, __fsub_rn(1.0f, m));
-  }
-}
-
-// arguments of pass `k` (0: along H forward, 1: along H backward writing
-// [W][H], 2: along W forward, 3: along W backward writing [H][W])
-__device__ void batch_pass_args(const fg_batch2d_item &it, int M, int k, int S, int depth, float r2, int *status,
-                                PassArgs *pa) {
-  PassArgs a;
-  const int H = it.H, W = it.W;
-  const bool alongW = k >= 2, back = (k & 1) != 0;
-  const long long P = (long long)H * W;
-  a.img = alongW ? it.image_t : it.image;
-  a.img_cs = P;
-  a.C = it.C;
-  float *r[2] = {it.out, it.d2}, *t[2] = {it.t1, it.t2};
-  const float ld[3] = {r2, 1.0f, r2};
-  for (int m = 0; m < kMaxMaps; m++) {
-    const int mm = m < M ? m : 0;
-    a.dsrc[m] = alongW ? t[mm] : r[mm];
-    a.ddst[m] = (k == 1) ? t[mm] : ((k == 3) ? r[mm] : const_cast<float *>(a.dsrc[m]));
-    a.lg[m] = it.l_grad;
-    for (int n = 0; n < 9; n++) a.e[m][n] = n < 3 ? __fmul_rn(it.l_eucl, ld[n]) : 0.0f;
-  }
-  a.L = alongW ? W : H;
-  a.dir = back ? -1 : 1;
-  a.s_str = alongW ? H : W;
-  a.st1 = 0;
-  const int N2 = alongW ? H : W;
-  if (k == 1) {
-    a.ws_str = 1, a.wst1 = 0, a.wst2 = H;
-  } else if (k == 3) {
-    a.ws_str = 1, a.wst1 = 0, a.wst2 = W;
-  } else {
-    a.ws_str = a.s_str, a.wst1 = 0, a.wst2 = 1;
-  }
-  a.N1 = 1;
-  a.N2 = N2;
-  a.T1 = 1, a.T2 = N2, a.K1 = 0, a.K2 = 0, a.tiles1 = 1, a.tiles2 = 1;
-  a.S = S;
-  a.B2 = ((N2 + 3) & ~3) + 8;
-  a.rowf = ring_pitch(a.B2);
-  bool vec = (H % 4 == 0) && (W % 4 == 0);
-  const void *ptrs[6] = {a.img, it.out, it.t1, M > 1 ? it.d2 : it.out, M > 1 ? it.t2 : it.t1, it.image_t};
-  for (int i = 0; i < 6; i++) vec = vec && ((reinterpret_cast<uintptr_t>(ptrs[i]) & 15) == 0);
-  a.vec = vec ? 1 : 0;
-  a.xch = nullptr;  // one tile per image: no halo exchange
-  a.epoch_base = 0;
-  a.status = status;
-  a.tape = nullptr;
-  a.P = depth;
-  *pa = a;
-}
-
-// One image's whole transform by one CTA: initial distances and the image
-// transpose, `iterations` x 4 passes, and the signed difference.
+// One job: the passes of M maps from map `first` of one image.  `pair` is the
+// split pair's word (ready +1 by the first half, +2 by each half when done).
 template <int CT, int M>
-__device__ __forceinline__ void batch_item(const fg_batch2d_item &it, int iterations, int S, float r2, int *status,
-                                           float *sm, PassArgs &s_args) {
-  if ((long long)it.H * it.W > 0) {
-    batch_prologue(it, M == 2, sm);
-    __threadfence();
-    __syncthreads();
-    for (int iter = 0; iter < iterations; iter++) {
-      for (int k = 0; k < 4; k++) {
-        const int L = k >= 2 ? it.W : it.H;
-        const bool wt = k & 1;
-        if (L <= 1 && !wt) continue;
-        if (threadIdx.x == 0)
-          batch_pass_args(it, M, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), M), r2, status, &s_args);
-        __syncthreads();
-        if (wt)
-          pass_body<1, CT, M, MODE_GENERAL, true, false, false>(s_args, 0, sm);
-        else
-          pass_body<1, CT, M, MODE_GENERAL, false, false, false>(s_args, 0, sm);
-        __threadfence();
-        __syncthreads();
-      }
-    }
-    if (M == 2) {
-      const long long P = (long long)it.H * it.W;
-      for (long long p = threadIdx.x; p < P; p += blockDim.x) it.out[p] = __fsub_rn(it.out[p], it.d2[p]);
-    }
-  }
+__device__ __forceinline__ void batch_item(const fg_batch2d_item &it, int first, bool split, unsigned *pair,
+                                           int iterations, size_t smem, float r2, int *status, float *sm,
+                                           PassArgs &s_args, int &s_flag) {
+  const int H = it.H, W = it.W;
+  const long long P = (long long)H * W;
+  if (P <= 0) return;
+  int S = 4, depth = 2;  // the launch sized `smem` for every job variant
+  batch_job_fit(it.C, M, max(H, W), smem, &S, &depth);
+  batch_prologue(it, first, M, first == 0, sm);
+  __threadfence();
   __syncthreads();
-}
-
-template <int CT, int M>
-__global__ void __launch_bounds__(kThreads, 1)
-    fg_batch2d_kernel(const fg_batch2d_item *items, int n, int iterations, int S, float r2, int *counter,
-                      int *status) {
-  extern __shared__ __align__(16) float sm[];
-  __shared__ int s_item;
-  __shared__ PassArgs s_args;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+  if (split && first == 0 && threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(pair, 1u);  // the transposed image is published
+  }
+  bool need_t = split && first == 1;
+  for (int iter = 0; iter < iterations; iter++) {
+    for (int k = 0; k < 4; k++) {
+      const int L = k >= 2 ? W : H;
+      const bool wt = k & 1;
+      if (L <= 1 && !wt) continue;
+      if (need_t && k >= 2) {
+        if (threadIdx.x == 0) wait_count(pair, 1u, status, kSpinLimit);
+        __syncthreads();
+        need_t = false;
+      }
+      if (threadIdx.x == 0) batch_pass_args(it, M, first, k, S, depth, r2, status, &s_args);
+      __syncthreads();
+      if (wt)
+        pass_body<1, CT, M, MODE_GENERAL, true, false, false>(s_args, 0, sm);
+      else
+        pass_body<1, CT, M, MODE_GENERAL, false, false, false>(s_args, 0, sm);
+      __threadfence();
+      __syncthreads();
+    }
+  }
+  if (M == 2) {
+    for (long long p = threadIdx.x; p < P; p += blockDim.x) it.out[p] = __fsub_rn(it.out[p], it.d2[p]);
+  }
+  if (split) {
+    // the second half to finish subtracts (the other's stores were fenced
+    // before its count; read them from L2)
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_flag = atomicAdd(pair, 2u) == 3u;
+      __threadfence();
+    }
     __syncthreads();
-    const int i = s_item;
-    if (i >= n) break;
-    batch_item<CT, M>(items[i], iterations, S, r2, status, sm, s_args);
+    if (s_flag) {
+      for (long long p = threadIdx.x; p < P; p += blockDim.x)
+        it.out[p] = __fsub_rn(__ldcg(it.out + p), __ldcg(it.d2 + p));
+    }
   }
 }
 
-// One image (the descriptor as a kernel parameter): the single-call form.
+// the job's channel variant
+template <int M>
+__device__ __forceinline__ void batch_item_ct(const fg_batch2d_item &it, int first, bool split, unsigned *pair,
+                                              int iterations, size_t smem, float r2, int *status, float *sm,
+                                              PassArgs &s_args, int &s_flag) {
+  switch (batch_ct(it.C)) {
+    case 1: batch_item<1, M>(it, first, split, pair, iterations, smem, r2, status, sm, s_args, s_flag); break;
+    case 2: batch_item<2, M>(it, first, split, pair, iterations, smem, r2, status, sm, s_args, s_flag); break;
+    case 3: batch_item<3, M>(it, first, split, pair, iterations, smem, r2, status, sm, s_args, s_flag); break;
+    default: batch_item<4, M>(it, first, split, pair, iterations, smem, r2, status, sm, s_args, s_flag); break;
+  }
+}
+
+__device__ __forceinline__ bool same_image(const fg_batch2d_item &a, const fg_batch2d_item &b) {
+  return a.image == b.image && a.mask == b.mask && a.out == b.out && a.image_t == b.image_t && a.d2 == b.d2 &&
+         a.t1 == b.t1 && a.t2 == b.t2 && a.C == b.C && a.H == b.H && a.W == b.W && a.v == b.v &&
+         a.l_grad == b.l_grad && a.l_eucl == b.l_eucl;
+}
+
+// Job j of the queue.  A split half whose partner descriptor is missing or
+// differs records FG_ERR_INVALID_ARGUMENT and runs nothing.
+__device__ void batch_job(const fg_batch2d_item *items, int n, int j, int all_signed, int iterations, size_t smem,
+                          float r2, unsigned *pairs, int *status, float *sm, PassArgs &s_args, int &s_flag) {
+  const fg_batch2d_item &it = items[j];  // read where used: a copy would stay live across the passes
+  const int sgn = all_signed ? FG_BATCH_SIGNED : 0;
+  const int f = it.flags | sgn;
+  const bool is_signed = (f & FG_BATCH_SIGNED) != 0;
+  const bool split = is_signed && (f & FG_BATCH_SPLIT) != 0;
+  const int first = split && (f & FG_BATCH_SECOND) ? 1 : 0;
+  if (split) {
+    const int jo = first ? j - 1 : j + 1;
+    bool ok = jo >= 0 && jo < n;
+    if (ok) {
+      const fg_batch2d_item &o = items[jo];
+      const int fo = o.flags | sgn;
+      ok = same_image(it, o) && (fo & FG_BATCH_SIGNED) && (fo & FG_BATCH_SPLIT) &&
+           ((fo & FG_BATCH_SECOND) != 0) == (first == 0);
+    }
+    if (!ok) {
+      if (threadIdx.x == 0) atomicCAS(status, 0, FG_ERR_INVALID_ARGUMENT);
+      return;
+    }
+  }
+  if (is_signed && !split)
+    batch_item_ct<2>(it, 0, false, nullptr, iterations, smem, r2, status, sm, s_args, s_flag);
+  else
+    batch_item_ct<1>(it, first, split, pairs + (j - first), iterations, smem, r2, status, sm, s_args, s_flag);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    fg_batch2d_kernel(const fg_batch2d_item *items, int n, int all_signed, int iterations, size_t smem, float r2,
+                      int *counter, int *status) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int s_job, s_flag;
+  __shared__ PassArgs s_args;
+  unsigned *pairs = reinterpret_cast<unsigned *>(counter + 1);
+  for (;;) {
+    if (threadIdx.x == 0) s_job = atomicAdd(counter, 1);
+    __syncthreads();
+    const int j = s_job;
+    if (j >= n) break;
+    batch_job(items, n, j, all_signed, iterations, smem, r2, pairs, status, sm, s_args, s_flag);
+    __syncthreads();
+  }
+}
+
+// One image (the descriptor as a kernel parameter): the single-call form,
+// both maps of a signed image in this one CTA.
 template <int CT, int M>
 __global__ void __launch_bounds__(kThreads, 1)
-    fg_batch2d_one_kernel(const fg_batch2d_item it, int iterations, int S, float r2, int *status) {
+    fg_batch2d_one_kernel(const fg_batch2d_item it, int iterations, size_t smem, float r2, int *status) {
   extern __shared__ __align__(16) float sm[];
+  __shared__ int s_flag;
   __shared__ PassArgs s_args;
-  batch_item<CT, M>(it, iterations, S, r2, status, sm, s_args);
+  batch_item<CT, M>(it, 0, false, nullptr, iterations, smem, r2, status, sm, s_args, s_flag);
 }
 
-template <int CT, int M>
-int launch_batch(const fg_batch2d_item *items, int n, int iterations, int S, int *counter, int *status,
-                 size_t smem, int grid, cudaStream_t s) {
-  auto fn = fg_batch2d_kernel<CT, M>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
-  fn<<<grid, kThreads, smem, s>>>(items, n, iterations, S, r2, counter, status);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  return FG_OK;
+// Dynamic shared memory of a launch whose jobs have up to max_C channels,
+// sides up to max_extent and 1 to `maps` distance maps: the most any job
+// variant takes at the first (S, depth) of batch_job_fit that fits the
+// limit.  0 if some variant fits none.
+size_t batch_plan(int max_C, int max_extent, int maps) {
+  size_t need = kBatchTransposeSmem;
+  for (int C = 1; C <= max_C; C++) {
+    for (int M = 1; M <= maps; M++) {
+      int S = 0, depth = 0;
+      if (!batch_job_fit(C, M, max_extent, kBatchSmemLimit, &S, &depth)) return 0;
+      need = std::max(need, batch_job_smem(C, M, max_extent, S, depth));
+    }
+  }
+  return need;
 }
 
-}  // namespace
-}  // namespace fgi
-
-namespace fgi {
-namespace {
-// shared memory of the batched kernel with S steps per transposed flush
-size_t batch_smem(int max_C, int max_extent, int is_signed, int S) {
-  const int M = is_signed ? 2 : 1;
-  const int nch = pass_nch(max_C == 1 ? 1 : 0, MODE_GENERAL);
-  const int depth = pass_depth(nch, M);
-  const int rowf = ring_pitch(((max_extent + 3) & ~3) + 8);  // one row: 4-cell apron, runs of 4, apron
-  // the largest pass: a transposed-writing one (S distance rows) over the longest side
-  const size_t pass = (size_t)(S * M + 2 * max_C) * (rowf + pass_edge_floats(1, 1, max_extent)) * 4 +
-                      (size_t)depth * (M + max_C) * kThreads * 16 +
-                      (size_t)max_extent * 8 + 64;
-  const size_t transpose = (size_t)(kThreads / 32) * 32 * 33 * 4;
-  return std::max(pass, transpose);
-}
-constexpr size_t kBatchSmemLimit = 227 * 1024;
-int batch_flush_steps(int max_C, int max_extent, int is_signed) {
-  return batch_smem(max_C, max_extent, is_signed, 8) <= kBatchSmemLimit ? 8 : 4;
-}
 }  // namespace
 }  // namespace fgi
 
@@ -205,25 +193,30 @@ int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, 
   const int ext = std::max(it.H, it.W);
   if (it.C < 1 || it.C > kMaxChannels || ext > 4 * kThreads)
     return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: 1 to 4 channels, sides up to 2048");
-  const int S = batch_flush_steps(it.C, ext, is_signed);
-  const size_t smem = batch_smem(it.C, ext, is_signed, S);
-  if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: shared memory");
+  const size_t smem = batch_plan(it.C, ext, is_signed ? 2 : 1);
+  if (smem == 0)
+    return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: shared memory");
   const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
   auto launch = [&](auto fn) -> int {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-    fn<<<1, kThreads, smem, s>>>(it, std::max(iterations, 0), S, r2, status);
+    fn<<<1, kThreads, smem, s>>>(it, std::max(iterations, 0), smem, r2, status);
     e = cudaGetLastError();
     return e == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   };
-  if (it.C == 1) return is_signed ? launch(fg_batch2d_one_kernel<1, 2>) : launch(fg_batch2d_one_kernel<1, 1>);
-  return is_signed ? launch(fg_batch2d_one_kernel<0, 2>) : launch(fg_batch2d_one_kernel<0, 1>);
+  switch (batch_ct(it.C)) {
+    case 1: return is_signed ? launch(fg_batch2d_one_kernel<1, 2>) : launch(fg_batch2d_one_kernel<1, 1>);
+    case 2: return is_signed ? launch(fg_batch2d_one_kernel<2, 2>) : launch(fg_batch2d_one_kernel<2, 1>);
+    case 3: return is_signed ? launch(fg_batch2d_one_kernel<3, 2>) : launch(fg_batch2d_one_kernel<3, 1>);
+    default: return is_signed ? launch(fg_batch2d_one_kernel<4, 2>) : launch(fg_batch2d_one_kernel<4, 1>);
+  }
 }
 }  // namespace fgi
 
 extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed) {
-  if (max_C < 1 || max_extent < 1) return 0;
-  return fgi::batch_smem(max_C, max_extent, is_signed, fgi::batch_flush_steps(max_C, max_extent, is_signed));
+  if (max_C < 1 || max_C > fgi::kMaxChannels || max_extent < 1) return 0;
+  (void)is_signed;  // a launch sizes for plain, split and two-map signed jobs alike
+  return fgi::batch_plan(max_C, max_extent, 2);
 }
 
 extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
@@ -237,525 +230,21 @@ extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, i
     return set_error(FG_ERR_UNSUPPORTED, "batch: image sides up to 2048 are supported (one CTA sweeps a whole row)");
   if (n == 0) return FG_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int) * (1 + (size_t)n), s);  // queue and pair words
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int S = batch_flush_steps(max_C, max_extent, is_signed);
-  const size_t smem = batch_smem(max_C, max_extent, is_signed, S);
-  if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "batch: shared memory plan too large");
-  const int grid = std::max(1, std::min(n, sms));
-  const int its = std::max(iterations, 0);
-  if (max_C == 1)
-    return is_signed ? launch_batch<1, 2>(items, n, its, S, counter, status, smem, grid, s)
-                     : launch_batch<1, 1>(items, n, its, S, counter, status, smem, grid, s);
-  return is_signed ? launch_batch<0, 2>(items, n, its, S, counter, status, smem, grid, s)
-                   : launch_batch<0, 1>(items, n, its, S, counter, status, smem, grid, s);
-}
-
-// ---------------------------------------------------------------------------
-// differentiable 2D transform: forward with argmin tape, adjoint kernel
-// ---------------------------------------------------------------------------
-
-namespace fgi {
-namespace {
-
-__device__ fg_batch2d_item as_batch_item(const fg_grad2d_item &g) {
-  fg_batch2d_item b;
-  b.image = g.image, b.mask = g.mask, b.out = g.out, b.image_t = g.image_t;
-  b.d2 = nullptr, b.t1 = g.t1, b.t2 = nullptr;
-  b.C = g.C, b.H = g.H, b.W = g.W, b.reserved0 = 0;
-  b.v = g.v, b.l_grad = g.l_grad, b.l_eucl = g.l_eucl, b.reserved1 = 0.0f;
-  return b;
-}
-
-// tape_pass < 0: record the tape of every pass at (iteration * 4 + pass) * H * W.
-// tape_pass >= 0: run the passes up to that one (numbered iteration * 4 + k)
-// and record only its tape, at the start of the item's tape buffer (the
-// memory-saving mode's recomputation).
-template <int CT>
-__global__ void __launch_bounds__(kThreads, 1)
-    fg_grad2d_forward_kernel(const fg_grad2d_item *items, int n, int iterations, int tape_pass, int S, float r2,
-                             int *counter, int *status) {
-  extern __shared__ __align__(16) float sm[];
-  __shared__ int s_item;
-  __shared__ PassArgs s_args;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-    __syncthreads();
-    const int i = s_item;
-    if (i >= n) break;
-    const fg_grad2d_item g = items[i];
-    const fg_batch2d_item it = as_batch_item(g);
-    const long long P = (long long)it.H * it.W;
-    if (P > 0) {
-      batch_prologue(it, false, sm);
-      __threadfence();
-      __syncthreads();
-      const int npass = tape_pass >= 0 ? tape_pass + 1 : 4 * iterations;
-      for (int pi = 0; pi < npass; pi++) {
-        const int k = pi & 3;
-        const int L = k >= 2 ? it.W : it.H;
-        const bool wt = k & 1;
-        if (L <= 1 && !wt) continue;
-        const bool rec = tape_pass < 0 || pi == tape_pass;
-        if (threadIdx.x == 0) {
-          batch_pass_args(it, 1, k, S, pass_depth(pass_nch(CT, MODE_GENERAL), 1), r2, status, &s_args);
-          s_args.tape = rec ? g.tape + (tape_pass < 0 ? (long long)pi * P : 0) : nullptr;
-        }
-        __syncthreads();
-        // the tape-recording body gives the same distances as the plain one
-        if (rec) {
-          if (wt)
-            pass_body<1, CT, 1, MODE_GENERAL, true, true, false>(s_args, 0, sm);
-          else
-            pass_body<1, CT, 1, MODE_GENERAL, false, true, false>(s_args, 0, sm);
-        } else {
-          if (wt)
-            pass_body<1, CT, 1, MODE_GENERAL, true, false, false>(s_args, 0, sm);
-          else
-            pass_body<1, CT, 1, MODE_GENERAL, false, false, false>(s_args, 0, sm);
-        }
-        __threadfence();
-        __syncthreads();
-      }
-    }
-    __syncthreads();
-  }
-}
-
-__device__ __forceinline__ float sgnf(float d) { return d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f); }
-
-// Adjoint of one pass of one image (one CTA).  The forward pass computed, for
-// t = 1..L-1 and every cell x, D[t][x] = min(Dold[t][x], D[t-1][x+k] + cost_k);
-// the tape holds which term won.  Walking t downwards, the gradient of a cell
-// either stays with Dold (the pass input) or moves to the predecessor
-// D[t-1][x+k] (and to the image through l_grad * |I - I'| of that step).
-template <int NCH, int J>
-__device__ void adjoint_pass(const fg_grad2d_item &g, int k, const unsigned char *tape, int C, float *sm) {
-  const int tid = threadIdx.x, NT = blockDim.x;
-  const int H = g.H, W = g.W;
-  const long long P = (long long)H * W;
-  const bool alongW = k >= 2;
-  const int dir = (k & 1) ? -1 : 1;
-  const int L = alongW ? W : H, N = alongW ? H : W;
-  const long long s_str = alongW ? H : W;                      // read layout: step stride (cross stride 1)
-  long long ws_str, wc;                                        // write layout
-  if (k == 1) ws_str = 1, wc = H;
-  else if (k == 3) ws_str = 1, wc = W;
-  else ws_str = s_str, wc = 1;
-  const float *Gout = (k == 0 || k == 3) ? g.g_r : g.g_t;
-  float *Gin = alongW ? g.g_t : g.g_r;
-  const float *I = alongW ? g.image_t : g.image;
-  float *gI = alongW ? g.gi_t : g.g_image;
-  const float lg = g.l_grad;
-  // the gradient each cell of a row hands to the previous row and its tape
-  // code, double-buffered by step parity (one barrier per step)
-  float *gvb = sm;                                   // [2][N]
-  int *cdb = reinterpret_cast<int *>(sm + 2 * N);    // [2][N]
-  // J cells per thread, x = tid + j * NT: N <= J * NT (J is chosen from the
-  // batch's widest image, so no thread carries empty cells)
-  auto pos = [&](int t) -> long long { return dir > 0 ? (long long)t : (long long)(L - 1 - t); };
-  // Per cell x = tid + j * NT: the step's inputs, loaded one step ahead so
-  // that no global load sits on a step's critical path.  Image rows are kept
-  // at x-1, x, x+1 (row s of the step and row sp before it); each step loads
-  // one new row, the next step's sp.
-  float go[J], gi[J][NCH], is_[J][NCH][3], isp[J][NCH][3];
-  int cd[J];
-  float go_n[J], gi_n[J][NCH], isp_n[J][NCH][3];
-  int cd_n[J];
-  auto load_row = [&](float (&dst)[J][NCH][3], long long r) {
-#pragma unroll
-    for (int j = 0; j < J; j++) {
-      const int x = tid + j * NT;
-#pragma unroll
-      for (int c = 0; c < NCH; c++)
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const int xx = x + q - 1;
-          dst[j][c][q] = (c < C && x < N && xx >= 0 && xx < N) ? I[c * P + r * s_str + xx] : 0.0f;
-        }
-    }
-  };
-  auto load_step = [&](float (&go_)[J], int (&cd_)[J], float (&gi_)[J][NCH], int t) {
-    const long long s = pos(t);
-#pragma unroll
-    for (int j = 0; j < J; j++) {
-      const int x = tid + j * NT;
-      go_[j] = x < N ? Gout[s * ws_str + x * wc] : 0.0f;
-      cd_[j] = (x < N && t > 0) ? (int)tape[s * s_str + x] : 0;
-#pragma unroll
-      for (int c = 0; c < NCH; c++) gi_[j][c] = (c < C && x < N) ? gI[c * P + s * s_str + x] : 0.0f;
-    }
-  };
-  float racc[J], gip[J][NCH];
-#pragma unroll
-  for (int j = 0; j < J; j++) {
-    racc[j] = 0.0f;
-#pragma unroll
-    for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
-  }
-  load_step(go, cd, gi, L - 1);
-  load_row(is_, pos(L - 1));
-  if (L > 1) load_row(isp, pos(L - 2));
-  for (int t = L - 1; t >= 0; t--) {
-    const long long s = pos(t);
-    // the next step's inputs, in flight during this step
-    if (t > 0) load_step(go_n, cd_n, gi_n, t - 1);
-    if (t > 1) load_row(isp_n, pos(t - 2));
-    float *gv = gvb + (t & 1) * N;
-    int *cdr = cdb + (t & 1) * N;
-#pragma unroll
-    for (int j = 0; j < J; j++) {
-      const int x = tid + j * NT;
-      if (x >= N) continue;
-      const float G = __fadd_rn(go[j], racc[j]);
-      const int code = cd[j];
-      float gself[NCH];
-#pragma unroll
-      for (int c = 0; c < NCH; c++) gself[c] = 0.0f;
-      if (code == kTapeSelf) {
-        Gin[s * s_str + x] = G;
-        gv[x] = 0.0f;
-      } else {
-        Gin[s * s_str + x] = 0.0f;
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-          if (c < C) {
-            // the predecessor x + code - 2 of row sp
-            const float ip = code == 1 ? isp[j][c][0] : (code == 2 ? isp[j][c][1] : isp[j][c][2]);
-            const float d = __fsub_rn(is_[j][c][1], ip);
-            gself[c] = __fmul_rn(__fmul_rn(G, lg), sgnf(d));
-          }
-        gv[x] = G;
-      }
-      cdr[x] = code;
-#pragma unroll
-      for (int c = 0; c < NCH; c++)
-        if (c < C) gI[c * P + s * s_str + x] = __fadd_rn(gi[j][c], __fadd_rn(gself[c], gip[j][c]));
-    }
-    __syncthreads();
-    if (t > 0) {
-#pragma unroll
-      for (int j = 0; j < J; j++) {
-        const int xq = tid + j * NT;  // cell of row t-1
-        racc[j] = 0.0f;
-#pragma unroll
-        for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
-        if (xq >= N) continue;
-#pragma unroll
-        for (int d = -1; d <= 1; d++) {
-          const int x = xq - d;  // a cell of row t whose step came from xq
-          if (x < 0 || x >= N || cdr[x] != d + 2) continue;
-          const float gx = gv[x];
-          racc[j] = __fadd_rn(racc[j], gx);
-#pragma unroll
-          for (int c = 0; c < NCH; c++)
-            if (c < C) {
-              const float dd = __fsub_rn(is_[j][c][1 - d], isp[j][c][1]);
-              gip[j][c] = __fsub_rn(gip[j][c], __fmul_rn(__fmul_rn(gx, lg), sgnf(dd)));
-            }
-        }
-      }
-      // rows and inputs move down one step
-#pragma unroll
-      for (int j = 0; j < J; j++) {
-        go[j] = go_n[j];
-        cd[j] = cd_n[j];
-#pragma unroll
-        for (int c = 0; c < NCH; c++) {
-          gi[j][c] = gi_n[j][c];
-#pragma unroll
-          for (int q = 0; q < 3; q++) is_[j][c][q] = isp[j][c][q], isp[j][c][q] = isp_n[j][c][q];
-        }
-      }
-    }
-  }
-  __syncthreads();  // the next pass reuses the exchange rows
-}
-
-// Ring of the staged adjoint (adjoint_pass_ring): a step's image row is read
-// again as the previous row of the next step, so a slot is refilled two
-// steps after its own and the loads run kAdjRing - 2 steps ahead.
-constexpr int kAdjRing = 8;
-// floats of one ring slot: upstream gradients, image-gradient row, image row
-// (C channels each where it applies) and the tape row as 4-byte words
-__host__ __device__ inline int adj_slot_floats(int N, int C) { return N * (1 + 2 * C) + (N + 3) / 4; }
-
-// The adjoint of one pass as adjoint_pass, with every global input of a step
-// (upstream gradient and image-gradient rows, image row, tape row) staged
-// into a shared ring by cp.async kAdjRing - 2 steps ahead; same arithmetic,
-// same order, same bits.
-template <int NCH, int J>
-__device__ void adjoint_pass_ring(const fg_grad2d_item &g, int k, const unsigned char *tape, int C, float *sm) {
-  const int tid = threadIdx.x, NT = blockDim.x;
-  const int H = g.H, W = g.W;
-  const long long P = (long long)H * W;
-  const bool alongW = k >= 2;
-  const int dir = (k & 1) ? -1 : 1;
-  const int L = alongW ? W : H, N = alongW ? H : W;
-  const long long s_str = alongW ? H : W;
-  long long ws_str, wc;
-  if (k == 1) ws_str = 1, wc = H;
-  else if (k == 3) ws_str = 1, wc = W;
-  else ws_str = s_str, wc = 1;
-  const float *Gout = (k == 0 || k == 3) ? g.g_r : g.g_t;
-  float *Gin = alongW ? g.g_t : g.g_r;
-  const float *I = alongW ? g.image_t : g.image;
-  float *gI = alongW ? g.gi_t : g.g_image;
-  const float lg = g.l_grad;
-  float *gvb = sm;                                   // [2][N] by step parity
-  int *cdb = reinterpret_cast<int *>(sm + 2 * N);    // [2][N]
-  float *ring = sm + 4 * N;                          // [kAdjRing][slot]
-  const int SLOT = adj_slot_floats(N, C);
-  // tape rows as 4-byte words where every row starts on one
-  const bool tw = N % 4 == 0 && s_str % 4 == 0 && (reinterpret_cast<uintptr_t>(tape) & 3) == 0;
-  auto pos = [&](int t) -> long long { return dir > 0 ? (long long)t : (long long)(L - 1 - t); };
-  auto slot = [&](int t) -> float * { return ring + (t & (kAdjRing - 1)) * SLOT; };
-  auto stage = [&](int u) {  // step u's inputs into its slot: one commit group, possibly empty
-    if (u >= 0) {
-      float *sl = slot(u);
-      const long long s = pos(u);
-      for (int x = tid; x < N; x += NT) {
-        cp_async4(sl + x, Gout + s * ws_str + x * wc);
-        for (int c = 0; c < C; c++) {
-          cp_async4(sl + (1 + c) * N + x, gI + c * P + s * s_str + x);
-          cp_async4(sl + (1 + C + c) * N + x, I + c * P + s * s_str + x);
-        }
-      }
-      if (tw && u > 0)
-        for (int w = tid; w < N / 4; w += NT) cp_async4(sl + (1 + 2 * C) * N + w, tape + s * s_str + 4 * w);
-    }
-    cp_async_commit();
-  };
-  float racc[J], gip[J][NCH];
-#pragma unroll
-  for (int j = 0; j < J; j++) {
-    racc[j] = 0.0f;
-#pragma unroll
-    for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
-  }
-  for (int u = L - 1; u >= L - (kAdjRing - 2); u--) stage(u);
-  cp_async_wait<kAdjRing - 4>();  // steps L-1 and L-2 have landed
-  __syncthreads();
-  for (int t = L - 1; t >= 0; t--) {
-    const long long s = pos(t);
-    const float *sl = slot(t), *slp = slot(t - 1);
-    float *gv = gvb + (t & 1) * N;
-    int *cdr = cdb + (t & 1) * N;
-#pragma unroll
-    for (int j = 0; j < J; j++) {
-      const int x = tid + j * NT;
-      if (x >= N) continue;
-      const float G = __fadd_rn(sl[x], racc[j]);
-      const int code = t == 0 ? 0
-                              : (tw ? (int)reinterpret_cast<const unsigned char *>(sl + (1 + 2 * C) * N)[x]
-                                    : (int)tape[s * s_str + x]);
-      float gself[NCH];
-#pragma unroll
-      for (int c = 0; c < NCH; c++) gself[c] = 0.0f;
-      if (code == kTapeSelf) {
-        Gin[s * s_str + x] = G;
-        gv[x] = 0.0f;
-      } else {
-        Gin[s * s_str + x] = 0.0f;
-        const int xp = x + code - 2;
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-          if (c < C) {
-            const float d = __fsub_rn(sl[(1 + C + c) * N + x], slp[(1 + C + c) * N + xp]);
-            gself[c] = __fmul_rn(__fmul_rn(G, lg), sgnf(d));
-          }
-        gv[x] = G;
-      }
-      cdr[x] = code;
-#pragma unroll
-      for (int c = 0; c < NCH; c++)
-        if (c < C) gI[c * P + s * s_str + x] = __fadd_rn(sl[(1 + c) * N + x], __fadd_rn(gself[c], gip[j][c]));
-    }
-    cp_async_wait<kAdjRing - 5>();  // step t-2 has landed (read after the barrier)
-    __syncthreads();
-    stage(t + 2 - kAdjRing);         // into the slot of step t+2, whose last reader (step t+1) is done
-    if (t > 0) {
-#pragma unroll
-      for (int j = 0; j < J; j++) {
-        const int xq = tid + j * NT;  // cell of row t-1
-        racc[j] = 0.0f;
-#pragma unroll
-        for (int c = 0; c < NCH; c++) gip[j][c] = 0.0f;
-        if (xq >= N) continue;
-#pragma unroll
-        for (int d = -1; d <= 1; d++) {
-          const int x = xq - d;  // a cell of row t whose step came from xq
-          if (x < 0 || x >= N || cdr[x] != d + 2) continue;
-          const float gx = gv[x];
-          racc[j] = __fadd_rn(racc[j], gx);
-#pragma unroll
-          for (int c = 0; c < NCH; c++)
-            if (c < C) {
-              const float dd = __fsub_rn(sl[(1 + C + c) * N + x], slp[(1 + C + c) * N + xq]);
-              gip[j][c] = __fsub_rn(gip[j][c], __fmul_rn(__fmul_rn(gx, lg), sgnf(dd)));
-            }
-        }
-      }
-    }
-  }
-  cp_async_wait<0>();
-  __syncthreads();  // the next pass reuses the ring and the exchange rows
-}
-
-// Adjoints of the passes pass_hi down to pass_lo (numbered iteration * 4 + k);
-// the tape of pass pi is at (pi - tape_base) * H * W.  kGradInit: the gradient
-// state starts from dLoss/dD; kGradFinal: dLoss/dmask and dLoss/dimage are
-// written at the end.  One call with both flags over every pass is the whole
-// backward; the memory-saving mode calls it once per pass.
-constexpr int kGradInit = 1, kGradFinal = 2;
-
-template <int NCH, int J, bool RING>
-__global__ void __launch_bounds__(kThreads, 1)
-    fg_grad2d_backward_kernel(const fg_grad2d_item *items, int n, int pass_hi, int pass_lo, int tape_base,
-                              int flags, int *counter) {
-  extern __shared__ __align__(16) float sm[];
-  __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-    __syncthreads();
-    const int i = s_item;
-    if (i >= n) break;
-    const fg_grad2d_item g = items[i];
-    const int H = g.H, W = g.W, C = g.C;
-    const long long P = (long long)H * W;
-    if (P > 0) {
-      if (flags & kGradInit) {
-        for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_r[p] = g.g_out[p];
-        for (long long p = threadIdx.x; p < C * P; p += blockDim.x) g.g_image[p] = 0.0f, g.gi_t[p] = 0.0f;
-        __threadfence();
-        __syncthreads();
-      }
-      for (int pi = pass_hi; pi >= pass_lo; pi--) {
-        const int k = pi & 3;
-        const int L = k >= 2 ? W : H;
-        if (L <= 1 && !(k & 1)) continue;  // the forward skipped this pass
-        if (RING)
-          adjoint_pass_ring<NCH, J>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
-        else
-          adjoint_pass<NCH, J>(g, k, g.tape + (long long)(pi - tape_base) * P, C, sm);
-        __threadfence();
-        __syncthreads();
-      }
-      if (flags & kGradFinal) {
-        // dLoss/dmask = v * dLoss/dD0 ; dLoss/dimage = its original-layout part + the transposed part
-        for (long long p = threadIdx.x; p < P; p += blockDim.x) g.g_mask[p] = __fmul_rn(g.v, g.g_r[p]);
-        for (long long q = threadIdx.x; q < C * P; q += blockDim.x) {
-          const long long c = q / P, r = q - c * P, h = r / W, w = r - h * W;
-          g.g_image[q] = __fadd_rn(g.g_image[q], g.gi_t[c * P + w * H + h]);
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-}  // namespace
-}  // namespace fgi
-
-namespace fgi {
-namespace {
-int grad_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent, int iterations, int tape_pass,
-                 int *counter, int *status, void *stream) {
-  if (n < 0 || (n > 0 && (!items || !counter || !status)))
-    return set_error(FG_ERR_INVALID_ARGUMENT, "grad: null descriptor, counter or status pointer");
-  if (max_C < 1 || max_C > kMaxChannels) return set_error(FG_ERR_UNSUPPORTED, "grad: images need 1 to 4 channels");
-  if (max_extent > 4 * kThreads) return set_error(FG_ERR_UNSUPPORTED, "grad: image sides up to 2048 are supported");
-  if (n == 0) return FG_OK;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
-  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int S = batch_flush_steps(max_C, max_extent, 0);
-  const size_t smem = batch_smem(max_C, max_extent, 0, S);
-  if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "grad: shared memory plan too large");
+  const size_t smem = batch_plan(max_C, std::max(max_extent, 1), 2);
+  if (smem == 0)
+    return set_error(FG_ERR_UNSUPPORTED, "batch: shared memory plan too large");
   const int grid = std::max(1, std::min(n, sms));
   const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
-  auto launch = [&](auto fn) -> int {
-    cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
-    fn<<<grid, kThreads, smem, s>>>(items, n, std::max(iterations, 0), tape_pass, S, r2, counter, status);
-    e2 = cudaGetLastError();
-    return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
-  };
-  return max_C == 1 ? launch(fg_grad2d_forward_kernel<1>) : launch(fg_grad2d_forward_kernel<0>);
-}
-}  // namespace
-}  // namespace fgi
-
-extern "C" FG_API int fg_grad_geodesic2d_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
-                                                 int iterations, int *counter, int *status, void *stream) {
-  return fgi::grad_forward(items, n, max_C, max_extent, iterations, -1, counter, status, stream);
-}
-
-extern "C" FG_API int fg_grad_geodesic2d_forward_pass(const fg_grad2d_item *items, int n, int max_C, int max_extent,
-                                                      int pass, int *counter, int *status, void *stream) {
-  if (pass < 0) return fgi::set_error(FG_ERR_INVALID_ARGUMENT, "grad: negative pass index");
-  return fgi::grad_forward(items, n, max_C, max_extent, pass / 4 + 1, pass, counter, status, stream);
-}
-
-namespace fgi {
-namespace {
-int grad_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent, int pass_hi, int pass_lo,
-                  int tape_base, int flags, int *counter, void *stream) {
-  if (n < 0 || (n > 0 && (!items || !counter)))
-    return set_error(FG_ERR_INVALID_ARGUMENT, "grad: null descriptor or counter pointer");
-  if (max_C < 1 || max_C > kMaxChannels) return set_error(FG_ERR_UNSUPPORTED, "grad: images need 1 to 4 channels");
-  if (max_extent > 4 * kThreads) return set_error(FG_ERR_UNSUPPORTED, "grad: image sides up to 2048 are supported");
-  if (n == 0) return FG_OK;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+  auto fn = fg_batch2d_kernel;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // adjoint_pass: gradient and code rows, two of each; the staged form adds its ring
-  const size_t smem_reg = (size_t)4 * max_extent * 4 + 64;
-  const size_t smem_ring = smem_reg + (size_t)kAdjRing * adj_slot_floats(max_extent, max_C) * 4;
-  const bool ring = smem_ring <= kBatchSmemLimit;
-  const size_t smem = ring ? smem_ring : smem_reg;
-  const int grid = std::max(1, std::min(n, sms));
-  auto launch = [&](auto fn) -> int {
-    cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
-    fn<<<grid, kThreads, smem, s>>>(items, n, pass_hi, pass_lo, tape_base, flags, counter);
-    e2 = cudaGetLastError();
-    return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
-  };
-  // cells per thread: the fewest that cover the widest image's rows and columns;
-  // the staged adjoint where its ring fits shared memory
-  auto by_j = [&](auto ring_tag) -> int {
-    constexpr bool R = decltype(ring_tag)::value;
-    if (max_extent <= kThreads)
-      return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 1, R>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 1, R>);
-    if (max_extent <= 2 * kThreads)
-      return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 2, R>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 2, R>);
-    return max_C == 1 ? launch(fg_grad2d_backward_kernel<1, 4, R>) : launch(fg_grad2d_backward_kernel<kMaxChannels, 4, R>);
-  };
-  return ring ? by_j(std::true_type{}) : by_j(std::false_type{});
-}
-}  // namespace
-}  // namespace fgi
-
-extern "C" FG_API int fg_grad_geodesic2d_backward(const fg_grad2d_item *items, int n, int max_C, int max_extent,
-                                                  int iterations, int *counter, int *status, void *stream) {
-  (void)status;
-  return fgi::grad_backward(items, n, max_C, max_extent, 4 * std::max(iterations, 0) - 1, 0, 0,
-                            fgi::kGradInit | fgi::kGradFinal, counter, stream);
-}
-
-extern "C" FG_API int fg_grad_geodesic2d_backward_pass(const fg_grad2d_item *items, int n, int max_C, int max_extent,
-                                                       int pass, int first, int last, int *counter, void *stream) {
-  if (pass < 0) return fgi::set_error(FG_ERR_INVALID_ARGUMENT, "grad: negative pass index");
-  return fgi::grad_backward(items, n, max_C, max_extent, pass, pass, pass,
-                            (first ? fgi::kGradInit : 0) | (last ? fgi::kGradFinal : 0), counter, stream);
+  fn<<<grid, kThreads, smem, s>>>(items, n, is_signed ? 1 : 0, std::max(iterations, 0), smem, r2, counter, status);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
+  return FG_OK;
 }

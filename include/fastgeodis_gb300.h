@@ -220,9 +220,9 @@ FG_API int fg_GSF3d_toivanen(const float *image, int C, int D, int H, int W, con
                              float theta, const float *spacing, float v, float lambda, int iterations, float *out,
                              void *workspace, size_t workspace_bytes, void *stream);
 
-/* One image of a batched 2D transform (see fg_batch_geodesic2d).  All
+/* One job of a batched 2D transform (see fg_batch_geodesic2d).  All
  * pointers are device pointers; float32, contiguous.  The scratch buffers
- * belong to the caller and must not overlap between items. */
+ * belong to the caller and must not overlap between images. */
 typedef struct fg_batch2d_item {
   const float *image; /* [C][H][W] */
   const float *mask;  /* [H][W] soft mask (one channel) */
@@ -231,20 +231,34 @@ typedef struct fg_batch2d_item {
   float *d2;          /* scratch [H][W] (signed only) */
   float *t1;          /* scratch [W][H] */
   float *t2;          /* scratch [W][H] (signed only) */
-  int C, H, W, reserved0;
+  int C, H, W, flags; /* flags: FG_BATCH_* */
   float v, l_grad, l_eucl, reserved1;
 } fg_batch2d_item;
 
+/* fg_batch2d_item.flags.  FG_BATCH_SPLIT runs a signed image as two jobs on
+ * two CTAs: the descriptor computes D(mask) and the next one, an identical
+ * copy with FG_BATCH_SECOND added, D(1 - mask); the job that finishes second
+ * writes the difference.  Without it both maps run in one CTA. */
+#define FG_BATCH_SIGNED 1 /* signed transform D(mask) - D(1 - mask) */
+#define FG_BATCH_SPLIT 2  /* signed, as two jobs */
+#define FG_BATCH_SECOND 4 /* the second descriptor of a split signed image */
+
 /* Batched generalised_geodesic2d / signed_generalised_geodesic2d over n
- * images of any sizes up to 2048 per side and 1-4 channels, in one
- * persistent launch: each CTA takes the next image from a work queue and
- * runs its whole transform (no counterpart in the reference, which takes one
- * image per call; per image the results are bit-identical to
- * fg_generalised_geodesic2d / fg_signed_generalised_geodesic2d).
- * `items`: device array of n descriptors, ideally ordered largest first;
- * max_C / max_extent: the largest channel count and side among them;
- * `counter`, `status`: device ints (the counter is reset by the call).
- * Capturable in a CUDA graph. */
+ * jobs -- images of any sizes up to 2048 per side and 1-4 channels, plain or
+ * signed, a signed image in one descriptor or split over two -- in one
+ * persistent launch: each CTA takes the next job from a work queue and runs
+ * it whole (no counterpart in the reference, which takes one image per call;
+ * per image the results are bit-identical to fg_generalised_geodesic2d /
+ * fg_signed_generalised_geodesic2d, split or not).
+ * `items`: device array of n descriptors, ideally ordered largest first (the
+ * two of a split image adjacent, the first first); max_C / max_extent: the
+ * largest channel count and side among them; is_signed: nonzero makes every
+ * descriptor signed (FG_BATCH_SIGNED implied), zero follows their flags;
+ * `counter`: device scratch of 1 + n ints (the work queue and one word per
+ * split image, cleared by the call); `status`: device int where
+ * FG_ERR_TIMEOUT or FG_ERR_INVALID_ARGUMENT (a split half without its
+ * partner) is recorded.  Capturable in a CUDA graph.  fg_batch2d_smem_bytes:
+ * the launch's dynamic shared memory (is_signed is ignored). */
 FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed);
 FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
                                int is_signed, int iterations, int *counter, int *status,

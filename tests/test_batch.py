@@ -1,0 +1,41 @@
+"""Host-side planning of the batched 2D transform (no GPU): the queue order
+of the jobs and when a signed image is split over two CTAs."""
+import pytest
+
+from fastgeodis_gb300.batch import ITEM_DTYPE, job_cost, plan_jobs
+
+
+def test_item_layout():
+    assert ITEM_DTYPE.itemsize == 88
+    assert ITEM_DTYPE.fields["flags"][1] == 68  # after 7 pointers and C, H, W
+
+
+def test_jobs_largest_first_and_pairs_adjacent():
+    shapes = [(1, 100, 100), (3, 2000, 1900), (1, 800, 600), (2, 50, 60)]
+    signed = [False, True, True, False]
+    jobs = plan_jobs(shapes, signed, 2, sms=152, split=True)
+    assert sorted(i for i, p in jobs if p in (0, 1)) == [0, 1, 2, 3]
+    for k, (i, p) in enumerate(jobs):
+        if p == 1:
+            assert jobs[k + 1] == (i, 2)
+    assert jobs[0] == (1, 1)  # the largest image first
+    assert [p for i, p in jobs if not signed[i]] == [0, 0]
+    assert all(p == 0 for _, p in plan_jobs(shapes, signed, 2, sms=152, split=False))
+
+
+def test_auto_split_only_the_critical_images():
+    # one huge signed image among many small ones: it alone is split
+    shapes = [(3, 2000, 2000)] + [(1, 200, 200)] * 40
+    signed = [True] * 41
+    jobs = plan_jobs(shapes, signed, 2, sms=152)
+    assert jobs[:2] == [(0, 1), (0, 2)]
+    assert all(p == 0 for _, p in jobs[2:])
+    # more work than the GPU runs at once: splitting would only add work
+    many = [(3, 1000, 1000)] * 1000
+    assert all(p == 0 for _, p in plan_jobs(many, [True] * 1000, 2, sms=152))
+
+
+def test_job_cost_monotone():
+    assert job_cost(1, 512, 512, 1, 2) < job_cost(3, 512, 512, 1, 2) < job_cost(3, 512, 512, 2, 2)
+    assert job_cost(1, 256, 256, 1, 2) < job_cost(1, 1024, 1024, 1, 2)
+    assert job_cost(1, 256, 256, 1, 4) == pytest.approx(2 * job_cost(1, 256, 256, 1, 2))

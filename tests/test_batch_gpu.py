@@ -70,3 +70,81 @@ def test_batch_rejects_bad_items():
         fg.generalised_geodesic2d_batch([torch.rand(1, 1, 8, 4096, device="cuda")],
                                         [torch.rand(1, 1, 8, 4096, device="cuda")], 1e10, 1.0)
     assert fg.generalised_geodesic2d_batch([], [], 1e10, 1.0) == []
+
+
+@pytest.mark.parametrize("split", [True, False, "auto"])
+def test_mixed_plain_and_signed_in_one_launch(split):
+    """Plain and signed images in one plan, signed images split over two CTAs
+    or not: every output bit-identical to its per-call transform."""
+    imgs, masks, lambs = make_batch(21, 10, (1, 400), [1, 2, 3, 4], odd=True)
+    n = len(imgs)
+    signed = [bool(i % 2) for i in range(n)] + [True] * n
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im in imgs] * 2
+    plan = fg.GeodesicBatch2d(shapes, signed=signed, iterations=2, use_graph=True, split=split,
+                              inputs=(imgs * 2, masks * 2))
+    plan.v, plan.lambs = 1e10, lambs * 2
+    halves = sum(1 for _, p in plan.jobs if p == 1)
+    if split is True:
+        assert halves == sum(signed)
+    if split is False:
+        assert halves == 0
+    for _ in range(2):  # capture, replay
+        outs = plan.run()
+    plan.check()
+    for i, o in enumerate(outs):
+        g = fg.signed_generalised_geodesic2d if signed[i] else fg.generalised_geodesic2d
+        ref = g(imgs[i % n], masks[i % n], 1e10, lambs[i % n], 2)
+        assert torch.equal(o.view(torch.int32), ref.view(torch.int32)), (i, shapes[i], signed[i])
+
+
+def test_split_halves_large_images():
+    """Split signed images whose second half reaches its first pass along W
+    long after the first half published the transposed image."""
+    imgs, masks, lambs = make_batch(5, 4, (1500, 2049), [1, 3])
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im in imgs]
+    plan = fg.GeodesicBatch2d(shapes, signed=True, iterations=1, use_graph=False, split=True,
+                              inputs=(imgs, masks))
+    plan.v, plan.lambs = 1e10, lambs
+    outs = plan.run()
+    plan.check()
+    for im, m, l, o in zip(imgs, masks, lambs, outs):
+        ref = fg.signed_generalised_geodesic2d(im, m, 1e10, l, 1)
+        assert torch.equal(o.view(torch.int32), ref.view(torch.int32))
+
+
+def test_split_halves_more_jobs_than_the_grid():
+    """240 jobs (120 split signed images) for a grid of one CTA per SM: halves
+    claimed late still find their first half published."""
+    imgs, masks, lambs = make_batch(13, 120, (8, 96), [1, 3], odd=True)
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im in imgs]
+    plan = fg.GeodesicBatch2d(shapes, signed=True, iterations=2, use_graph=True, split=True, inputs=(imgs, masks))
+    plan.v, plan.lambs = 1e10, lambs
+    assert len(plan.jobs) == 240
+    for _ in range(2):
+        outs = plan.run()
+    plan.check()
+    for im, m, l, o in zip(imgs, masks, lambs, outs):
+        ref = fg.signed_generalised_geodesic2d(im, m, 1e10, l, 2)
+        assert torch.equal(o.view(torch.int32), ref.view(torch.int32))
+
+
+def test_split_pair_without_partner_is_reported():
+    """A descriptor marked as the first half of a split image whose partner is
+    missing runs nothing and records FG_ERR_INVALID_ARGUMENT."""
+    from fastgeodis_gb300 import _lib
+    from fastgeodis_gb300.batch import FG_BATCH_SIGNED, FG_BATCH_SPLIT
+
+    imgs, masks, lambs = make_batch(9, 2, (16, 40), [1])
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im in imgs]
+    plan = fg.GeodesicBatch2d(shapes, signed=True, iterations=1, use_graph=False, split=False,
+                              inputs=(imgs, masks))
+    plan.v, plan.lambs = 1e10, lambs
+    plan.run()
+    plan.check()
+    plan._items_host[0]["flags"] = FG_BATCH_SIGNED | FG_BATCH_SPLIT  # no FG_BATCH_SECOND copy follows
+    host = torch.from_numpy(plan._items_host.view(np.uint8).copy())
+    plan._items_dev[: host.numel()].copy_(host)
+    plan._launch()
+    with pytest.raises(_lib.EngineError):
+        plan.check()
+    plan.check()  # cleared: the context stays usable
