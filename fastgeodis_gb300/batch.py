@@ -40,14 +40,14 @@ MAX_CHANNELS = 4
 # with square images, 2 iterations.
 STEP_ROWS = (256, 512, 1024, 2048)
 STEP_US = {
-    (1, 1): (0.3233, 0.372, 0.5249, 0.9472),
-    (1, 2): (0.4022, 0.5079, 0.7557, 1.816),
-    (2, 1): (0.3736, 0.4618, 0.6804, 1.4291),
-    (2, 2): (0.4768, 0.5912, 0.9409, 2.4003),
-    (3, 1): (0.4197, 0.5257, 0.8414, 2.1059),
-    (3, 2): (0.5349, 0.6739, 1.0994, 2.834),
-    (4, 1): (0.4881, 0.6244, 1.0118, 2.5494),
-    (4, 2): (0.6061, 0.7746, 1.2716, 3.8427),
+    (1, 1): (0.3196, 0.3633, 0.5081, 0.921),
+    (1, 2): (0.3973, 0.4968, 0.7373, 1.7835),
+    (2, 1): (0.3699, 0.4594, 0.6665, 1.4057),
+    (2, 2): (0.4706, 0.5834, 0.9154, 2.3594),
+    (3, 1): (0.4124, 0.5212, 0.8246, 2.0833),
+    (3, 2): (0.5316, 0.667, 1.071, 2.8031),
+    (4, 1): (0.4831, 0.6196, 0.9951, 2.5186),
+    (4, 2): (0.5957, 0.7626, 1.2446, 3.8202),
 }
 
 

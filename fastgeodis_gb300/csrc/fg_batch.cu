@@ -73,8 +73,10 @@ __device__ __forceinline__ void batch_item(const fg_batch2d_item &it, int first,
       __syncthreads();
     }
   }
+  float *out = it.out;  // in registers: the stores below could alias the descriptor
+  const float *d2 = it.d2;
   if (M == 2) {
-    for (long long p = threadIdx.x; p < P; p += blockDim.x) it.out[p] = __fsub_rn(it.out[p], it.d2[p]);
+    for (long long p = threadIdx.x; p < P; p += blockDim.x) out[p] = __fsub_rn(out[p], d2[p]);
   }
   if (split) {
     // the second half to finish subtracts (the other's stores were fenced
@@ -86,8 +88,7 @@ __device__ __forceinline__ void batch_item(const fg_batch2d_item &it, int first,
     }
     __syncthreads();
     if (s_flag) {
-      for (long long p = threadIdx.x; p < P; p += blockDim.x)
-        it.out[p] = __fsub_rn(__ldcg(it.out + p), __ldcg(it.d2 + p));
+      for (long long p = threadIdx.x; p < P; p += blockDim.x) out[p] = __fsub_rn(__ldcg(out + p), __ldcg(d2 + p));
     }
   }
 }

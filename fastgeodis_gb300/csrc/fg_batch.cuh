@@ -57,16 +57,21 @@ __host__ __device__ inline bool batch_job_fit(int C, int M, int ext, size_t smem
 // distances of the job's maps: v*M for map 0, v*(1-M) for map 1.
 __device__ inline void batch_prologue(const fg_batch2d_item &it, int first, int M, bool transpose, float *sm) {
   const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
-  const int H = it.H, W = it.W;
+  // the descriptor's fields in registers: the stores below could alias a
+  // descriptor in global memory and would make every iteration reload them
+  const int C = it.C, H = it.H, W = it.W;
+  const float v = it.v;
+  const float *image = it.image, *mask = it.mask;
+  float *image_t = it.image_t, *out = it.out, *d2 = it.d2;
   const long long P = (long long)H * W;
   if (transpose) {
     // image [C][H][W] -> [C][W][H], 32x32 tiles through shared memory, one per warp
     float *tb = sm + warp * 32 * 33;
     const int th = (H + 31) / 32, tw = (W + 31) / 32;
-    for (int job = warp; job < it.C * th * tw; job += nwarps) {
+    for (int job = warp; job < C * th * tw; job += nwarps) {
       const int c = job / (th * tw), r = job - c * th * tw, h0 = (r / tw) * 32, w0 = (r % tw) * 32;
-      const float *src = it.image + c * P;
-      float *dst = it.image_t + c * P;
+      const float *src = image + c * P;
+      float *dst = image_t + c * P;
       for (int y = 0; y < 32; y++) {
         int h = h0 + y, w = w0 + lane;
         if (h < H && w < W) tb[y * 33 + lane] = src[(long long)h * W + w];
@@ -81,9 +86,9 @@ __device__ inline void batch_prologue(const fg_batch2d_item &it, int first, int 
   }
   const bool m0 = first == 0, m1 = first == 1 || M == 2;
   for (long long i = tid; i < P; i += NT) {
-    const float m = it.mask[i];
-    if (m0) it.out[i] = __fmul_rn(it.v, m);
-    if (m1) it.d2[i] = __fmul_rn(it.v, __fsub_rn(1.0f, m));
+    const float m = mask[i];
+    if (m0) out[i] = __fmul_rn(v, m);
+    if (m1) d2[i] = __fmul_rn(v, __fsub_rn(1.0f, m));
   }
 }
 
