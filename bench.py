@@ -639,7 +639,7 @@ def sweep_kernel_name(w, tuned):
     if w.get("method") == "toivanen":
         return "fg_toivanen_kernel"
     if w["dims"] == 2 and max(w["image"].shape[2:]) <= _one_launch_side():
-        return "fg_batch2d_one_kernel"
+        return "fg_row2d_kernel"
     flags = [int(v[3]) for v in (tuned or {}).get("plans", {}).values() if int(v[0]) > 0]
     from fastgeodis_gb300 import _lib
 
@@ -883,7 +883,7 @@ def run_gpu_arm(args, w, rank, world):
                    "plans": ({"autotuned": tuned} if tuned else
                              "wavefront, no plan" if w.get("method") == "toivanen" else
                              "the whole transform in one launch, no pass plans"
-                             if sweep_kernel_name(w, None) == "fg_batch2d_one_kernel" else "cost model"),
+                             if sweep_kernel_name(w, None) == "fg_row2d_kernel" else "cost model"),
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB write outside the timed events)",
                    "wall_s_timed_region": round(wall, 4),
                    **({"graph_batch": graph_batch} if graph_batch else {}),

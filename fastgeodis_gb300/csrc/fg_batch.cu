@@ -20,9 +20,7 @@
 // 4), so a mixed batch costs what its images cost alone; with the count a
 // run-time value the general body spilled registers beside the others in
 // this kernel.  Each image's arithmetic is exactly that of the per-call path:
-// results are bit-identical, alone, in a batch, split or not.  The per-call
-// path itself runs small images (sides up to FG_ONE_LAUNCH_SIDE) through the
-// same per-image body in a one-CTA launch (fg_batch2d_one_kernel).
+// results are bit-identical, alone, in a batch, split or not.
 
 #include <math.h>
 
@@ -159,17 +157,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// One image (the descriptor as a kernel parameter): the single-call form,
-// both maps of a signed image in this one CTA.
-template <int CT, int M>
-__global__ void __launch_bounds__(kThreads, 1)
-    fg_batch2d_one_kernel(const fg_batch2d_item it, int iterations, size_t smem, float r2, int *status) {
-  extern __shared__ __align__(16) float sm[];
-  __shared__ int s_flag;
-  __shared__ PassArgs s_args;
-  batch_item<CT, M>(it, 0, false, nullptr, iterations, smem, r2, status, sm, s_args, s_flag);
-}
-
 // Dynamic shared memory of a launch whose jobs have up to max_C channels,
 // sides up to max_extent and 1 to `maps` distance maps: the most any job
 // variant takes at the first (S, depth) of batch_job_fit that fits the
@@ -187,31 +174,6 @@ size_t batch_plan(int max_C, int max_extent, int maps) {
 }
 
 }  // namespace
-}  // namespace fgi
-
-namespace fgi {
-int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, int *status, cudaStream_t s) {
-  const int ext = std::max(it.H, it.W);
-  if (it.C < 1 || it.C > kMaxChannels || ext > 4 * kThreads)
-    return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: 1 to 4 channels, sides up to 2048");
-  const size_t smem = batch_plan(it.C, ext, is_signed ? 2 : 1);
-  if (smem == 0)
-    return set_error(FG_ERR_UNSUPPORTED, "one-launch image transform: shared memory");
-  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
-  auto launch = [&](auto fn) -> int {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-    fn<<<1, kThreads, smem, s>>>(it, std::max(iterations, 0), smem, r2, status);
-    e = cudaGetLastError();
-    return e == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  };
-  switch (batch_ct(it.C)) {
-    case 1: return is_signed ? launch(fg_batch2d_one_kernel<1, 2>) : launch(fg_batch2d_one_kernel<1, 1>);
-    case 2: return is_signed ? launch(fg_batch2d_one_kernel<2, 2>) : launch(fg_batch2d_one_kernel<2, 1>);
-    case 3: return is_signed ? launch(fg_batch2d_one_kernel<3, 2>) : launch(fg_batch2d_one_kernel<3, 1>);
-    default: return is_signed ? launch(fg_batch2d_one_kernel<4, 2>) : launch(fg_batch2d_one_kernel<4, 1>);
-  }
-}
 }  // namespace fgi
 
 extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed) {

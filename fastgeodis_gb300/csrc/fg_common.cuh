@@ -146,9 +146,10 @@ int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, 
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int cluster_capacity(int size, int threads, size_t smem, int *out);
 
-// A whole 2D transform (plain, or signed) of one image by one CTA in one
-// launch (fg_batch.cu, the batched kernel's per-image body): initial
-// distances, the image transpose, every pass and the signed difference.
+// A whole 2D transform (plain, or signed) of one image with both sides up to
+// kOneLaunchSide by one CTA in one launch (fg_row2d.cu, one thread per cell
+// of a row): initial distances, the image transpose, every pass and the
+// signed difference.
 int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, int *status, cudaStream_t s);
 constexpr int kOneLaunchSide = FG_ONE_LAUNCH_SIDE;  // images up to this side (measured faster than per-pass launches)
 

@@ -102,6 +102,21 @@ def test_2d_vs_oracle(shape, C):
         assert bits_equal(got, want), (shape, C, lamb, it, np.abs(got - want).max())
 
 
+@pytest.mark.parametrize("shape", [(1, 5), (31, 33), (96, 200), (512, 384)])
+@pytest.mark.parametrize("C", [1, 2, 3, 4])
+def test_one_launch_forms_vs_oracle(shape, C):
+    """Images up to 512 per side run in one launch (one thread per cell of a
+    row), compiled per channel count and lamb form (0: no image term, 1: no
+    spatial term, else general): plain and signed against the oracle."""
+    rng = np.random.default_rng(hash((shape, C, "one")) % 2**32)
+    img, m = rand_case(rng, shape, C)
+    for lamb in (0.0, 1.0, 0.37):
+        got = fg.generalised_geodesic2d(t(img), t(m), 1e10, lamb, 2)[0].cpu().numpy()
+        assert bits_equal(got, oracle.geodesic2d(img, m, 1e10, lamb, 2)), (shape, C, lamb)
+        got = fg.signed_generalised_geodesic2d(t(img), t(m), 1e10, lamb, 2)[0].cpu().numpy()
+        assert bits_equal(got, oracle.signed2d(img, m, 1e10, lamb, 2)), (shape, C, lamb, "signed")
+
+
 @pytest.mark.parametrize("shape", [(300, 257), (64, 2000), (2048, 96)])
 @pytest.mark.parametrize("region", [40, 200])
 def test_2d_vs_oracle_multi_tile(shape, region, tuning):
