@@ -55,23 +55,28 @@ class _Buffers:
         self.counter = torch.zeros(2, dtype=torch.int32, device=dev)
         self.items = np.zeros(B, dtype=GRAD_ITEM_DTYPE)
         P = H * W
-        for b in range(B):
-            it = self.items[b]
-            it["image"] = image.data_ptr() + b * C * P * 4
-            it["mask"] = softmask.data_ptr() + b * P * 4
-            it["out"] = self.out.data_ptr() + b * P * 4
-            it["image_t"] = self.image_t.data_ptr() + b * C * P * 4
-            it["t1"] = self.t1.data_ptr() + b * P * 4
-            it["tape"] = self.tape.data_ptr() + b * self.tape.shape[1]
-            it["C"], it["H"], it["W"] = C, H, W
-            it["v"] = np.float32(v)
-            it["l_grad"] = np.float32(lamb)
-            it["l_eucl"] = np.float32(1.0 - float(lamb))  # FastGeodis/__init__.py:63-65
+        b = np.arange(B, dtype=np.uint64)
+        it = self.items
+        it["image"] = np.uint64(image.data_ptr()) + b * np.uint64(C * P * 4)
+        it["mask"] = np.uint64(softmask.data_ptr()) + b * np.uint64(P * 4)
+        it["out"] = np.uint64(self.out.data_ptr()) + b * np.uint64(P * 4)
+        it["image_t"] = np.uint64(self.image_t.data_ptr()) + b * np.uint64(C * P * 4)
+        it["t1"] = np.uint64(self.t1.data_ptr()) + b * np.uint64(P * 4)
+        it["tape"] = np.uint64(self.tape.data_ptr()) + b * np.uint64(self.tape.shape[1])
+        it["C"], it["H"], it["W"] = C, H, W
+        it["v"] = np.float32(v)
+        it["l_grad"] = np.float32(lamb)
+        it["l_eucl"] = np.float32(1.0 - float(lamb))  # FastGeodis/__init__.py:63-65
         self.dev = dev
+        self._pinned = []  # host copies of uploaded descriptors, alive until their copies are done
 
-    def upload(self):
-        host = torch.from_numpy(self.items.view(np.uint8).copy())
-        return host.to(self.dev, non_blocking=False)
+    def upload(self, items=None):
+        """Descriptors to the device without a host synchronisation: pinned
+        host memory, asynchronous copy on the current stream."""
+        arr = self.items if items is None else items
+        host = torch.from_numpy(arr.view(np.uint8).copy()).pin_memory()
+        self._pinned.append(host)
+        return host.to(self.dev, non_blocking=True)
 
     @property
     def npass(self):
@@ -103,14 +108,14 @@ class _Buffers:
         g_r = torch.empty((B, H, W), device=dev)
         g_t = torch.empty((B, W, H), device=dev)
         gi_t = torch.empty((B, C, W, H), device=dev)
-        for b in range(B):
-            it = self.items[b]
-            it["g_out"] = g_out.data_ptr() + b * P * 4
-            it["g_image"] = g_image.data_ptr() + b * C * P * 4
-            it["g_mask"] = g_mask.data_ptr() + b * P * 4
-            it["g_r"] = g_r.data_ptr() + b * P * 4
-            it["g_t"] = g_t.data_ptr() + b * P * 4
-            it["gi_t"] = gi_t.data_ptr() + b * C * P * 4
+        b = np.arange(B, dtype=np.uint64)
+        it = self.items
+        it["g_out"] = np.uint64(g_out.data_ptr()) + b * np.uint64(P * 4)
+        it["g_image"] = np.uint64(g_image.data_ptr()) + b * np.uint64(C * P * 4)
+        it["g_mask"] = np.uint64(g_mask.data_ptr()) + b * np.uint64(P * 4)
+        it["g_r"] = np.uint64(g_r.data_ptr()) + b * np.uint64(P * 4)
+        it["g_t"] = np.uint64(g_t.data_ptr()) + b * np.uint64(P * 4)
+        it["gi_t"] = np.uint64(gi_t.data_ptr()) + b * np.uint64(C * P * 4)
         L = _lib.load()
         items = self.upload()
         stream = torch.cuda.current_stream(dev).cuda_stream
@@ -122,9 +127,8 @@ class _Buffers:
             return g_image, g_mask
         # recompute into scratch distance maps, so the forward output stays intact
         re = self.items.copy()
-        for b in range(B):
-            re[b]["out"] = self.scratch.data_ptr() + b * H * W * 4
-        re_dev = torch.from_numpy(re.view(np.uint8).copy()).to(dev)
+        re["out"] = np.uint64(self.scratch.data_ptr()) + np.arange(B, dtype=np.uint64) * np.uint64(H * W * 4)
+        re_dev = self.upload(re)
         last = self.npass - 1
         for p in range(last, -1, -1):
             if p < last:  # the forward's tape holds the last pass; recompute the others

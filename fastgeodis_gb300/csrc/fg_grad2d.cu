@@ -9,7 +9,7 @@
 #include <algorithm>
 #include <type_traits>
 
-#include "fg_batch.cuh"
+#include "fg_row2d.cuh"
 
 namespace fgi {
 namespace {
@@ -89,6 +89,63 @@ __global__ void __launch_bounds__(kThreads, 1)
           else
             pass_body<1, CT, 1, MODE_GENERAL, false, false, false>(s_args, 0, sm);
         }
+        __threadfence();
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The forward of images up to 512 per side: the row body (one thread per
+// cell of a row, fg_row2d.cuh), compiled per channel count, the same
+// distances and the same tape as fg_grad2d_forward_kernel.
+template <bool REC, bool WT>
+__device__ __forceinline__ void grad_row_pass(int C, const PassArgs &a, float *sm) {
+  switch (C) {
+    case 1: row_pass<1, 1, MODE_GENERAL, WT, REC>(a, sm); break;
+    case 2: row_pass<2, 1, MODE_GENERAL, WT, REC>(a, sm); break;
+    case 3: row_pass<3, 1, MODE_GENERAL, WT, REC>(a, sm); break;
+    default: row_pass<4, 1, MODE_GENERAL, WT, REC>(a, sm); break;
+  }
+}
+
+__global__ void __launch_bounds__(512, 1)
+    fg_grad2d_forward_row_kernel(const fg_grad2d_item *items, int n, int iterations, int tape_pass, int S, float r2,
+                                 int *counter, int *status) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int s_item;
+  __shared__ PassArgs s_args;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int i = s_item;
+    if (i >= n) break;
+    const fg_grad2d_item g = items[i];
+    const fg_batch2d_item it = as_batch_item(g);
+    const long long P = (long long)it.H * it.W;
+    if (P > 0) {
+      batch_prologue(it, 0, 1, true, sm);
+      __threadfence();
+      __syncthreads();
+      const int npass = tape_pass >= 0 ? tape_pass + 1 : 4 * iterations;
+      for (int pi = 0; pi < npass; pi++) {
+        const int k = pi & 3;
+        const int L = k >= 2 ? it.W : it.H;
+        const bool wt = k & 1;
+        if (L <= 1 && !wt) continue;
+        const bool rec = tape_pass < 0 || pi == tape_pass;
+        if (threadIdx.x == 0) {
+          batch_pass_args(it, 1, 0, k, S, 2, r2, status, &s_args);
+          s_args.tape = rec ? g.tape + (tape_pass < 0 ? (long long)pi * P : 0) : nullptr;
+        }
+        __syncthreads();
+        // every pass runs the recording body; a pass without a tape (the
+        // memory-saving mode's earlier passes) skips only its write-back
+        if (wt)
+          grad_row_pass<true, true>(it.C, s_args, sm);
+        else
+          grad_row_pass<true, false>(it.C, s_args, sm);
         __threadfence();
         __syncthreads();
       }
@@ -447,11 +504,22 @@ int grad_forward(const fg_grad2d_item *items, int n, int max_C, int max_extent, 
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = std::max(1, std::min(n, sms));
+  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
+  if (max_extent <= kOneLaunchSide) {
+    // rows up to 512 cells: the row body, one thread per cell
+    const int NT = std::max(32, (max_extent + 31) / 32 * 32), S = 8;
+    const size_t smem = std::max(row_smem(max_C, 1, max_extent, S, true), (size_t)(NT / 32) * 32 * 33 * 4);
+    auto fn = fg_grad2d_forward_row_kernel;
+    cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
+    fn<<<grid, NT, smem, s>>>(items, n, std::max(iterations, 0), tape_pass, S, r2, counter, status);
+    e2 = cudaGetLastError();
+    return e2 == cudaSuccess ? FG_OK : set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
+  }
   const int S = grad_flush_steps(max_C, max_extent);
   const size_t smem = grad_fwd_smem(max_C, max_extent, S);
   if (smem > kBatchSmemLimit) return set_error(FG_ERR_UNSUPPORTED, "grad: shared memory plan too large");
-  const int grid = std::max(1, std::min(n, sms));
-  const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
   auto launch = [&](auto fn) -> int {
     cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e2 != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e2));
