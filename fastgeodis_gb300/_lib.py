@@ -31,6 +31,7 @@ EXPORTED = (
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
     "fg_GSF2d", "fg_GSF3d", "fg_batch2d_smem_bytes", "fg_batch_geodesic2d",
+    "fg_batch2d_tiled_scratch_bytes", "fg_batch_geodesic2d_tiled",
     "fg_grad_geodesic2d_forward", "fg_grad_geodesic2d_backward",
     "fg_grad_geodesic2d_forward_pass", "fg_grad_geodesic2d_backward_pass",
     "fg_generalised_geodesic2d_noalloc", "fg_click_mask",
@@ -86,7 +87,10 @@ def load():
     L.fg_generalised_geodesic2d_noalloc.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp]
     L.fg_batch2d_smem_bytes.argtypes = [i, i, i]
     L.fg_batch2d_smem_bytes.restype = sz
-    L.fg_batch_geodesic2d.argtypes = [vp, i, i, i, i, i, vp, vp, vp]
+    L.fg_batch_geodesic2d.argtypes = [vp, i, i, i, i, i, vp, vp, i, vp]
+    L.fg_batch2d_tiled_scratch_bytes.argtypes = [i, i]
+    L.fg_batch2d_tiled_scratch_bytes.restype = sz
+    L.fg_batch_geodesic2d_tiled.argtypes = [vp, ctypes.POINTER(ctypes.c_int), i, i, i, i, vp, sz, vp, vp]
     L.fg_grad_geodesic2d_forward.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_grad_geodesic2d_backward.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_grad_geodesic2d_forward_pass.argtypes = [vp, i, i, i, i, vp, vp, vp]

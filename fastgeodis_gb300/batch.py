@@ -15,6 +15,7 @@ the launch from a captured CUDA graph.
 """
 from __future__ import annotations
 
+import ctypes
 from typing import List, Optional, Sequence, Tuple, Union
 
 import numpy as np
@@ -96,6 +97,59 @@ def plan_jobs(shapes: Sequence[Tuple[int, int, int]], signed: Sequence[bool], it
     return jobs
 
 
+# A tiled strip's hand-off of its edges through L2, once per 8 steps, and the
+# CTAs per tiled image tried: on the uneven 2D batch (GB300) 11 images at 3
+# CTAs took 19.5 ms, at 4 CTAs 16.8, at 6 16.6 (the untiled rest then sets
+# the time); 3 CTAs per image imply about 5 us per hand-off of an image's
+# two maps.
+HANDOFF_US = 5.0
+TILE_COUNTS = (4, 6, 8)
+MAX_TILED = 32  # images per tiled launch (fg_batch_geodesic2d_tiled)
+
+
+def tiled_width(n2: int, k: int, s: int = 8) -> int:
+    """Strip width of a row of n2 cells over k CTAs (fg_batch_tiled.cu)."""
+    return max(((n2 + k - 1) // k + 3) & ~3, s)
+
+
+def tiled_cost(C: int, H: int, W: int, maps: int, iterations: int, k: int) -> float:
+    """Estimated microseconds of an image whose rows are split over k CTAs."""
+    h = HANDOFF_US / 8.0
+    return 2.0 * max(iterations, 1) * (H * (step_us(C, maps, tiled_width(W, k) + 16) + h) +
+                                       W * (step_us(C, maps, tiled_width(H, k) + 16) + h))
+
+
+def _rest_bound(shapes, signed, iterations, sms) -> float:
+    """Lower bound on the time of a batch: its longest job or its work over the SMs."""
+    jobs = plan_jobs(shapes, signed, iterations, sms)
+    cost = [job_cost(*shapes[i], 1 if p else (2 if signed[i] else 1), iterations) for i, p in jobs]
+    return max(max(cost, default=0.0), sum(cost) / max(1, sms))
+
+
+def plan_tiles(shapes: Sequence[Tuple[int, int, int]], signed: Sequence[bool], iterations: int, sms: int,
+               max_images: int = 12) -> dict:
+    """Images to run tiled beside the batch, ``{image: CTAs}``: the largest
+    images, as many and as finely split as lowers the estimated time of the
+    whole (the tiled images' longest against the rest of the batch on the
+    SMs left to it); none when tiling does not pay."""
+    n = len(shapes)
+    whole = [job_cost(C, H, W, 2 if signed[i] else 1, iterations) for i, (C, H, W) in enumerate(shapes)]
+    order = [i for i in sorted(range(n), key=lambda i: -whole[i]) if max(shapes[i][1], shapes[i][2]) >= 256]
+    best, best_t = {}, _rest_bound(shapes, signed, iterations, sms)
+    for count in range(1, min(max_images, len(order)) + 1):
+        top = order[:count]
+        rest = [i for i in range(n) if i not in set(top)]
+        for k in TILE_COUNTS:
+            if count * k > sms // 2:
+                break
+            t_tiled = max(tiled_cost(*shapes[i], 2 if signed[i] else 1, iterations, k) for i in top)
+            t_rest = _rest_bound([shapes[i] for i in rest], [signed[i] for i in rest], iterations, sms - count * k)
+            t = max(t_tiled, t_rest)
+            if t < best_t * 0.97:
+                best, best_t = {i: k for i in top}, t
+    return best
+
+
 def _check_item(image: torch.Tensor, mask: torch.Tensor, device) -> None:
     if image.dim() != 4 or mask.dim() != 4:
         raise ValueError("batch items must be [1, C, H, W] images with [1, 1, H, W] soft masks")
@@ -127,6 +181,9 @@ class GeodesicBatch2d:
         inputs: optional caller-owned ``(images, masks)`` lists, used in place.
         split: ``"auto"`` (see :func:`plan_jobs`), ``True`` (every signed image
             as two jobs) or ``False`` (every signed image as one job).
+        tiles: ``"auto"`` (see :func:`plan_tiles`), ``None`` (no tiled images)
+            or ``{image: CTAs}``: images whose rows are split over several
+            CTAs of a cooperative launch beside the batch.
 
     Fill ``images[i]`` / ``masks[i]`` (in place), set ``v`` / ``lambs``, call
     :meth:`run`; results are in ``outputs[i]``.
@@ -134,7 +191,7 @@ class GeodesicBatch2d:
 
     def __init__(self, shapes: Sequence[Sequence[int]], signed: Union[bool, Sequence[bool]] = False,
                  iterations: int = 2, device=None, use_graph: bool = True, inputs=None,
-                 split: Union[str, bool] = "auto"):
+                 split: Union[str, bool] = "auto", tiles: Union[str, dict, None] = "auto"):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.iterations = int(iterations)
         self.shapes = [tuple(int(x) for x in s) for s in shapes]
@@ -163,7 +220,33 @@ class GeodesicBatch2d:
                 s["t2"] = torch.empty((W, H), device=dev)
             self._scratch.append(s)
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
-        self.jobs = plan_jobs(self.shapes, self.signed, self.iterations, sms, split)
+        self.sms = sms
+        if tiles == "auto":
+            self.tiled = plan_tiles(self.shapes, self.signed, self.iterations, sms)
+        else:
+            self.tiled = {int(i): int(k) for i, k in (tiles or {}).items()}
+        for i, k in self.tiled.items():
+            if not (0 <= i < n) or not (2 <= k <= 16):
+                raise ValueError("tiles: {image: 2 to 16 CTAs}")
+        rest = [i for i in range(n) if i not in self.tiled]
+        sub = plan_jobs([self.shapes[i] for i in rest], [self.signed[i] for i in rest], self.iterations,
+                        sms - sum(self.tiled.values()), split)
+        self.jobs = [(rest[i], part) for i, part in sub]
+        # tiled images grouped by channel count, one cooperative launch each
+        self._tiled_groups = []
+        for C in sorted({self.shapes[i][0] for i in self.tiled}):
+            idx = [i for i in sorted(self.tiled) if self.shapes[i][0] == C]
+            for g0 in range(0, len(idx), MAX_TILED):
+                g = idx[g0:g0 + MAX_TILED]
+                ext = max(max(self.shapes[i][1], self.shapes[i][2]) for i in g)
+                scratch = torch.empty(max(1, _lib.load().fg_batch2d_tiled_scratch_bytes(len(g), ext)),
+                                      dtype=torch.uint8, device=dev)
+                self._tiled_groups.append({
+                    "images": g, "C": C, "ext": ext, "scratch": scratch,
+                    "tiles": (ctypes.c_int * len(g))(*[self.tiled[i] for i in g]),
+                    "host": np.zeros(len(g), dtype=ITEM_DTYPE),
+                    "dev": torch.empty(len(g) * ITEM_DTYPE.itemsize, dtype=torch.uint8, device=dev),
+                    "stream": torch.cuda.Stream(dev)})
         nj = len(self.jobs)
         self._items_host = np.zeros(nj, dtype=ITEM_DTYPE)
         self._items_dev = torch.empty(max(1, nj * ITEM_DTYPE.itemsize), dtype=torch.uint8, device=dev)
@@ -177,7 +260,30 @@ class GeodesicBatch2d:
         self._graph_key = None
         self.use_graph = bool(use_graph)
 
+    def _describe(self, rec, i, flags):
+        """Descriptor of image i (fg_batch2d_item) into the record rec."""
+        C, H, W = self.shapes[i]
+        s = self._scratch[i]
+        lamb = float(self.lambs[i])
+        sg = self.signed[i]
+        rec["image"] = self.images[i].data_ptr()
+        rec["mask"] = self.masks[i].data_ptr()
+        rec["out"] = self.outputs[i].data_ptr()
+        rec["image_t"] = s["image_t"].data_ptr()
+        rec["t1"] = s["t1"].data_ptr()
+        rec["d2"] = s["d2"].data_ptr() if sg else 0
+        rec["t2"] = s["t2"].data_ptr() if sg else 0
+        rec["C"], rec["H"], rec["W"] = C, H, W
+        rec["flags"] = flags
+        rec["v"] = np.float32(self.v)
+        rec["l_grad"] = np.float32(lamb)
+        rec["l_eucl"] = np.float32(1.0 - lamb)  # FastGeodis/__init__.py:63-65
+
     def _fill_items(self):
+        for g in self._tiled_groups:
+            for slot, i in enumerate(g["images"]):
+                self._describe(g["host"][slot], i, FG_BATCH_SIGNED if self.signed[i] else 0)
+            g["dev"].copy_(torch.from_numpy(g["host"].view(np.uint8).copy()), non_blocking=False)
         it = self._items_host
         for slot, (i, part) in enumerate(self.jobs):
             C, H, W = self.shapes[i]
@@ -202,10 +308,21 @@ class GeodesicBatch2d:
 
     def _launch(self):
         L = _lib.load()
-        stream = torch.cuda.current_stream(self.device).cuda_stream
-        rc = L.fg_batch_geodesic2d(self._items_dev.data_ptr(), len(self.jobs), self.max_C, self.max_extent, 0,
-                                   self.iterations, self._counter.data_ptr(), self._status.data_ptr(), stream)
-        _lib.check(rc)
+        main = torch.cuda.current_stream(self.device)
+        for g in self._tiled_groups:  # beside the batch, on their own streams
+            g["stream"].wait_stream(main)
+            with torch.cuda.stream(g["stream"]):
+                rc = L.fg_batch_geodesic2d_tiled(g["dev"].data_ptr(), g["tiles"], len(g["images"]), g["C"], g["ext"],
+                                                 self.iterations, g["scratch"].data_ptr(), g["scratch"].numel(),
+                                                 self._status.data_ptr(), g["stream"].cuda_stream)
+            _lib.check(rc)
+        if self.jobs:
+            rc = L.fg_batch_geodesic2d(self._items_dev.data_ptr(), len(self.jobs), self.max_C, self.max_extent, 0,
+                                       self.iterations, self._counter.data_ptr(), self._status.data_ptr(),
+                                       max(1, self.sms - sum(self.tiled.values())), main.cuda_stream)
+            _lib.check(rc)
+        for g in self._tiled_groups:
+            main.wait_stream(g["stream"])
 
     def run(self):
         """Compute all outputs (asynchronously on the current stream)."""

@@ -183,7 +183,8 @@ extern "C" FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is
 }
 
 extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
-                                          int is_signed, int iterations, int *counter, int *status, void *stream) {
+                                          int is_signed, int iterations, int *counter, int *status, int max_ctas,
+                                          void *stream) {
   using namespace fgi;
   if (n < 0 || (n > 0 && (!items || !counter || !status)))
     return set_error(FG_ERR_INVALID_ARGUMENT, "batch: null descriptor, counter or status pointer");
@@ -201,7 +202,7 @@ extern "C" FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, i
   const size_t smem = batch_plan(max_C, std::max(max_extent, 1), 2);
   if (smem == 0)
     return set_error(FG_ERR_UNSUPPORTED, "batch: shared memory plan too large");
-  const int grid = std::max(1, std::min(n, sms));
+  const int grid = std::max(1, std::min(n, max_ctas > 0 ? std::min(max_ctas, sms) : sms));
   const float r2 = (float)sqrt(2.0);  // fastgeodis_cpu.cpp:67
   auto fn = fg_batch2d_kernel;
   e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -54,8 +54,10 @@ __host__ __device__ inline bool batch_job_fit(int C, int M, int ext, size_t smem
 }
 
 // Transposed image copy (unless `transpose` is false) and the initial
-// distances of the job's maps: v*M for map 0, v*(1-M) for map 1.
-__device__ inline void batch_prologue(const fg_batch2d_item &it, int first, int M, bool transpose, float *sm) {
+// distances of the job's maps: v*M for map 0, v*(1-M) for map 1.  A CTA that
+// is part `part` of `parts` CTAs sharing one image does that share.
+__device__ inline void batch_prologue(const fg_batch2d_item &it, int first, int M, bool transpose, float *sm,
+                                      int part = 0, int parts = 1) {
   const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
   // the descriptor's fields in registers: the stores below could alias a
   // descriptor in global memory and would make every iteration reload them
@@ -68,7 +70,7 @@ __device__ inline void batch_prologue(const fg_batch2d_item &it, int first, int 
     // image [C][H][W] -> [C][W][H], 32x32 tiles through shared memory, one per warp
     float *tb = sm + warp * 32 * 33;
     const int th = (H + 31) / 32, tw = (W + 31) / 32;
-    for (int job = warp; job < C * th * tw; job += nwarps) {
+    for (int job = warp + part * nwarps; job < C * th * tw; job += nwarps * parts) {
       const int c = job / (th * tw), r = job - c * th * tw, h0 = (r / tw) * 32, w0 = (r % tw) * 32;
       const float *src = image + c * P;
       float *dst = image_t + c * P;
@@ -85,7 +87,7 @@ __device__ inline void batch_prologue(const fg_batch2d_item &it, int first, int 
     }
   }
   const bool m0 = first == 0, m1 = first == 1 || M == 2;
-  for (long long i = tid; i < P; i += NT) {
+  for (long long i = tid + (long long)part * NT; i < P; i += (long long)NT * parts) {
     const float m = mask[i];
     if (m0) out[i] = __fmul_rn(v, m);
     if (m1) d2[i] = __fmul_rn(v, __fsub_rn(1.0f, m));

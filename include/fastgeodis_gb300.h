@@ -257,12 +257,28 @@ typedef struct fg_batch2d_item {
  * `counter`: device scratch of 1 + n ints (the work queue and one word per
  * split image, cleared by the call); `status`: device int where
  * FG_ERR_TIMEOUT or FG_ERR_INVALID_ARGUMENT (a split half without its
- * partner) is recorded.  Capturable in a CUDA graph.  fg_batch2d_smem_bytes:
- * the launch's dynamic shared memory (is_signed is ignored). */
+ * partner) is recorded; max_ctas: CTAs of the persistent launch at most (0:
+ * one per SM).  Capturable in a CUDA graph.  fg_batch2d_smem_bytes: the
+ * launch's dynamic shared memory (is_signed is ignored). */
 FG_API size_t fg_batch2d_smem_bytes(int max_C, int max_extent, int is_signed);
 FG_API int fg_batch_geodesic2d(const fg_batch2d_item *items, int n, int max_C, int max_extent,
                                int is_signed, int iterations, int *counter, int *status,
-                               void *stream);
+                               int max_ctas, void *stream);
+
+/* Tiled images beside a batch: images whose one-CTA job would set the
+ * batch's time run in this cooperative launch (on another stream), the rows
+ * of items[i] split over tiles[i] CTAs (2-16, a host array) that hand their
+ * strips' edges over through L2 every few steps and meet between passes; up
+ * to 32 images, all of C channels, plain or FG_BATCH_SIGNED (one descriptor
+ * each, never split).  `scratch`: device memory of
+ * fg_batch2d_tiled_scratch_bytes(n, max_extent) bytes; `status` as in
+ * fg_batch_geodesic2d.  Bit-identical to the one-CTA job.  The launch needs
+ * sum(tiles) CTAs resident at once: give the batch beside it max_ctas =
+ * SMs - sum(tiles). */
+FG_API size_t fg_batch2d_tiled_scratch_bytes(int n, int max_extent);
+FG_API int fg_batch_geodesic2d_tiled(const fg_batch2d_item *items, const int *tiles, int n, int C, int max_extent,
+                                     int iterations, void *scratch, size_t scratch_bytes, int *status,
+                                     void *stream);
 
 /* One image of a differentiable 2D transform (fg_grad_geodesic2d_forward /
  * _backward; no counterpart in the reference, which is not differentiable).

@@ -39,3 +39,25 @@ def test_job_cost_monotone():
     assert job_cost(1, 512, 512, 1, 2) < job_cost(3, 512, 512, 1, 2) < job_cost(3, 512, 512, 2, 2)
     assert job_cost(1, 256, 256, 1, 2) < job_cost(1, 1024, 1024, 1, 2)
     assert job_cost(1, 256, 256, 1, 4) == pytest.approx(2 * job_cost(1, 256, 256, 1, 2))
+
+
+def test_plan_tiles_splits_only_the_critical_images():
+    from fastgeodis_gb300.batch import plan_tiles, tiled_cost, job_cost
+
+    # one large 3-channel image among many small ones: it alone is tiled
+    shapes = [(3, 2000, 1900)] + [(1, 300, 300)] * 60
+    tl = plan_tiles(shapes, [False] * 61, 2, 152)
+    assert list(tl) == [0] and 2 <= tl[0] <= 8
+    assert tiled_cost(3, 2000, 1900, 1, 2, tl[0]) < job_cost(3, 2000, 1900, 1, 2)
+    # a batch of equal images that fills the GPU: nothing to gain
+    assert plan_tiles([(1, 1024, 1024)] * 400, [False] * 400, 2, 152) == {}
+    # small images are never tiled
+    assert plan_tiles([(1, 200, 200)] * 3, [True] * 3, 2, 152) == {}
+
+
+def test_tiled_width():
+    from fastgeodis_gb300.batch import tiled_width
+
+    assert tiled_width(1968, 3) == 656 and tiled_width(1968, 3) % 4 == 0
+    assert tiled_width(30, 8) == 8  # at least the halo
+    assert tiled_width(2048, 2) == 1024

@@ -148,3 +148,40 @@ def test_split_pair_without_partner_is_reported():
     with pytest.raises(_lib.EngineError):
         plan.check()
     plan.check()  # cleared: the context stays usable
+
+
+@pytest.mark.parametrize("signed", [False, True])
+def test_tiled_images_beside_the_batch(signed):
+    """Images whose rows are split over 2-8 CTAs of the cooperative launch
+    beside the batch (odd sizes, 1-4 channels): bit-identical to per call."""
+    imgs, masks, lambs = make_batch(31 + signed, 9, (40, 700), [1, 2, 3, 4], odd=True)
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im in imgs]
+    tiles = {0: 2, 2: 3, 3: 8, 5: 4, 6: 2, 8: 6}
+    plan = fg.GeodesicBatch2d(shapes, signed=signed, iterations=2, use_graph=True, tiles=tiles,
+                              inputs=(imgs, masks))
+    plan.v, plan.lambs = 1e10, lambs
+    assert {i for i, _ in plan.jobs} == {1, 4, 7}
+    for _ in range(3):  # capture, replay
+        outs = plan.run()
+    plan.check()
+    g = fg.signed_generalised_geodesic2d if signed else fg.generalised_geodesic2d
+    for i, (im, m, l, o) in enumerate(zip(imgs, masks, lambs, outs)):
+        ref = g(im, m, 1e10, l, 2)
+        assert torch.equal(o.view(torch.int32), ref.view(torch.int32)), (i, shapes[i], tiles.get(i))
+
+
+def test_tiled_auto_plan_large_images():
+    """The automatic plan tiles the largest images of a batch like the
+    uneven-batch workload's; every output still matches its per-call one."""
+    imgs, masks, lambs = make_batch(41, 24, (200, 2049), [1, 3])
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im in imgs]
+    plan = fg.GeodesicBatch2d(shapes * 2, signed=[False] * 24 + [True] * 24, iterations=2, use_graph=True,
+                              inputs=(imgs * 2, masks * 2))
+    plan.v, plan.lambs = 1e10, lambs * 2
+    assert plan.tiled  # the largest images run tiled
+    outs = plan.run()
+    plan.check()
+    for i, o in enumerate(outs):
+        g = fg.signed_generalised_geodesic2d if i >= 24 else fg.generalised_geodesic2d
+        ref = g(imgs[i % 24], masks[i % 24], 1e10, lambs[i % 24], 2)
+        assert torch.equal(o.view(torch.int32), ref.view(torch.int32)), (i, shapes[i % 24], plan.tiled.get(i))
