@@ -185,3 +185,27 @@ def test_tiled_auto_plan_large_images():
         g = fg.signed_generalised_geodesic2d if i >= 24 else fg.generalised_geodesic2d
         ref = g(imgs[i % 24], masks[i % 24], 1e10, lambs[i % 24], 2)
         assert torch.equal(o.view(torch.int32), ref.view(torch.int32)), (i, shapes[i % 24], plan.tiled.get(i))
+
+
+def test_tiled_degenerate_shapes():
+    """Tiled images with one row, one column, rows narrower than a halo and
+    more CTAs than strips: every CTA still meets the barriers, results match."""
+    shapes = [(1, 1, 700), (3, 600, 1), (1, 5, 7), (2, 3, 900), (1, 64, 40)]
+    rng = np.random.default_rng(17)
+    imgs, masks = [], []
+    for C, H, W in shapes:
+        imgs.append(torch.from_numpy((rng.random((1, C, H, W)) * 255).astype(np.float32)).cuda())
+        m = torch.ones((1, 1, H, W))
+        m[0, 0, H // 2, W // 2] = 0
+        masks.append(m.cuda())
+    lambs = [0.3, 0.9, 0.5, 1.0, 0.0]
+    for signed in (False, True):
+        plan = fg.GeodesicBatch2d(shapes, signed=signed, iterations=2, use_graph=False,
+                                  tiles={0: 4, 1: 8, 2: 3, 3: 16, 4: 2}, inputs=(imgs, masks))
+        plan.v, plan.lambs = 1e10, lambs
+        outs = plan.run()
+        plan.check()
+        g = fg.signed_generalised_geodesic2d if signed else fg.generalised_geodesic2d
+        for i, o in enumerate(outs):
+            ref = g(imgs[i], masks[i], 1e10, lambs[i], 2)
+            assert torch.equal(o.view(torch.int32), ref.view(torch.int32)), (shapes[i], signed)
