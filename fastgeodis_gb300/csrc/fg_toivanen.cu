@@ -180,15 +180,23 @@ __global__ void __launch_bounds__(1024, 1) fg_toivanen_kernel(const ToivArgs a) 
 // into registers.  CT: 1 for one image channel, 0 for 2-4 channels.
 constexpr int kRowAhead = 4;
 
-template <int CT>
+// VEC (rows a multiple of 4 cells, 16-byte aligned maps and image): a
+// thread's own cells are read and written four at a time (one float4 per 4
+// waves) instead of one scalar access per wave; across a warp every access
+// is a different row, so each warp instruction is 32 separate requests and
+// their number, not their bytes, bounds a wave.
+template <int CT, bool VEC>
 __global__ void __launch_bounds__(1024, 1) fg_toivanen_rows_kernel(const ToivArgs a) {
   extern __shared__ float rings[];
   constexpr int NCH = CT == 1 ? 1 : 4;
+  constexpr int WIN = VEC ? 8 : kRowAhead;  // own cells held ahead (VEC: this group of 4 and the next)
   const int C = CT == 1 ? 1 : a.C;
   const int H = a.H, W = a.W;
   float *dm = a.dist[blockIdx.x];
-  float *rd = rings;           // [H][4] latest distances of each row
-  float *ri = rings + 4 * H;   // [C][H][4] latest image values of each row
+  // the latest 4 distances and image values of each row, [4][H] and
+  // [C][4][H]: a warp's threads (consecutive rows) read consecutive words
+  float *rd = rings;
+  float *ri = rings + 4 * H;
   const int hm = threadIdx.x;  // this thread's row, in the pass's (mirrored) coordinates
   const bool row = hm < H;
   const int T = 2 * (H - 1) + W;
@@ -197,15 +205,35 @@ __global__ void __launch_bounds__(1024, 1) fg_toivanen_rows_kernel(const ToivArg
       const bool bwd = dir == 1;
       const int h = bwd ? H - 1 - hm : hm;  // the row in memory
       auto at = [&](int wm) { return (long long)h * W + (bwd ? W - 1 - wm : wm); };
-      // own old values of cells wm .. wm + kRowAhead - 1, loaded ahead
-      float dpf[kRowAhead], ipf[kRowAhead][NCH];
-#pragma unroll
-      for (int k = 0; k < kRowAhead; k++) {
-        if (row && k < W) {
-          dpf[k] = dm[at(k)];
+      // cells wm .. wm + 3 as a float4 in pass order (the memory order reversed backwards)
+      auto ld4 = [&](const float *base, int wm, float *out) {
+        const float4 v = *reinterpret_cast<const float4 *>(base + (bwd ? at(wm + 3) : at(wm)));
+        if (bwd) out[0] = v.w, out[1] = v.z, out[2] = v.y, out[3] = v.x;
+        else out[0] = v.x, out[1] = v.y, out[2] = v.z, out[3] = v.w;
+      };
+      // own old values of cells wm .. wm + WIN - 1, loaded ahead
+      float dpf[WIN], ipf[WIN][NCH], wbuf[4];
+      if (VEC) {
+        if (row) {
+          ld4(dm, 0, dpf);
 #pragma unroll
           for (int c = 0; c < NCH; c++)
-            if (c < C) ipf[k][c] = __ldg(a.img + c * a.img_cs + at(k));
+            if (c < C) {
+              float t4[4];
+              ld4(a.img + c * a.img_cs, 0, t4);
+#pragma unroll
+              for (int k = 0; k < 4; k++) ipf[k][c] = t4[k];
+            }
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kRowAhead; k++) {
+          if (row && k < W) {
+            dpf[k] = dm[at(k)];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+              if (c < C) ipf[k][c] = __ldg(a.img + c * a.img_cs + at(k));
+          }
         }
       }
       // step lengths by relative position: above-left, above, above-right, left
@@ -213,6 +241,20 @@ __global__ void __launch_bounds__(1024, 1) fg_toivanen_rows_kernel(const ToivArg
       for (int t = 0; t < T; t++) {
         const int wm = t - 2 * hm;
         if (row && wm >= 0 && wm < W) {
+          if (VEC && (wm & 3) == 0 && wm + 4 < W) {
+            // the next group of 4 behind this one
+            float t4[4];
+            ld4(dm, wm + 4, t4);
+#pragma unroll
+            for (int k = 0; k < 4; k++) dpf[4 + k] = t4[k];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+              if (c < C) {
+                ld4(a.img + c * a.img_cs, wm + 4, t4);
+#pragma unroll
+                for (int k = 0; k < 4; k++) ipf[4 + k][c] = t4[k];
+              }
+          }
           const float dold = dpf[0];
           float icur[NCH];
 #pragma unroll
@@ -220,12 +262,12 @@ __global__ void __launch_bounds__(1024, 1) fg_toivanen_rows_kernel(const ToivArg
             if (c < C) icur[c] = ipf[0][c];
           // next cell ahead
 #pragma unroll
-          for (int k = 0; k < kRowAhead - 1; k++) {
+          for (int k = 0; k < WIN - 1; k++) {
             dpf[k] = dpf[k + 1];
 #pragma unroll
             for (int c = 0; c < NCH; c++) ipf[k][c] = ipf[k + 1][c];
           }
-          if (wm + kRowAhead < W) {
+          if (!VEC && wm + kRowAhead < W) {
             dpf[kRowAhead - 1] = dm[at(wm + kRowAhead)];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
@@ -239,22 +281,32 @@ __global__ void __launch_bounds__(1024, 1) fg_toivanen_rows_kernel(const ToivArg
             if (r < 0 || x < 0 || x >= W) continue;
             float l1;
             if (CT == 1) {
-              l1 = fabsf(__fsub_rn(icur[0], ri[r * 4 + (x & 3)]));
+              l1 = fabsf(__fsub_rn(icur[0], ri[(x & 3) * H + r]));
             } else {
               l1 = 0.0f;
 #pragma unroll
               for (int c = 0; c < NCH; c++)
-                if (c < C) l1 = __fadd_rn(l1, fabsf(__fsub_rn(icur[c], ri[(c * H + r) * 4 + (x & 3)])));
+                if (c < C) l1 = __fadd_rn(l1, fabsf(__fsub_rn(icur[c], ri[(c * 4 + (x & 3)) * H + r])));
             }
             const float ld = (j == 0 || j == 2) ? r2 : one;
-            const float cur = __fadd_rn(__fadd_rn(rd[r * 4 + (x & 3)], __fmul_rn(a.le, ld)), __fmul_rn(a.lg, l1));
+            const float cur = __fadd_rn(__fadd_rn(rd[(x & 3) * H + r], __fmul_rn(a.le, ld)), __fmul_rn(a.lg, l1));
             nd = cur < nd ? cur : nd;  // std::min(new_dist, cur_dist)
           }
-          rd[hm * 4 + (wm & 3)] = nd;
+          rd[(wm & 3) * H + hm] = nd;
 #pragma unroll
           for (int c = 0; c < NCH; c++)
-            if (c < C) ri[(c * H + hm) * 4 + (wm & 3)] = icur[c];
-          dm[at(wm)] = nd;
+            if (c < C) ri[(c * 4 + (wm & 3)) * H + hm] = icur[c];
+          if (VEC) {
+            // results of cells wm - 3 .. wm, written as one float4 when a group ends
+            wbuf[0] = wbuf[1], wbuf[1] = wbuf[2], wbuf[2] = wbuf[3], wbuf[3] = nd;
+            if ((wm & 3) == 3) {
+              const float4 v = bwd ? make_float4(wbuf[3], wbuf[2], wbuf[1], wbuf[0])
+                                   : make_float4(wbuf[0], wbuf[1], wbuf[2], wbuf[3]);
+              *reinterpret_cast<float4 *>(dm + (bwd ? at(wm) : at(wm - 3))) = v;
+            }
+          } else {
+            dm[at(wm)] = nd;
+          }
         }
         __syncthreads();
       }
@@ -312,14 +364,21 @@ int launch_toivanen(const float *img, int C, int D, int H, int W, const float *s
   if (!is3d && H <= 1024 && C <= 4) {  // images: one thread per row
     const int threads = std::max(32, (H + 31) / 32 * 32);
     const size_t smem = (size_t)4 * H * (1 + C) * sizeof(float);
+    // own cells four at a time where every row starts on 16 bytes
+    bool vec = W % 4 == 0 && (reinterpret_cast<uintptr_t>(img) & 15) == 0;
+    for (int m = 0; m < nmaps; m++) vec = vec && (reinterpret_cast<uintptr_t>(maps[m]) & 15) == 0;
+    auto launch = [&](auto fn) -> cudaError_t {
+      cudaError_t e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e2 == cudaSuccess) fn<<<nmaps, threads, smem, s>>>(a);
+      return e2;
+    };
     cudaError_t e;
-    if (C == 1) {
-      e = cudaFuncSetAttribute(fg_toivanen_rows_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e == cudaSuccess) fg_toivanen_rows_kernel<1><<<nmaps, threads, smem, s>>>(a);
-    } else {
-      e = cudaFuncSetAttribute(fg_toivanen_rows_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e == cudaSuccess) fg_toivanen_rows_kernel<0><<<nmaps, threads, smem, s>>>(a);
-    }
+    // (several channels keep the scalar form: their 8-cell window of image
+    // values spills at the 64 registers of a 1024-thread CTA)
+    if (C == 1)
+      e = vec ? launch(fg_toivanen_rows_kernel<1, true>) : launch(fg_toivanen_rows_kernel<1, false>);
+    else
+      e = launch(fg_toivanen_rows_kernel<0, false>);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
     return FG_OK;

@@ -29,8 +29,9 @@ def t(a):
 
 
 # up to 1024 rows: one thread per row; taller images: the wave kernel
+# (rows of a multiple of 4 cells read and write their own cells four at a time)
 @pytest.mark.parametrize("shape", [(1, 1), (1, 37), (29, 1), (2, 3), (130, 97), (64, 200), (257, 31), (1024, 9),
-                                   (1100, 23)])
+                                   (1100, 23), (1, 4), (5, 12), (300, 128), (1024, 16), (512, 512)])
 @pytest.mark.parametrize("C", [1, 3])
 def test_2d_vs_oracle(shape, C):
     rng = np.random.default_rng(sum(shape) * 7 + C)
