@@ -139,3 +139,22 @@ def test_defaults_match_reference_signatures():
     assert inspect.signature(fg.signed_generalised_geodesic2d).parameters["iter"].default == 2
     assert inspect.signature(fg.signed_generalised_geodesic3d).parameters["iter"].default == 4
     assert list(inspect.signature(fg.GSF3d).parameters) == ["image", "softmask", "theta", "spacing", "v", "lamb", "iter"]
+
+
+def test_tiled_batch_arguments_without_launch():
+    """The tiled batch entry refuses bad arguments before any CUDA call."""
+    L = _lib.load()
+    buf = (ctypes.c_float * 64)()
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    tiles = (ctypes.c_int * 2)(4, 6)
+    need = L.fg_batch2d_tiled_scratch_bytes(2, 1000)
+    assert need >= 2 * 4 * 1000 * 8  # exchange words: 2 parities x 2 maps per cell of the longest side
+    assert L.fg_batch2d_tiled_scratch_bytes(-1, 10) == 0 and L.fg_batch2d_tiled_scratch_bytes(1, 0) == 0
+    assert L.fg_batch_geodesic2d_tiled(p, tiles, 0, 1, 100, 2, p, need, p, None) == _lib.FG_OK  # nothing to do
+    assert L.fg_batch_geodesic2d_tiled(p, tiles, 33, 1, 100, 2, p, need, p, None) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_batch_geodesic2d_tiled(p, tiles, 2, 1, 100, 2, None, need, p, None) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_batch_geodesic2d_tiled(p, tiles, 2, 5, 100, 2, p, need, p, None) == _lib.FG_ERR_UNSUPPORTED
+    assert L.fg_batch_geodesic2d_tiled(p, tiles, 2, 1, 4096, 2, p, need, p, None) == _lib.FG_ERR_UNSUPPORTED
+    assert L.fg_batch_geodesic2d_tiled(p, tiles, 2, 1, 1000, 2, p, need - 8, p, None) == _lib.FG_ERR_WORKSPACE
+    bad = (ctypes.c_int * 2)(4, 1)
+    assert L.fg_batch_geodesic2d_tiled(p, bad, 2, 1, 1000, 2, p, need, p, None) == _lib.FG_ERR_INVALID_ARGUMENT
