@@ -54,6 +54,19 @@ def test_3d_vs_oracle(shape, C):
         assert bits_equal(got, want), (shape, C, sp, lamb, it, np.abs(got - want).max())
 
 
+@pytest.mark.parametrize("shape", [(64, 128, 256)])
+def test_3d_groups_vs_oracle(shape):
+    """A volume whose waves hold more than 4096 cells (8192): a cooperative
+    group of CTAs per map with a bounded barrier between waves; plain and
+    signed."""
+    rng = np.random.default_rng(sum(shape))
+    img, m = case(rng, shape, 1)
+    got = fg.generalised_geodesic3d_toivanen(t(img), t(m), [1.0, 0.7, 1.3], 1e10, 0.6, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.toivanen3d(img, m, [1.0, 0.7, 1.3], 1e10, 0.6, 1))
+    got = fg.signed_generalised_geodesic3d_toivanen(t(img), t(m), [1.0, 1.0, 1.0], 1e10, 1.0, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.toivanen3d(img, m, [1.0, 1.0, 1.0], 1e10, 1.0, 1, signed=True))
+
+
 def test_signed_gsf_many_channels_and_soft_masks():
     rng = np.random.default_rng(31)
     img, m = case(rng, (70, 45), 5, soft=True)  # five channels: no channel limit on this path
