@@ -286,23 +286,9 @@ class GeodesicBatch2d:
             g["dev"].copy_(torch.from_numpy(g["host"].view(np.uint8).copy()), non_blocking=False)
         it = self._items_host
         for slot, (i, part) in enumerate(self.jobs):
-            C, H, W = self.shapes[i]
-            s = self._scratch[i]
-            lamb = float(self.lambs[i])
-            sg = self.signed[i]
-            it[slot]["image"] = self.images[i].data_ptr()
-            it[slot]["mask"] = self.masks[i].data_ptr()
-            it[slot]["out"] = self.outputs[i].data_ptr()
-            it[slot]["image_t"] = s["image_t"].data_ptr()
-            it[slot]["t1"] = s["t1"].data_ptr()
-            it[slot]["d2"] = s["d2"].data_ptr() if sg else 0
-            it[slot]["t2"] = s["t2"].data_ptr() if sg else 0
-            it[slot]["C"], it[slot]["H"], it[slot]["W"] = C, H, W
-            it[slot]["flags"] = (FG_BATCH_SIGNED if sg else 0) | (FG_BATCH_SPLIT if part else 0) | \
+            flags = (FG_BATCH_SIGNED if self.signed[i] else 0) | (FG_BATCH_SPLIT if part else 0) | \
                 (FG_BATCH_SECOND if part == 2 else 0)
-            it[slot]["v"] = np.float32(self.v)
-            it[slot]["l_grad"] = np.float32(lamb)
-            it[slot]["l_eucl"] = np.float32(1.0 - lamb)  # FastGeodis/__init__.py:63-65
+            self._describe(it[slot], i, flags)
         host = torch.from_numpy(it.view(np.uint8).copy())
         self._items_dev[: host.numel()].copy_(host, non_blocking=False)
 
