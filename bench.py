@@ -404,7 +404,7 @@ def run_serve_arm(args, rank, world):
         return pct, wall, peak
 
     clocks = ClockSampler(local).start()
-    pct_b, wall_b, peak_b = serve(8, 4)
+    pct_b, wall_b, peak_b = serve(16, 8)
     clk = clocks.stop()
     pct_s, wall_s, _ = serve(1, 1)
     vp_total = sum(s[4] for s in specs)
@@ -418,7 +418,7 @@ def run_serve_arm(args, rank, world):
         "config": {"workload": f"{n_req} requests, Poisson arrivals at 200/s, 70% 2D 256^2-2048^2 C 1-3, "
                                "30% 3D 64^3-256^3 spacing U[0.5,3], 1-5 clicks (r=3), 10% GSF (theta 0.5), "
                                "v 1e10, lamb 1, iterations 2",
-                   "server": "continuous batching, 8 in flight, 4 streams, 16 GB HBM budget",
+                   "server": "continuous batching, 16 in flight, 8 streams, 16 GB HBM budget",
                    "p50_ms": round(pct_b["p50"], 3), "p99_ms": round(pct_b["p99"], 3),
                    "peak_inflight": peak_b, "gvoxel_passes_per_s": round(vp_total / wall_b / 1e9, 3),
                    "per_call_path": {"p50_ms": round(pct_s["p50"], 3), "p99_ms": round(pct_s["p99"], 3),
