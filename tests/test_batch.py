@@ -61,3 +61,20 @@ def test_tiled_width():
     assert tiled_width(1968, 3) == 656 and tiled_width(1968, 3) % 4 == 0
     assert tiled_width(30, 8) == 8  # at least the halo
     assert tiled_width(2048, 2) == 1024
+
+
+def test_split_pairs_and_tiled_costs():
+    from fastgeodis_gb300.batch import _rest_bound, plan_jobs, tiled_cost
+
+    shapes = [(1, 500, 500), (3, 900, 1200), (2, 64, 64)]
+    signed = [True, True, False]
+    jobs = plan_jobs(shapes, signed, 2, sms=152, split=True)
+    assert sorted(jobs) == [(0, 1), (0, 2), (1, 1), (1, 2), (2, 0)]
+    for k, (i, p) in enumerate(jobs):
+        if p == 1:
+            assert jobs[k + 1] == (i, 2)
+    # more CTAs per strip shorten a large image's chain, with diminishing returns
+    c = [tiled_cost(3, 1544, 1968, 1, 2, k) for k in (2, 4, 8)]
+    assert c[0] > c[1] > c[2] and (c[0] - c[1]) > (c[1] - c[2])
+    # fewer SMs never make the batch's lower bound shorter
+    assert _rest_bound(shapes, signed, 2, 8) >= _rest_bound(shapes, signed, 2, 152)
