@@ -16,7 +16,7 @@ the launch from a captured CUDA graph.
 from __future__ import annotations
 
 import ctypes
-from typing import List, Optional, Sequence, Tuple, Union
+from typing import List, Sequence, Tuple, Union
 
 import numpy as np
 import torch
