@@ -34,7 +34,7 @@ EXPORTED = (
     "fg_batch2d_tiled_scratch_bytes", "fg_batch_geodesic2d_tiled",
     "fg_grad_geodesic2d_forward", "fg_grad_geodesic2d_backward",
     "fg_grad_geodesic2d_forward_pass", "fg_grad_geodesic2d_backward_pass",
-    "fg_generalised_geodesic2d_noalloc", "fg_click_mask",
+    "fg_generalised_geodesic2d_noalloc", "fg_noalloc_status", "fg_click_mask",
     "fg_generalised_geodesic2d_toivanen", "fg_generalised_geodesic3d_toivanen",
     "fg_signed_generalised_geodesic2d_toivanen", "fg_signed_generalised_geodesic3d_toivanen",
     "fg_GSF2d_toivanen", "fg_GSF3d_toivanen",
@@ -85,6 +85,7 @@ def load():
     L.fg_signed_generalised_geodesic3d.argtypes = L.fg_generalised_geodesic3d.argtypes
     L.fg_GSF2d.argtypes = [vp, i, i, i, vp, i, f, f, f, i, vp, vp, sz, vp]
     L.fg_generalised_geodesic2d_noalloc.argtypes = [vp, i, i, i, vp, i, vp, f, f, f, i, vp]
+    L.fg_noalloc_status.argtypes = [vp]
     L.fg_batch2d_smem_bytes.argtypes = [i, i, i]
     L.fg_batch2d_smem_bytes.restype = sz
     L.fg_batch_geodesic2d.argtypes = [vp, i, i, i, i, i, vp, vp, i, vp]

@@ -345,14 +345,24 @@ FG_API int fg_click_mask(float *mask, int D, int H, int W, const int *clicks, in
  * 32 * max(H, W) bytes plus about 1 KiB must fit in 16 MiB (for example C = 1 up to about 2 million pixels);
  * larger sizes return FG_ERR_UNSUPPORTED.  All calls share the array: calls
  * whose GPU work overlaps race and give wrong results, so order them on one
- * stream.  The first call on a device looks up the array's address there
- * and should come before any stream capture.  Allocates nothing (no
- * cudaMalloc / cudaFree); results are bit-identical to
- * fg_generalised_geodesic2d. */
+ * stream.  The array's address is looked up on the current device at every
+ * call made outside a stream capture (so a context re-created by
+ * cudaDeviceReset is followed); a call inside a capture reuses the last
+ * lookup, so make one call on the device before capturing.  A bounded wait
+ * that expires leaves FG_ERR_TIMEOUT in the array's status word until
+ * fg_noalloc_status reads it.  Allocates nothing (no cudaMalloc /
+ * cudaFree); results are bit-identical to fg_generalised_geodesic2d. */
 FG_API int fg_generalised_geodesic2d_noalloc(const float *image, int C, int H, int W,
                                              const float *mask, int Cm, float *out, float v,
                                              float l_grad, float l_eucl, int iterations,
                                              void *stream);
+
+/* Status of the allocation-free entry point's fixed scratch array (no
+ * counterpart in the reference): synchronises `stream`, returns FG_OK or the
+ * code a kernel of an earlier fg_generalised_geodesic2d_noalloc call left
+ * there (FG_ERR_TIMEOUT), and clears it.  The word is not cleared by the
+ * transform calls, so one check covers every call since the last one. */
+FG_API int fg_noalloc_status(void *stream);
 
 #ifdef __cplusplus
 }
