@@ -12,6 +12,12 @@ is bit-identical to :func:`fastgeodis_gb300.generalised_geodesic2d` /
 
 :class:`GeodesicBatch2d` fixes the shapes once, owns the buffers and replays
 the launch from a captured CUDA graph.
+
+Images the persistent kernel does not take -- more than four channels, or a
+side above 2048 -- are accepted too: they run through the per-call engine
+(``fg_generalised_geodesic2d`` / ``fg_signed_generalised_geodesic2d``) on a
+side stream beside the launch, outside the captured graph, with the same
+bits as a single call.
 """
 from __future__ import annotations
 
@@ -163,9 +169,8 @@ def _check_item(image: torch.Tensor, mask: torch.Tensor, device) -> None:
         raise RuntimeError("expected scalar type Float")
     if not (image.is_cuda and mask.is_cuda) or image.device != device or mask.device != device:
         raise ValueError("all batch tensors must be CUDA tensors on one device")
-    C, H, W = image.shape[1], image.shape[2], image.shape[3]
-    if C > MAX_CHANNELS or max(H, W) > MAX_SIDE:
-        raise RuntimeError(f"batched transforms handle up to {MAX_CHANNELS} channels and sides up to {MAX_SIDE}")
+    if image.size(1) < 1:
+        raise RuntimeError("batch items need at least one image channel")
 
 
 class GeodesicBatch2d:
@@ -203,8 +208,12 @@ class GeodesicBatch2d:
         else:
             self.signed = [bool(signed)] * n
         for C, H, W in self.shapes:
-            if C < 1 or C > MAX_CHANNELS or max(H, W) > MAX_SIDE or min(H, W) < 0:
+            if C < 1 or min(H, W) < 0:
                 raise RuntimeError(f"unsupported batch item shape {(C, H, W)}")
+        # images the persistent kernel does not take: the per-call engine
+        self.percall = [i for i, (C, H, W) in enumerate(self.shapes) if C > MAX_CHANNELS or max(H, W) > MAX_SIDE]
+        pc = set(self.percall)
+        batched = [i for i in range(n) if i not in pc]
         dev = self.device
         if inputs is not None:  # caller-owned tensors, used in place
             self.images, self.masks = list(inputs[0]), list(inputs[1])
@@ -213,7 +222,10 @@ class GeodesicBatch2d:
             self.masks = [torch.ones((1, 1, H, W), device=dev) for _, H, W in self.shapes]
         self.outputs = [torch.empty((1, 1, H, W), device=dev) for _, H, W in self.shapes]
         self._scratch = []
-        for (C, H, W), sg in zip(self.shapes, self.signed):
+        for i, ((C, H, W), sg) in enumerate(zip(self.shapes, self.signed)):
+            if i in pc:
+                self._scratch.append(None)
+                continue
             s = {"image_t": torch.empty((C, W, H), device=dev), "t1": torch.empty((W, H), device=dev)}
             if sg:
                 s["d2"] = torch.empty((H, W), device=dev)
@@ -222,13 +234,15 @@ class GeodesicBatch2d:
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         self.sms = sms
         if tiles == "auto":
-            self.tiled = plan_tiles(self.shapes, self.signed, self.iterations, sms)
+            sub = plan_tiles([self.shapes[i] for i in batched], [self.signed[i] for i in batched], self.iterations,
+                             sms)
+            self.tiled = {batched[i]: k for i, k in sub.items()}
         else:
             self.tiled = {int(i): int(k) for i, k in (tiles or {}).items()}
         for i, k in self.tiled.items():
-            if not (0 <= i < n) or not (2 <= k <= 16):
-                raise ValueError("tiles: {image: 2 to 16 CTAs}")
-        rest = [i for i in range(n) if i not in self.tiled]
+            if not (0 <= i < n) or not (2 <= k <= 16) or i in pc:
+                raise ValueError("tiles: {image: 2 to 16 CTAs} (images of up to 4 channels and sides up to 2048)")
+        rest = [i for i in batched if i not in self.tiled]
         sub = plan_jobs([self.shapes[i] for i in rest], [self.signed[i] for i in rest], self.iterations,
                         sms - sum(self.tiled.values()), split)
         self.jobs = [(rest[i], part) for i, part in sub]
@@ -252,8 +266,14 @@ class GeodesicBatch2d:
         self._items_dev = torch.empty(max(1, nj * ITEM_DTYPE.itemsize), dtype=torch.uint8, device=dev)
         self._counter = torch.zeros(1 + nj, dtype=torch.int32, device=dev)  # queue + one word per split image
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.max_C = max([s[0] for s in self.shapes], default=1)
-        self.max_extent = max([max(s[1], s[2]) for s in self.shapes], default=1)
+        self.max_C = max([self.shapes[i][0] for i in batched], default=1)
+        self.max_extent = max([max(self.shapes[i][1], self.shapes[i][2]) for i in batched], default=1)
+        # per-call images run one after another on one side stream: one workspace
+        L = _lib.load()
+        need = [int(L.fg_workspace_bytes(_lib.FG_OP_SIGNED if self.signed[i] else _lib.FG_OP_PLAIN, C, 1, H, W))
+                for i, (C, H, W) in enumerate(self.shapes) if i in pc]
+        self._pc_ws = torch.zeros(max(need), dtype=torch.uint8, device=dev) if need else None
+        self._pc_stream = torch.cuda.Stream(dev) if need else None
         self.v = 1e10
         self.lambs = [1.0] * n
         self._graph = None
@@ -310,6 +330,26 @@ class GeodesicBatch2d:
         for g in self._tiled_groups:
             main.wait_stream(g["stream"])
 
+    def _launch_percall(self):
+        """The images the persistent kernel does not take, through the per-call
+        engine on a side stream (not captured: it runs beside the graph)."""
+        if not self.percall:
+            return
+        L = _lib.load()
+        main = torch.cuda.current_stream(self.device)
+        side = self._pc_stream
+        side.wait_stream(main)
+        ws = self._pc_ws
+        for i in self.percall:
+            C, H, W = self.shapes[i]
+            lamb = float(self.lambs[i])
+            fn = L.fg_signed_generalised_geodesic2d if self.signed[i] else L.fg_generalised_geodesic2d
+            rc = fn(self.images[i].data_ptr(), C, H, W, self.masks[i].data_ptr(), 1, self.outputs[i].data_ptr(),
+                    float(np.float32(self.v)), lamb, 1.0 - lamb, self.iterations, ws.data_ptr(), ws.numel(),
+                    side.cuda_stream)
+            _lib.check(rc)
+        main.wait_stream(side)
+
     def run(self):
         """Compute all outputs (asynchronously on the current stream)."""
         if not self.shapes:
@@ -320,6 +360,7 @@ class GeodesicBatch2d:
                 self._fill_items()  # descriptors change only with v / lambs
                 self._graph = None
                 self._graph_key = key
+            self._launch_percall()
             if not self.use_graph:
                 self._launch()
                 return self.outputs
@@ -343,6 +384,8 @@ class GeodesicBatch2d:
         if code:
             self._status.zero_()
             raise _lib.EngineError(f"fastgeodis_gb300 batch error {code}")
+        if self._pc_ws is not None:
+            _lib.check(_lib.load().fg_workspace_status(self._pc_ws.data_ptr(), self._pc_stream.cuda_stream))
 
 
 def _as_list(x, n, name) -> List[float]:

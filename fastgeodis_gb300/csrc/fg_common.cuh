@@ -27,6 +27,7 @@ __host__ __device__ constexpr int pass_max_threads(int cross, int cimg, int maps
 }
 constexpr int kMaxMaps = 2;              // distance maps updated by one launch (they share the image)
 constexpr int kMaxChannels = 4;          // image channels held in registers
+constexpr int kWideChannels = -1;        // channel template argument of passes over more than kMaxChannels channels
 constexpr int kMaxTiles = 2048;          // tiles of one pass (all co-resident)
 constexpr int kMaxCluster = 16;          // CTAs of a cluster plan (non-portable cluster size)
 constexpr unsigned kSpinLimit = 1u << 23; // polls of one halo word (each an L2 round trip, ~0.3-1 us) before FG_ERR_TIMEOUT

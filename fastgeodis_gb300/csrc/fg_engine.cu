@@ -247,6 +247,7 @@ std::map<std::tuple<int, int, int>, std::tuple<int, int, int, int>> g_overrides;
 bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1, int rpt, bool want_lean, Plan *out) {
   const int cimg = mode == MODE_EUCLID ? 0 : C;
   if (rpt != 0 && (cimg > 1 || rpt != 2)) return false;
+  if (cimg > kMaxChannels) return false;  // wide images run on tile plans
   const int step = std::max(rpt, 1);
   T1 = std::max(1, std::min(T1, N1));
   T1 = (T1 + step - 1) / step * step;
@@ -316,7 +317,8 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     int runs = R1 * ((R2 + 3) / 4);
     if (runs > max_threads) return -1;
     int B2, rowf, nown;
-    const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
+    // image channels staged per step (wide images: none, they are read through L1)
+    const int nch = mode == MODE_EUCLID || C > kMaxChannels ? 0 : (C == 1 ? 1 : kMaxChannels);
     // deepest staging that still leaves room for a second CTA on the SM (then
     // concurrent transforms on other streams share its issue slots)
     int depth = max_pass_depth(nch, M);
@@ -598,10 +600,7 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
   axes_for(g, ax, &nax);
   const int cross = g.is3d ? 2 : 1;
   const int mode = select_mode(ms.lg, ms.le);
-  const int Cimg = mode == MODE_EUCLID ? 0 : g.C;
-  if (g.C > kMaxChannels && mode != MODE_EUCLID)
-    return fail(FG_ERR_UNSUPPORTED, "images with more than " + std::to_string(kMaxChannels) +
-                                        " channels are not supported by this build");
+  const int Cimg = mode == MODE_EUCLID ? 0 : g.C;  // any count: above kMaxChannels the wide pass variant
   const long long HW = (long long)g.H * g.W, DH = (long long)g.D * g.H;
   for (int it = 0; it < iterations; it++) {
     for (int k = 0; k < nax; k++) {
@@ -734,7 +733,7 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
     fg_unswept_kernel<<<ew_grid(n), 256, 0, s>>>(out + P, mask + P, n, v, theta, op);
     FG_CUDA(cudaGetLastError());
   }
-  if (!g.is3d && !toivanen && op != FG_OP_GSF && one_launch_image(g.H, g.W)) {
+  if (!g.is3d && !toivanen && op != FG_OP_GSF && g.C <= kMaxChannels && one_launch_image(g.H, g.W)) {
     // small images: the whole transform in one launch (its CTA runs the passes
     // back to back), with the workspace's buffers as scratch
     fg_batch2d_item it{};
@@ -807,7 +806,7 @@ namespace fgi {
 
 size_t pass_smem_bytes(int cross, int C, int M, int mode, bool wt, int S, int R1, int R2, int *B2o, int *rowfo,
                        int *nown_max, int depth) {
-  const int ci = mode == MODE_EUCLID ? 0 : C;  // image arrays staged
+  const int ci = mode == MODE_EUCLID || C > kMaxChannels ? 0 : C;  // image arrays staged (wide: none)
   const int B1 = cross == 2 ? R1 + 2 : 1, B2 = ((R2 + 3) & ~3) + 8;
   const int rowf = ring_pitch(B1 * B2);
   const int SR = wt ? S : 2;

@@ -164,9 +164,10 @@ __device__ __forceinline__ int cta_sort_position(int key, int nkeys, int *scratc
   return pos;
 }
 
-// channels staged per step and the prefetch depth (steps) of a kernel variant
+// channels staged per step and the prefetch depth (steps) of a kernel variant;
+// ct < 0 (kWideChannels): more than kMaxChannels channels, none staged
 __host__ __device__ constexpr int pass_nch(int ct, int mode) {
-  return mode == MODE_EUCLID ? 0 : (ct == 0 ? kMaxChannels : ct);
+  return mode == MODE_EUCLID || ct < 0 ? 0 : (ct == 0 ? kMaxChannels : ct);
 }
 __host__ __device__ constexpr int pass_depth(int nch, int m) { return (nch + m <= 4) ? 4 : 2; }
 
@@ -190,6 +191,19 @@ __device__ __forceinline__ void cp_async_wait() {
 // MULTI = false compiles a single-tile body (no halo exchange, no cone): the
 // batched kernels, whose CTA always owns a whole image.
 //
+// CT: image channels staged through shared memory, 1 .. 4 (0: any count up
+// to 4), or kWideChannels for images of more than 4 channels.  A wide pass
+// stages no image values (its shared memory does not grow with the channel
+// count, so every cross-section still tiles): at each step a thread reads its
+// own cells' and the previous row's image values through L1 (the neighbour
+// rows of consecutive steps overlap, so they hit) and sums the L1 distances
+// of its 3 x 3 (2D: 3) candidates x 4 cells in registers, channel 0 first --
+// the reference's summation order (fastgeodis_cpu.cpp:96-104,
+// fastgeodis_cuda.cu:170-177).  Coordinates outside the image are clamped
+// to it: such a neighbour's distance is NaN in the rings, so its candidate is
+// NaN whatever its L1 sum, and the minimum ignores it, as with staged values.
+// Tile plans only (no cluster plans, no batch or tape variants).
+//
 // CL = true: a cluster plan.  The CTAs of one thread-block cluster own strips
 // of whole rows of the cross-section (tiles1 = cluster size, tiles2 = 1, no
 // halo; `tile` is the CTA's rank).  After every step but the last, a strip's
@@ -204,6 +218,8 @@ template <int CROSS, int CT, int M, int MODE, bool WT, bool TAPE = false, bool M
 __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, float *sm) {
   const PassArgs a = ar;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
+  constexpr bool WIDE = CT < 0 && USE_IMG;  // image read through L1, not staged
+  static_assert(!(CT < 0 && (CL || TAPE || !MULTI)), "wide images run on tile plans only");
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
   const int P = a.P;                     // steps of own inputs in flight (power of 2)
@@ -212,7 +228,8 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NT = blockDim.x, nwarps = NT >> 5;
-  const int C = USE_IMG ? (CT == 0 ? a.C : CT) : 0;
+  const int C = USE_IMG && !WIDE ? (CT == 0 ? a.C : CT) : 0;  // channels staged in shared memory
+  const int CW = WIDE ? a.C : 0;                                // channels read through L1
   const int L = a.L, S = a.S, lgS = __ffs(S) - 1;  // S is a power of two
   const int SR = WT ? S : 2;                        // distance rows kept in shared memory
   const int ti1 = tile / a.tiles2, ti2 = tile - ti1 * a.tiles2;
@@ -428,6 +445,12 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         // min; an even-numbered candidate waits in pend for the next one
         float best[M][4], pend[M][4];
         unsigned code[4] = {kTapeSelf, kTapeSelf, kTapeSelf, kTapeSelf};  // TAPE: argmin of map 0
+        // wide images: columns g20 - 1 .. g20 + 4 clamped to the image
+        int colo[6];
+        if (WIDE) {
+#pragma unroll
+          for (int j = 0; j < 6; j++) colo[j] = min(max(g20 - 1 + j, 0), a.N2 - 1) - g20;
+        }
 #pragma unroll
         for (int m = 0; m < M; m++)
 #pragma unroll
@@ -445,6 +468,29 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
               const float2 ev = EDGES ? *reinterpret_cast<const float2 *>(ie0 + c * edgef + d1 * EP2)
                                       : make_float2(q[-1], q[4]);
               ip[c][0] = ev.x, ip[c][1] = v.x, ip[c][2] = v.y, ip[c][3] = v.z, ip[c][4] = v.w, ip[c][5] = ev.y;
+            }
+          }
+          // wide images: this row's L1 sums (3 columns x 4 cells), channel by
+          // channel in order, from the image in global memory
+          float l1w[3][4];
+          if (WIDE) {
+            const int g = CROSS == 2 ? min(max(g1 + d1, 0), a.N1 - 1) : g1;  // previous step's row d1, clamped
+            const long long ro = rcur - rstep + (long long)(g - g1) * a.st1;
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+#pragma unroll
+              for (int i = 0; i < 4; i++) l1w[j][i] = 0.0f;
+            for (int c = 0; c < CW; c++) {
+              const float *ic = a.img + c * a.img_cs;
+              float own[4], nb[6];
+#pragma unroll
+              for (int i = 0; i < 4; i++) own[i] = __ldg(ic + rcur + colo[i + 1]);
+#pragma unroll
+              for (int j = 0; j < 6; j++) nb[j] = __ldg(ic + ro + colo[j]);
+#pragma unroll
+              for (int j = 0; j < 3; j++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) l1w[j][i] = __fadd_rn(l1w[j][i], fabsf(__fsub_rn(own[i], nb[i + j])));
             }
           }
           float dp[M][6];
@@ -465,7 +511,9 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
               // one image channel: d = I(x) - I(y); the reference's l_grad * |d|
               // equals |l_grad * d| bit for bit (round to nearest is symmetric in sign)
               float d = 0.0f, l1 = 0.0f;
-              if (USE_IMG) {
+              if (WIDE) {
+                l1 = l1w[d2 + 1][i];
+              } else if (USE_IMG) {
                 if (CT == 1) {
                   d = __fsub_rn(f4get(icur[0], i), ip[0][i + 1 + d2]);
                   l1 = fabsf(d);
@@ -722,7 +770,7 @@ int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
 
 template <int CROSS, int CT, int M, int MODE, bool WT, bool CLU>
 int launch_regs(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
-  if constexpr (pass_lean(CROSS, CT == 0 ? kMaxChannels : CT, M)) {  // CT = 0: up to 4 channels
+  if constexpr (pass_lean(CROSS, CT <= 0 ? kMaxChannels : CT, M)) {  // CT = 0: up to 4 channels; < 0: more
     if (c.lean) return launch_variant<CROSS, CT, M, MODE, WT, true, CLU>(a, c, s);
   }
   if (c.threads > kThreads) return set_error(FG_ERR_UNSUPPORTED, "a 128-register sweep CTA has at most 512 threads");
@@ -733,6 +781,14 @@ template <int CROSS, int M, bool WT, bool CLU>
 int launch_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStream_t s) {
   const bool one = a.C == 1;
   if (mode == MODE_EUCLID) return launch_regs<CROSS, 1, M, MODE_EUCLID, WT, CLU>(a, c, s);
+  if (a.C > kMaxChannels) {
+    if constexpr (CLU) {
+      return set_error(FG_ERR_UNSUPPORTED, "images with more than 4 channels run on tile plans");
+    } else {
+      return mode == MODE_GEO ? launch_regs<CROSS, kWideChannels, M, MODE_GEO, WT, false>(a, c, s)
+                              : launch_regs<CROSS, kWideChannels, M, MODE_GENERAL, WT, false>(a, c, s);
+    }
+  }
   if (mode == MODE_GEO)
     return one ? launch_regs<CROSS, 1, M, MODE_GEO, WT, CLU>(a, c, s) : launch_regs<CROSS, 0, M, MODE_GEO, WT, CLU>(a, c, s);
   return one ? launch_regs<CROSS, 1, M, MODE_GENERAL, WT, CLU>(a, c, s)

@@ -67,9 +67,40 @@ def test_batch_rejects_bad_items():
     with pytest.raises(ValueError):
         fg.generalised_geodesic2d_batch([a], [torch.rand(1, 2, 8, 8, device="cuda")], 1e10, 1.0)
     with pytest.raises(RuntimeError):
-        fg.generalised_geodesic2d_batch([torch.rand(1, 1, 8, 4096, device="cuda")],
-                                        [torch.rand(1, 1, 8, 4096, device="cuda")], 1e10, 1.0)
+        fg.generalised_geodesic2d_batch([torch.rand(1, 1, 8, 8, device="cuda", dtype=torch.float64)],
+                                        [torch.rand(1, 1, 8, 8, device="cuda")], 1e10, 1.0)
     assert fg.generalised_geodesic2d_batch([], [], 1e10, 1.0) == []
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_takes_any_channel_count_and_side(graph):
+    """Images of more than four channels and a side above 2048 go through the
+    per-call engine beside the persistent launch: every output equals the
+    oracle's bits, plain and signed, mixed with ordinary images."""
+    from golden_cases import bits_equal
+    from oracle import oracle
+
+    rng = np.random.default_rng(40)
+    shapes = [(5, 37, 61), (1, 90, 70), (8, 50, 33), (2, 8, 2100), (3, 64, 64), (6, 2050, 6)]
+    signed = [False, True, True, False, False, True]
+    imgs = [torch.from_numpy((rng.random((1,) + s) * 255).astype(np.float32)).cuda() for s in shapes]
+    msks = []
+    for _, H, W in shapes:
+        m = np.ones((1, 1, H, W), np.float32)
+        m[0, 0, H // 2, W // 3] = 0
+        msks.append(torch.from_numpy(m).cuda())
+    lambs = [0.6, 0.3, 1.0, 0.8, 0.0, 0.5]
+    plan = fg.GeodesicBatch2d(shapes, signed=signed, iterations=2, use_graph=graph, inputs=(imgs, msks))
+    assert sorted(plan.percall) == [0, 2, 3, 5]
+    plan.v, plan.lambs = 1e10, lambs
+    for _ in range(2):
+        outs = plan.run()
+    torch.cuda.synchronize()
+    plan.check()
+    for im, m, l, sg, o in zip(imgs, msks, lambs, signed, outs):
+        f = oracle.signed2d if sg else oracle.geodesic2d
+        want = f(im[0].cpu().numpy(), m[0].cpu().numpy(), 1e10, l, 2)
+        assert bits_equal(o[0].cpu().numpy(), want), (im.shape, l, sg)
 
 
 @pytest.mark.parametrize("split", [True, False, "auto"])

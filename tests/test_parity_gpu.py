@@ -303,3 +303,45 @@ def test_small_images_run_in_one_launch_unless_plans_are_pinned():
     finally:
         _lib.check(L.fg_set_tuning(0, 0))
     fg.check_status()
+
+
+# More than four image channels: the wide pass variant (channels streamed from
+# the shared rings, L1 summed in channel order), on the planner's tiles and on
+# forced small regions (many tiles, halo hand-offs).
+@pytest.mark.parametrize("C", [5, 8])
+@pytest.mark.parametrize("region", [0, 48])
+@pytest.mark.parametrize("shape", [(64, 77), (300, 257), (1, 40), (520, 9)])
+def test_2d_wide_channels_vs_oracle(shape, C, region, tuning):
+    if region:
+        tuning(region)
+    rng = np.random.default_rng(C * 1000 + shape[0] * 7 + shape[1] + region)
+    img, m = rand_case(rng, shape, C)
+    for lamb in (0.0, 0.45, 1.0):
+        got = fg.generalised_geodesic2d(t(img), t(m), 1e10, lamb, 2)[0].cpu().numpy()
+        want = oracle.geodesic2d(img, m, 1e10, lamb, 2)
+        assert bits_equal(got, want), (shape, C, region, lamb, np.abs(got - want).max())
+    got = fg.signed_generalised_geodesic2d(t(img), t(m), 1e10, 0.7, 2)[0].cpu().numpy()
+    assert bits_equal(got, oracle.signed2d(img, m, 1e10, 0.7, 2)), (shape, C, region, "signed")
+    fg.check_status()
+
+
+@pytest.mark.parametrize("C", [5, 8])
+@pytest.mark.parametrize("region", [0, 64])
+@pytest.mark.parametrize("shape", [(9, 23, 31), (24, 40, 36), (1, 12, 17)])
+def test_3d_wide_channels_vs_oracle(shape, C, region, tuning):
+    if region:
+        tuning(region)
+    rng = np.random.default_rng(C * 1000 + sum(shape) + region)
+    img = rng.random((C,) + shape).astype(np.float32)
+    m = np.ones((1,) + shape, np.float32)
+    m[(0,) + tuple(n // 2 for n in shape)] = 0
+    sp = [1.3, 0.7, 0.9]
+    for lamb in (0.0, 0.5, 1.0):
+        got = fg.generalised_geodesic3d(t(img), t(m), sp, 1e10, lamb, 2)[0].cpu().numpy()
+        want = oracle.geodesic3d(img, m, sp, 1e10, lamb, 2)
+        assert bits_equal(got, want), (shape, C, region, lamb, np.abs(got - want).max())
+    got = fg.signed_generalised_geodesic3d(t(img), t(m), sp, 1e10, 0.3, 2)[0].cpu().numpy()
+    assert bits_equal(got, oracle.signed3d(img, m, sp, 1e10, 0.3, 2)), (shape, C, region, "signed")
+    got = fg.GSF3d(t(img), t(m), 0.5, sp, 1e10, 0.6, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.gsf3d(img, m, 0.5, sp, 1e10, 0.6, 1)), (shape, C, region, "gsf")
+    fg.check_status()
