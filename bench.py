@@ -159,7 +159,7 @@ def batch_cpu_sample(images, masks, lambs, budget_s=15.0):
     return vp / t_total / 1e9, "port", oracle.max_threads(), sample
 
 
-def run_batch_reference_arm(args, rank):
+def run_batch_reference_arm(args, rank, world=1):
     """The uneven batch on the reference's CPU path (its C restatement, all
     host threads): a bounded sample of the batch's plain + signed transforms."""
     import torch
@@ -175,7 +175,7 @@ def run_batch_reference_arm(args, rank):
     wall = time.perf_counter() - t0
     line = {
         "impl": "reference", "metric": "generalised_geodesic2d uneven batch throughput", "value": round(value, 4),
-        "unit": "Gvoxel-passes/s", "n_gpus": args.gpus, "steps": 1, "warmup": 0,
+        "unit": "Gvoxel-passes/s", "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": round(1e3 * wall, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "64 images H,W ~ U[128,2048] step 4, C in {1,3}, smoothed noise [0,255], "
@@ -603,58 +603,113 @@ def committed_traffic(workload_name):
 # CPU side: oracle / reference timing
 # ---------------------------------------------------------------------------
 
-def cpu_transform_fn(kind_pref="reference"):
-    """Returns (callable(w, lamb), kind, cores).  kind 'reference' = the
-    reference's own CPU build (where its sources were available to compile),
-    'port' = the C restatement in oracle/."""
+def reference_install(build: bool = True):
+    """The reference as its users install it: its own ``FastGeodis`` package
+    over its ``FastGeodisCpp`` extension (OpenMP CPU path, CUDA path for
+    sm_103a), assembled in baseline/_ref by oracle/build_oracle.py from the
+    reference's source files staged there.  Compiled on first use on this
+    machine when `build`; None when the sources are not present."""
+    from oracle import build_oracle
+
+    try:
+        FG = build_oracle.load_reference_install()
+        if FG is None and build and build_oracle.build_reference_install() is not None:
+            FG = build_oracle.load_reference_install()
+        return FG
+    except Exception as exc:  # a failed build leaves the port as the CPU baseline
+        print(f"reference install unavailable: {exc}", file=sys.stderr)
+        return None
+
+
+def host_threads() -> int:
+    """Every host core: the OpenMP threads of the reference's CPU path."""
+    import torch
+
+    n = os.cpu_count() or 1
+    torch.set_num_threads(n)
+    return torch.get_num_threads()
+
+
+def reference_call(FG, w):
+    """f(image, mask, lamb) through the reference's public API
+    (FastGeodis/__init__.py:37-98, :165-238) for the workload's method."""
+    tv = w.get("method") == "toivanen"
+    if w["dims"] == 3:
+        fn = FG.generalised_geodesic3d_toivanen if tv else FG.generalised_geodesic3d
+        return lambda im, m, lamb: fn(im, m, w["spacing"], w["v"], lamb, w["iters"])
+    fn = FG.generalised_geodesic2d_toivanen if tv else FG.generalised_geodesic2d
+    return lambda im, m, lamb: fn(im, m, w["v"], lamb, w["iters"])
+
+
+def cpu_transform_fn(kind_pref="reference", build=False):
+    """Returns (callable(w, lamb, k), kind, cores).  kind 'reference' = the
+    reference's own build (its installed package in baseline/_ref, else its
+    CPU sources compiled into oracle/_ref), 'port' = the C restatement in
+    oracle/.  k selects the workload's k-th (image, mask) pair."""
     from oracle import build_oracle, oracle
 
-    ref = build_oracle.load_reference() if kind_pref == "reference" else None
-    if ref is not None:
-        import torch
+    def pair(w, k):
+        return (w.get("images") or [(w["image"], w["mask"])])[k % len(w.get("images") or [0])]
 
-        cores = torch.get_num_threads()
+    if kind_pref == "reference":
+        FG = reference_install(build=build)
+        if FG is not None:
+            import torch
 
-        def f(w, lamb):
-            img = torch.from_numpy(w["image"])
-            m = torch.from_numpy(w["mask"])
-            if w.get("method") == "toivanen":  # geodis_toivanen.cpp: one thread
+            cores = host_threads()
+
+            def f(w, lamb, k=0):
+                im, m = pair(w, k)
+                return reference_call(FG, w)(torch.from_numpy(im), torch.from_numpy(m), lamb)
+
+            return f, "reference", cores
+        ref = build_oracle.load_reference()
+        if ref is not None:
+            import torch
+
+            cores = host_threads()
+
+            def f(w, lamb, k=0):
+                im, m = pair(w, k)
+                img, msk = torch.from_numpy(im), torch.from_numpy(m)
+                if w.get("method") == "toivanen":  # geodis_toivanen.cpp: one thread
+                    if w["dims"] == 3:
+                        return ref.generalised_geodesic3d_toivanen(img, msk, w["spacing"], w["v"], lamb, 1 - lamb,
+                                                                   w["iters"])
+                    return ref.generalised_geodesic2d_toivanen(img, msk, w["v"], lamb, 1 - lamb, w["iters"])
                 if w["dims"] == 3:
-                    return ref.generalised_geodesic3d_toivanen(img, m, w["spacing"], w["v"], lamb, 1 - lamb,
-                                                               w["iters"])
-                return ref.generalised_geodesic2d_toivanen(img, m, w["v"], lamb, 1 - lamb, w["iters"])
-            if w["dims"] == 3:
-                return ref.generalised_geodesic3d(img, m, w["spacing"], w["v"], lamb, 1 - lamb, w["iters"])
-            return ref.generalised_geodesic2d(img, m, w["v"], lamb, 1 - lamb, w["iters"])
+                    return ref.generalised_geodesic3d(img, msk, w["spacing"], w["v"], lamb, 1 - lamb, w["iters"])
+                return ref.generalised_geodesic2d(img, msk, w["v"], lamb, 1 - lamb, w["iters"])
 
-        return f, "reference", cores
+            return f, "reference", cores
     cores = oracle.max_threads()
 
-    def f(w, lamb):
+    def f(w, lamb, k=0):
+        im, m = pair(w, k)
         if w.get("method") == "toivanen":
             if w["dims"] == 3:
-                return oracle.toivanen3d(w["image"][0], w["mask"][0], w["spacing"], w["v"], lamb, w["iters"])
-            return oracle.toivanen2d(w["image"][0], w["mask"][0], w["v"], lamb, w["iters"])
+                return oracle.toivanen3d(im[0], m[0], w["spacing"], w["v"], lamb, w["iters"])
+            return oracle.toivanen2d(im[0], m[0], w["v"], lamb, w["iters"])
         if w["dims"] == 3:
-            return oracle.geodesic3d(w["image"][0], w["mask"][0], w["spacing"], w["v"], lamb, w["iters"])
-        return oracle.geodesic2d(w["image"][0], w["mask"][0], w["v"], lamb, w["iters"])
+            return oracle.geodesic3d(im[0], m[0], w["spacing"], w["v"], lamb, w["iters"])
+        return oracle.geodesic2d(im[0], m[0], w["v"], lamb, w["iters"])
 
     return f, "port", cores
 
 
 def time_cpu_sample(w, kind_pref="reference", max_runs=None, budget_s=20.0):
-    """Times single transforms (cycling through the workload's lambs) until
-    about `budget_s` seconds of CPU work; returns Gvp/s and a description."""
+    """Times single transforms (cycling through the workload's transforms)
+    until about `budget_s` seconds of CPU work; returns Gvp/s and a description."""
     f, kind, cores = cpu_transform_fn(kind_pref)
     if w.get("method") == "toivanen":
         cores = 1  # Toivanen's scan is sequential in the reference (and the port)
     vp_one = voxel_passes(w) / len(w["lambs"])
-    f(w, w["lambs"][0])  # warm-up (page-in, thread pool)
+    f(w, w["lambs"][0], 0)  # warm-up (page-in, thread pool)
     t_total, runs = 0.0, 0
     while True:
         lamb = w["lambs"][runs % len(w["lambs"])]
         t0 = time.perf_counter()
-        f(w, lamb)
+        f(w, lamb, runs)
         t_total += time.perf_counter() - t0
         runs += 1
         if (max_runs and runs >= max_runs) or (not max_runs and t_total >= budget_s) or runs >= 30:
@@ -664,32 +719,156 @@ def time_cpu_sample(w, kind_pref="reference", max_runs=None, budget_s=20.0):
     return value, kind, cores, sample
 
 
-def run_reference_arm(args, w, rank):
+def reference_cuda_record(FG, w, steps):
+    """The reference's own CUDA kernels (fastgeodis_cuda.cu:131-318, :407-656,
+    built for sm_103a) on the workload's step, timed with CUDA events on the
+    stream they launch on (the legacy default stream, which is torch's
+    default stream), and their difference from the oracle (the reference's
+    CPU semantics): the reference's thread blocks read neighbour cells at
+    their seams without ordering, so cells there may differ."""
+    import torch
+
+    from oracle import oracle
+
+    if w.get("method") == "toivanen" or not torch.cuda.is_available():
+        return None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    pairs = w.get("images") or [(w["image"], w["mask"])] * len(w["lambs"])
+    d_in = [(torch.from_numpy(im).to(dev), torch.from_numpy(m).to(dev)) for im, m in pairs]
+    call = reference_call(FG, w)
+
+    def step():
+        return [call(im, m, lamb) for (im, m), lamb in zip(d_in, w["lambs"])]
+
+    try:
+        step()
+        torch.cuda.synchronize()
+    except Exception as exc:  # built without its CUDA path
+        return {"unavailable": f"{type(exc).__name__}: {str(exc).splitlines()[0][:200]}"}
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    tot = 0.0
+    for k in range(steps):
+        flush.fill_(float(k))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        outs = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    ms = tot / steps
+    worst = {"max_abs_diff": 0.0, "max_rel_diff": 0.0, "cells_differing": 0, "cells_compared": 0}
+    for (im, m), lamb, o in list(zip(pairs, w["lambs"], outs))[:3]:
+        want = (oracle.geodesic3d(im[0], m[0], w["spacing"], w["v"], lamb, w["iters"]) if w["dims"] == 3
+                else oracle.geodesic2d(im[0], m[0], w["v"], lamb, w["iters"]))
+        got = o[0].cpu().numpy()
+        d = np.abs(got.astype(np.float64) - want.astype(np.float64))
+        worst["max_abs_diff"] = max(worst["max_abs_diff"], float(d.max()))
+        worst["max_rel_diff"] = max(worst["max_rel_diff"],
+                                    float((d / np.maximum(np.abs(want.astype(np.float64)), 1e-30)).max()))
+        worst["cells_differing"] += int(np.count_nonzero(got.view(np.uint32) != want.view(np.uint32)))
+        worst["cells_compared"] += int(got.size)
+    return {"value": round(voxel_passes(w) / (ms * 1e-3) / 1e9, 4), "unit": "Gvoxel-passes/s",
+            "ms_per_step": round(ms, 3), "steps": steps,
+            "timing": "CUDA events on the legacy default stream, inputs resident, L2 flushed between steps",
+            "vs_oracle": worst, "build": "the reference's fastgeodis_cuda.cu for sm_103a, nvcc defaults (FMA on)"}
+
+
+def signed_gsf_record(FG, repeats=3):
+    """The reference's signed and GSF transforms on the host cores, as it
+    calls them (fastgeodis.cpp:241-258, :319-343: the second transform of a
+    signed pair in a std::async thread) and as sequential plain calls (2 per
+    signed, 6 per GSF), on the 512^2 image of the 2D workload."""
+    import torch
+
+    w = workload("c1")
+    img, m = torch.from_numpy(w["image"]), torch.from_numpy(w["mask"])
+    lamb, it, v = 1.0, 2, 1e10
+
+    def med(fn):
+        fn()
+        ts = []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts))
+
+    def plain_pairs(n):
+        def fn():
+            for k in range(n):
+                FG.generalised_geodesic2d(img, m if k % 2 == 0 else 1 - m, v, lamb, it)
+        return fn
+
+    t_signed = med(lambda: FG.signed_generalised_geodesic2d(img, m, v, lamb, it))
+    t_2 = med(plain_pairs(2))
+    t_gsf = med(lambda: FG.GSF2d(img, m, 0.5, v, lamb, it))
+    t_6 = med(plain_pairs(6))
+    return {"image": "1x1x512x512 (the 2D workload), lamb 1.0, iterations 2", "repeats": repeats,
+            "signed2d_s": round(t_signed, 4), "two_sequential_plain_s": round(t_2, 4),
+            "GSF2d_s": round(t_gsf, 4), "six_sequential_plain_s": round(t_6, 4),
+            "note": "median seconds; the reference's signed/GSF run each pair's second transform in a std::async "
+                    "thread beside the first, two OpenMP teams on the same cores"}
+
+
+def run_reference_arm(args, w, rank, world):
+    """The reference's own implementation on the workload, on all host cores:
+    its installed package (OpenMP CPU path) where it could be built here,
+    else its CPU sources (oracle/_ref), else the C restatement."""
     if rank != 0:
         return
-    f, kind, cores = cpu_transform_fn("reference")
+    f, kind, cores = cpu_transform_fn("reference", build=True)
     if w.get("method") == "toivanen":
         cores = 1  # Toivanen's scan is sequential in the reference (and the port)
-    vp_one = voxel_passes(w) / len(w["lambs"])
-    for i in range(args.warmup):
-        f(w, w["lambs"][i % len(w["lambs"])])
+    units = [(k, lamb) for k, lamb in enumerate(w["lambs"])]
+    vp_unit = voxel_passes(w) / len(units)
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        f(w, w["lambs"][i % len(w["lambs"])])
+    f(w, units[0][1], units[0][0])  # page-in, thread pool
+    t_unit = time.perf_counter() - t0
+    # a step is the GPU arm's step (every transform of the workload) when it
+    # fits in about 4 s of CPU time, else one transform, cycling
+    whole = t_unit * len(units) <= 4.0
+    per_step = units if whole else None
+
+    def step(i):
+        todo = per_step if per_step else [units[i % len(units)]]
+        for k, lamb in todo:
+            f(w, lamb, k)
+        return len(todo)
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    done = sum(step(i) for i in range(args.steps))
     dt = time.perf_counter() - t0
-    value = vp_one * args.steps / dt / 1e9
+    value = vp_unit * done / dt / 1e9
     line = {
         "impl": "reference",
         "metric": metric_name(w), "value": round(value, 4), "unit": "Gvoxel-passes/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w["desc"], "step": "one transform per step, lamb cycling through the set"},
+        "config": {"workload": w["desc"],
+                   "step": ("every transform of the workload per step, as the GPU arm's step" if whole else
+                            "one transform per step, cycling through the workload's transforms"),
+                   "implementation": {"reference": "the reference's FastGeodis package and its FastGeodisCpp "
+                                                   "OpenMP CPU path, built on this host",
+                                      "port": "the oracle's C restatement of the reference's CPU path"}[kind]},
         "cpu_baseline": {"value": round(value, 4), "unit": "Gvoxel-passes/s", "cores": cores, "kind": kind,
-                         "sample": f"{args.steps} single transforms after {args.warmup} warm-up transforms"},
+                         "sample": f"{args.steps} steps ({done} transforms) after {args.warmup} warm-up steps"},
         "e2e": {"value": round(value, 4), "unit": "Gvoxel-passes/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    FG = reference_install(build=False) if kind == "reference" else None
+    if FG is not None:
+        try:
+            rc = reference_cuda_record(FG, w, max(1, min(args.steps, 5)))
+            if rc:
+                line["reference_cuda"] = rc
+        except Exception as exc:
+            line["reference_cuda"] = {"unavailable": f"{type(exc).__name__}: {str(exc)[:200]}"}
+        if w["name"] in ("c1", "c2") and not args.no_signed_gsf:
+            line["signed_gsf_cpu"] = signed_gsf_record(FG)
     print(json.dumps(line), flush=True)
 
 
@@ -731,6 +910,175 @@ def transform_fns(fg, w):
 # GPU arm
 # ---------------------------------------------------------------------------
 
+def smooth_noise_gpu(gen, shape, sigma, lo, hi, dev):
+    """uniform[lo, hi] noise from `gen`, Gaussian-smoothed on the device
+    (separable kernel truncated at 4 sigma, reflected borders), float32."""
+    import torch
+    import torch.nn.functional as F
+
+    x = (torch.rand(shape, generator=gen, device=dev) * (hi - lo) + lo)[None, None]
+    r = int(4 * sigma + 0.5)
+    t = torch.arange(-r, r + 1, dtype=torch.float32, device=dev)
+    k = torch.exp(-0.5 * (t / sigma) ** 2)
+    k = k / k.sum()
+    nd = len(shape)
+    conv = F.conv3d if nd == 3 else F.conv2d
+    for ax in range(nd):
+        if shape[ax] <= r:
+            continue
+        pad = [0, 0] * nd
+        pad[2 * (nd - 1 - ax)] = pad[2 * (nd - 1 - ax) + 1] = r
+        view = [1, 1] + [1] * nd
+        view[2 + ax] = 2 * r + 1
+        x = conv(F.pad(x, pad, mode="reflect"), k.view(view))
+    return x[0, 0].contiguous()
+
+
+def _max_over_ranks(x, dist, dev):
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def b256_record(args, dev, rank, world, dist, n=8, steps=5):
+    """Spec target 1 (>= 60% of the HBM roofline on 256^3): a batch of
+    8 volumes 256^3 (smoothed noise generated on the device, one 6^3 seed cube
+    each, spacing 1, iterations 4, lamb cycling 0 / 0.5 / 1), one transform per
+    volume, through GeodesicBatch3d (cluster plans pinned by the batch,
+    replayed from one CUDA graph).  Volumes are split across ranks."""
+    import torch
+
+    import fastgeodis_gb300 as fg
+    from fastgeodis_gb300.replicas import partition
+
+    shape = (256, 256, 256)
+    mine = partition([1.0] * n, world)[rank]
+    gen = torch.Generator(device=dev).manual_seed(256)
+    rng = np.random.default_rng(256)
+    imgs, msks, lambs = [], [], []
+    for k in range(n):
+        vol = smooth_noise_gpu(gen, shape, 2.0, 0.0, 1.0, dev)
+        c = [int(rng.integers(0, s - 6)) for s in shape]
+        if k not in mine:
+            continue
+        m = torch.ones(shape, device=dev)
+        m[c[0]:c[0] + 6, c[1]:c[1] + 6, c[2]:c[2] + 6] = 0.0
+        imgs.append(vol[None, None])
+        msks.append(m[None, None])
+        lambs.append([0.0, 0.5, 1.0][k % 3])
+    b = fg.GeodesicBatch3d([(1,) + shape] * len(imgs), iterations=4, use_graph=True, streams=max(1, len(imgs)),
+                           inputs=(imgs, msks), device=dev)
+    b.v, b.lambs, b.spacings = 1e10, lambs, [(1.0, 1.0, 1.0)] * len(imgs)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        b.run()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    tot = 0.0
+    for k in range(steps):
+        flush.fill_(float(k))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run()
+        e1.record(stream)
+        e1.synchronize()
+        tot += e0.elapsed_time(e1)
+    b.check()
+    plans = sorted({str(fg_plan) for fg_plan in b._pinned})
+    b.release_plans()
+    ms = _max_over_ranks(tot / steps, dist, dev)
+    del b, imgs, msks
+    torch.cuda.empty_cache()
+    vp = float(n) * float(np.prod(shape)) * 6 * 4
+    value = vp / (ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    return {"workload": "8 volumes 1x1x256x256x256, smoothed (sigma 2) uniform[0,1] noise generated on the device, "
+                        "one 6^3 seed cube each, spacing 1, v 1e10, iterations 4, lamb cycling 0/0.5/1",
+            "api": "GeodesicBatch3d, one CUDA graph per step, cluster plans pinned by the batch",
+            "plans_pinned_for": plans, "steps": steps, "ms_per_step": round(ms, 3),
+            "value": round(value, 2), "unit": "Gvoxel-passes/s",
+            "hbm_achieved_gbs": round(value * 12, 1), "hbm_frac": round(value * 12 / peak, 4),
+            "peak_gbs": peak, "peak_source": peak_kind, "target_frac": 0.6,
+            "bytes_per_voxel_pass": 12, "l2": "flushed between steps"}
+
+
+def c3_record(args, dev, rank, world, dist, steps=5):
+    """Spec target 2 (>= 5x the plain per-call drop-in on the uneven 2D
+    batch): the 64-image batch, plain and signed of every image, through
+    GeodesicBatch2d (one CUDA graph) against the same transforms called one
+    by one through the drop-in API.  Images are split across ranks."""
+    import torch
+
+    import fastgeodis_gb300 as fg
+    from fastgeodis_gb300.replicas import partition, transform_cost
+
+    items = batch_workload()
+    mine = partition([transform_cost(tuple(im.shape[2:]), 2) for im, _, _ in items], world)[rank]
+    items = [items[i] for i in mine]
+    shapes = [(im.shape[1], im.shape[2], im.shape[3]) for im, _, _ in items]
+    n = len(items)
+    plan = fg.GeodesicBatch2d(shapes + shapes, signed=[False] * n + [True] * n, iterations=2, use_graph=True,
+                              inputs=([im for im, _, _ in items] * 2, [m for _, m, _ in items] * 2))
+    plan.v, plan.lambs = 1e10, [l for _, _, l in items] * 2
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def per_call():
+        for im, m, l in items:
+            fg.generalised_geodesic2d(im, m, 1e10, l, 2)
+            fg.signed_generalised_geodesic2d(im, m, 1e10, l, 2)
+
+    def timed(fn, k_steps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        tot = 0.0
+        for k in range(k_steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return _max_over_ranks(tot / k_steps, dist, dev)
+
+    ms_b = timed(plan.run, steps)
+    plan.check()
+    ms_p = timed(per_call, 2)
+    fg.check_status()
+    tiled = len(plan.tiled)
+    del plan
+    torch.cuda.empty_cache()
+    vp_all = _sum_over_ranks(float(sum(s[1] * s[2] for s in shapes)) * 4 * 2 * 3, dist, dev)
+    return {"workload": "64 images H,W ~ U[128,2048] step 4, C in {1,3}, smoothed noise [0,255], 1-10 seed disks, "
+                        "lamb ~ U[0,1], iterations 2; plain and signed of every image",
+            "api": "GeodesicBatch2d (one persistent launch + tiled launch, one CUDA graph) vs the per-call drop-in",
+            "tiled_images": tiled, "steps": steps,
+            "batched_ms_per_step": round(ms_b, 3), "batched_value": round(vp_all / (ms_b * 1e-3) / 1e9, 2),
+            "per_call_ms_per_step": round(ms_p, 3), "per_call_value": round(vp_all / (ms_p * 1e-3) / 1e9, 2),
+            "speedup_vs_per_call": round(ms_p / ms_b, 2), "target_speedup": 5.0, "unit": "Gvoxel-passes/s",
+            "l2": "flushed between steps"}
+
+
+def _sum_over_ranks(x, dist, dev):
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def run_gpu_arm(args, w, rank, world):
     import torch
 
@@ -745,6 +1093,14 @@ def run_gpu_arm(args, w, rank, world):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
+    # a batch of independent volumes is split across ranks (no collective on
+    # the data path); a single-image workload is replicated on every rank
+    vp_all = voxel_passes(w) * (1 if w.get("images") else world)
+    if w.get("images") and world > 1:
+        from fastgeodis_gb300.replicas import partition
+
+        mine = partition([float(np.prod(im.shape)) for im, _ in w["images"]], world)[rank]
+        w = dict(w, images=[w["images"][i] for i in mine], lambs=[w["lambs"][i] for i in mine])
     # inputs of the step's transforms: one (image, mask) per transform, or the
     # workload's one image for all (several lambs of one image)
     pairs = w.get("images") or [(w["image"], w["mask"])] * len(w["lambs"])
@@ -801,6 +1157,10 @@ def run_gpu_arm(args, w, rank, world):
             main.wait_stream(s)
         return outs
 
+    # clocks sampled across all of this arm's GPU work (warm-up, timed steps,
+    # end-to-end leg and the records below): the timed steps alone are too
+    # short for nvidia-smi's sampling period
+    clocks = ClockSampler(local).start()
     nvtx = torch.cuda.nvtx  # ranges let a profiler select the timed launches (ncu --nvtx-include timed/)
     nvtx.range_push("warmup")
     for _ in range(args.warmup):
@@ -815,7 +1175,6 @@ def run_gpu_arm(args, w, rank, world):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local).start()
     _lib.profile_begin()
     t0 = time.perf_counter()
     for k in range(args.steps):
@@ -830,7 +1189,6 @@ def run_gpu_arm(args, w, rank, world):
     pass_ms, pass_launches, pass_vp = _lib.profile_end()
     if dist:
         dist.barrier()
-    clk = clocks.stop()
     fg.check_status()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = float(np.sum(step_ms) / args.steps)
@@ -839,9 +1197,10 @@ def run_gpu_arm(args, w, rank, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     vp_step = voxel_passes(w)
-    value = world * vp_step / (ms * 1e-3) / 1e9
+    value = vp_all / (ms * 1e-3) / 1e9
 
     if args.kernels_only:
+        clocks.stop()
         if rank == 0:
             print(json.dumps({"kernels_only": True, "ms_per_step": round(ms, 4), "pass_launches": pass_launches}))
         return
@@ -868,7 +1227,7 @@ def run_gpu_arm(args, w, rank, world):
         b.check()
         gm = float(np.mean(g_ms))
         graph_batch = {"api": f"GeodesicBatch3d, {len(d_in)} streams, one CUDA graph per step",
-                       "ms_per_step": round(gm, 4), "value": round(world * vp_step / (gm * 1e-3) / 1e9, 4)}
+                       "ms_per_step": round(gm, 4), "value": round(vp_all / (gm * 1e-3) / 1e9, 4)}
     # end to end through the public API with host buffers (pinned): every call
     # copies its inputs to the device and returns its result in host memory.
     # The step's calls are independent, so each is issued from its own host
@@ -910,6 +1269,36 @@ def run_gpu_arm(args, w, rank, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     pool.shutdown()
+
+    # the dominant kernel timed alone: one transform of the step (the middle
+    # lamb) on one stream, every pass launch bracketed by CUDA events, so the
+    # roofline below divides by the kernel's own duration (in the step above
+    # three transforms share the SMs)
+    alone = None
+    if w.get("method") != "toivanen" and not (w["dims"] == 2 and max(w["image"].shape[2:]) <= _one_launch_side()):
+        ka = len(w["lambs"]) // 2
+        im_a, mk_a = d_in[ka]
+        n_alone = max(3, min(args.steps, 10))
+        for _ in range(2):
+            f3(im_a, mk_a, w["spacing"], w["v"], w["lambs"][ka], w["iters"]) if w["dims"] == 3 else \
+                f2(im_a, mk_a, w["v"], w["lambs"][ka], w["iters"])
+        torch.cuda.synchronize()
+        _lib.profile_begin()
+        for k in range(n_alone):
+            flush.fill_(float(k))
+            if w["dims"] == 3:
+                f3(im_a, mk_a, w["spacing"], w["v"], w["lambs"][ka], w["iters"])
+            else:
+                f2(im_a, mk_a, w["v"], w["lambs"][ka], w["iters"])
+        torch.cuda.synchronize()
+        a_ms, a_launches, a_vp = _lib.profile_end()
+        alone = {"lamb": w["lambs"][ka], "transforms": n_alone, "pass_ms": a_ms, "launches": a_launches, "vp": a_vp}
+    extra = {}
+    if w["name"] == "c2" and not args.no_extras:
+        # the benchmark spec's targets, measured in the same run (outside the timed steps)
+        extra["b256"] = b256_record(args, dev, rank, world, dist)
+        extra["c3"] = c3_record(args, dev, rank, world, dist)
+    clk = clocks.stop()
     n_calls = len(w["lambs"])
     h2d = sum((im.numel() + mk.numel()) * 4 for im, mk in h_in)
     d2h = sum(mk.numel() * 4 for _, mk in h_in)
@@ -923,11 +1312,17 @@ def run_gpu_arm(args, w, rank, world):
     bytes_per_vp = 4 * w["C"] + 8
     avg_launch_ms = pass_ms / max(pass_launches, 1)
     alg_bytes_launch = pass_vp / max(pass_launches, 1) * bytes_per_vp
-    achieved = alg_bytes_launch / (avg_launch_ms * 1e-3) / 1e9
+    achieved_step = alg_bytes_launch / (avg_launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     traffic = committed_traffic(w["name"])
+    if alone:
+        avg_alone = alone["pass_ms"] / max(alone["launches"], 1)
+        bytes_alone = alone["vp"] / max(alone["launches"], 1) * bytes_per_vp
+        achieved = bytes_alone / (avg_alone * 1e-3) / 1e9
+    else:
+        avg_alone, bytes_alone, achieved = avg_launch_ms, alg_bytes_launch, achieved_step
     init_launches = n_calls * args.steps  # v*mask initialisation, one per transform
-    cpu_val, cpu_kind, cpu_cores, cpu_sample = time_cpu_sample(w, "port", budget_s=args.cpu_budget)
+    cpu_val, cpu_kind, cpu_cores, cpu_sample = time_cpu_sample(w, "reference", budget_s=args.cpu_budget)
     f64 = None
     if w.get("method") != "toivanen":
         # the transform of the step with the middle lamb, against the float64 scan
@@ -955,22 +1350,75 @@ def run_gpu_arm(args, w, rank, world):
                    **({"fp64_check": f64} if f64 else {})},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum per launch from an ncu "
+                                        "capture committed in profiles/traffic.json, not measured in this run"
+                                        if traffic else None),
                      "kernel": sweep_kernel_name(w, tuned),
-                     "avg_launch_ms": round(avg_launch_ms, 5),
-                     "alg_bytes_per_launch": int(alg_bytes_launch), "peak_source": peak_kind,
+                     "avg_launch_ms": round(avg_alone, 5),
+                     "alg_bytes_per_launch": int(bytes_alone), "peak_source": peak_kind,
+                     "measured": ("one transform of the step (lamb %s) alone on one stream, %d launches, CUDA events "
+                                  "around each launch" % (alone["lamb"], alone["launches"]) if alone else
+                                  "the timed steps' launches"),
+                     "in_step": {"avg_launch_ms": round(avg_launch_ms, 5), "achieved": round(achieved_step, 1),
+                                 "frac": round(achieved_step / peak, 4),
+                                 "note": "launches of the timed steps, where the step's transforms share the SMs"},
                      "pass_time_share": round(pass_ms / (ms * args.steps), 4),
-                     "achieved_aggregate": round(pass_vp * bytes_per_vp / (ms * args.steps * 1e-3) / 1e9, 1)},
+                     "achieved_aggregate": round(pass_vp * bytes_per_vp / (ms * args.steps * 1e-3) / 1e9, 1),
+                     "frac_aggregate": round(pass_vp * bytes_per_vp / (ms * args.steps * 1e-3) / 1e9 / peak, 4)},
         "cpu_baseline": {"value": round(cpu_val, 4), "unit": "Gvoxel-passes/s", "cores": cpu_cores,
                          "kind": cpu_kind, "sample": cpu_sample},
-        "e2e": {"value": round(world * vp_step / e2e_s / 1e9, 4), "unit": "Gvoxel-passes/s",
+        "e2e": {"value": round(vp_all / e2e_s / 1e9, 4), "unit": "Gvoxel-passes/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": f"public API with pinned host tensors, {n_calls} calls per step from {n_calls} host threads"},
         "clocks": clk,
         "gpu_launches": int((pass_launches + init_launches) / args.steps),
+        **({"north_star": extra} if extra else {}),
     }
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def spawn_ranks(n: int, argv) -> int:
+    """Re-launch this script as n ranks on this node (torch.distributed.run,
+    one process per GPU, rendezvous on 127.0.0.1); returns its exit code.
+    NCCL's own log stays on (NCCL_DEBUG=INFO unless set), so the ranks of
+    every communicator are visible on stderr."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *argv]
+    env = dict(os.environ)
+    env.setdefault("NCCL_DEBUG", "INFO")
+    return subprocess.call(cmd, env=env)
+
+
+def run_dry(args, rank, world):
+    """The multi-rank plumbing without the workload: process group (NCCL on
+    GPUs, gloo without), barrier, the max-over-ranks reduction of a per-rank
+    time, and rank 0's line with the world size."""
+    import torch
+    import torch.distributed as dist
+
+    t = float(rank + 1)
+    if world > 1:
+        gpu = torch.cuda.is_available() and torch.cuda.device_count() >= world and args.impl == "ours"
+        if gpu:
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl" if gpu else "gloo")
+        dist.barrier()
+        x = torch.tensor([t], device="cuda" if gpu else "cpu")
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+        dist.destroy_process_group()
+    if rank == 0:
+        line = {"dry_run": True, "n_gpus": world, "max_over_ranks": t}
+        if args.impl == "reference":
+            line["impl"] = "reference"
+        print(json.dumps(line), flush=True)
 
 
 def main():
@@ -988,30 +1436,44 @@ def main():
     ap.add_argument("--plans", default=None, help="pin plans from this JSON file (from --save-plans) instead of tuning")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run warm-up and timed GPU steps only (no end-to-end or CPU legs): for profiler captures")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the north-star records (batch of 256^3 volumes, uneven 2D batch) of the default run")
+    ap.add_argument("--no-signed-gsf", action="store_true",
+                    help="reference arm: skip the signed / GSF timings of the reference's CPU path")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="only the multi-rank plumbing (spawn, rendezvous, max over ranks): no workload")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: launched here when the caller did not use torchrun
+        sys.exit(spawn_ranks(args.gpus, sys.argv[1:]))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.dry_run:
+        run_dry(args, rank, world)
+        return
     if args.workload == "c5":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the reference has no server"}))
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no server"}))
             return
         run_serve_arm(args, rank, world)
         return
     if args.workload == "c4":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradient"}))
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradient"}))
             return
         run_grad_arm(args, rank, world)
         return
     if args.workload == "c3":
         if args.impl == "reference":
-            run_batch_reference_arm(args, rank)
+            run_batch_reference_arm(args, rank, world)
             return
         run_batch_arm(args, rank, world)
         return
     w = workload(args.workload)
     if args.impl == "reference":
-        run_reference_arm(args, w, rank)
+        run_reference_arm(args, w, rank, world)
         return
     run_gpu_arm(args, w, rank, world)
 

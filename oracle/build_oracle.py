@@ -12,8 +12,23 @@ Two artefacts are produced here; neither is part of the shipped product:
   ``setup.py``.  It only exists where the reference source tree is mounted and
   is used to generate the committed golden vectors under ``tests/golden/``.
 
+The unmodified reference as its users install it -- its ``FastGeodis``
+Python package over a ``FastGeodisCpp`` extension with the OpenMP CPU path
+and the CUDA path (``WITH_CUDA``, kernels built for sm_103a) -- is assembled
+in ``baseline/_ref/`` (git-ignored, the slot of the reference install) for the
+benchmark's reference arm:
+
+* :func:`stage_reference` copies the files of the reference's source
+  distribution (its ``MANIFEST.in``: ``FastGeodis/*.{py,cpp,cu,h}`` and the
+  header-only ``dependency/fmm``) into ``baseline/_ref/src`` where the
+  reference tree is mounted, so that they travel with the working copy;
+* :func:`build_reference_install` compiles them on the machine that runs them
+  (``g++`` for the C++ files, ``nvcc`` for ``fastgeodis_cuda.cu`` with the
+  compiler's defaults, as the reference's ``setup.py`` would) into
+  ``baseline/_ref/FastGeodisCpp*.so`` and copies the Python package beside it.
+
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
-may load these libraries.
+and reference arm may load these libraries.
 """
 from __future__ import annotations
 
@@ -113,6 +128,114 @@ def build_reference(ref_root: str = DEFAULT_REF_ROOT, force: bool = False,
     return out
 
 
+ROOT = os.path.dirname(HERE)
+INSTALL_DIR = os.path.join(ROOT, "baseline", "_ref")
+STAGE_DIR = os.path.join(INSTALL_DIR, "src")
+INSTALL_MODULE = "FastGeodisCpp"
+
+
+def stage_reference(ref_root: str = DEFAULT_REF_ROOT) -> str | None:
+    """Copy the reference's source-distribution files into baseline/_ref/src
+    (git-ignored).  Returns the staged root, or None without a reference tree."""
+    import shutil
+
+    src_dir = os.path.join(ref_root, "FastGeodis")
+    if not os.path.isdir(src_dir):
+        return None
+    dst = os.path.join(STAGE_DIR, "FastGeodis")
+    os.makedirs(dst, exist_ok=True)
+    for f in sorted(os.listdir(src_dir)):
+        if f.endswith((".py", ".cpp", ".cu", ".h")):
+            shutil.copyfile(os.path.join(src_dir, f), os.path.join(dst, f))
+    fmm = os.path.join(ref_root, "dependency", "fmm", "include")
+    if os.path.isdir(fmm):
+        shutil.copytree(fmm, os.path.join(STAGE_DIR, "dependency", "fmm", "include"), dirs_exist_ok=True)
+    return STAGE_DIR
+
+
+def install_module_path() -> str:
+    return os.path.join(INSTALL_DIR, INSTALL_MODULE + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_reference_install(force: bool = False, verbose: bool = False, cuda: bool = True) -> str | None:
+    """Compile the staged reference (or the mounted tree) into the extension
+    module ``FastGeodisCpp`` under baseline/_ref and copy its Python package
+    there.  The compile follows what the reference's setup.py asks of
+    torch.utils.cpp_extension: the C++ files with OpenMP and ``WITH_CUDA``,
+    ``fastgeodis_cuda.cu`` with nvcc's defaults (FMA contraction on) for
+    sm_103a.  Returns the module path, or None when no sources are present."""
+    import shutil
+
+    root = STAGE_DIR if os.path.isdir(os.path.join(STAGE_DIR, "FastGeodis")) else DEFAULT_REF_ROOT
+    src_dir = os.path.join(root, "FastGeodis")
+    if not os.path.isdir(src_dir):
+        return None
+    import torch
+    from torch.utils import cpp_extension
+
+    out = install_module_path()
+    cpp = sorted(os.path.join(src_dir, f) for f in os.listdir(src_dir) if f.endswith(".cpp"))
+    cu = sorted(os.path.join(src_dir, f) for f in os.listdir(src_dir) if f.endswith(".cu")) if cuda else []
+    pkg = os.path.join(INSTALL_DIR, "FastGeodis")
+    os.makedirs(pkg, exist_ok=True)
+    for f in os.listdir(src_dir):
+        if f.endswith(".py"):
+            shutil.copyfile(os.path.join(src_dir, f), os.path.join(pkg, f))
+    if not force and _newer(out, *(cpp + cu)):
+        return out
+    tmp = os.path.join(INSTALL_DIR, "_obj")
+    os.makedirs(tmp, exist_ok=True)
+    abi = int(torch._C._GLIBCXX_USE_CXX11_ABI)
+    cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    inc = [f"-I{p}" for p in cpp_extension.include_paths()]
+    inc += [f"-I{os.path.join(cuda_home, 'include')}", f"-I{sysconfig.get_paths()['include']}", f"-I{src_dir}",
+            f"-I{os.path.join(root, 'dependency')}"]
+    defs = ["-DTORCH_API_INCLUDE_EXTENSION_H", f"-DTORCH_EXTENSION_NAME={INSTALL_MODULE}",
+            f"-D_GLIBCXX_USE_CXX11_ABI={abi}", "-DAT_PARALLEL_OPENMP=1"] + (["-DWITH_CUDA"] if cu else [])
+
+    def compile_one(src: str) -> str:
+        obj = os.path.join(tmp, os.path.basename(src) + ".o")
+        if src.endswith(".cu"):
+            nvcc = os.path.join(cuda_home, "bin", "nvcc")
+            cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
+                   *cpp_extension.COMMON_NVCC_FLAGS, *defs, *inc, "-c", src, "-o", obj]
+        else:
+            cmd = ["g++", "-O2", "-g0", "-std=c++17", "-fPIC", "-fopenmp", *defs, *inc, "-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.check_call(cmd)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(compile_one, cpp + cu))
+    lib_dir = os.path.join(os.path.dirname(torch.__file__), "lib")
+    libs = ["-lc10", "-ltorch", "-ltorch_cpu", "-ltorch_python"]
+    if cu:
+        libs += ["-lc10_cuda", "-ltorch_cuda", f"-L{os.path.join(cuda_home, 'lib64')}", "-lcudart"]
+    link = ["g++", "-shared", "-fopenmp", *objs, "-o", out + ".tmp", f"-L{lib_dir}", *libs,
+            f"-Wl,-rpath,{lib_dir}"]
+    if verbose:
+        print(" ".join(link), flush=True)
+    subprocess.check_call(link)
+    os.replace(out + ".tmp", out)
+    shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
+def load_reference_install():
+    """Import the reference's own Python package over its built extension
+    (``import FastGeodis`` from baseline/_ref); None if it was not built."""
+    if not os.path.exists(install_module_path()):
+        return None
+    import torch  # noqa: F401  (loads libtorch before the extension)
+
+    if INSTALL_DIR not in sys.path:
+        sys.path.insert(0, INSTALL_DIR)
+    import FastGeodis  # the reference's FastGeodis/__init__.py
+
+    return FastGeodis
+
+
 def load_reference():
     """Import the compiled reference CPU module (None if it was not built)."""
     path = reference_module_path()
@@ -128,5 +251,9 @@ def load_reference():
 
 
 if __name__ == "__main__":
-    print(build_port(force="--force" in sys.argv, verbose=True))
-    print(build_reference(force="--force" in sys.argv, verbose=True))
+    force = "--force" in sys.argv
+    print(build_port(force=force, verbose=True))
+    print(build_reference(force=force, verbose=True))
+    if "--install" in sys.argv:  # the reference as installed, for the benchmark's reference arm
+        print(stage_reference())
+        print(build_reference_install(force=force, verbose=True))
