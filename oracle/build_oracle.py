@@ -1,11 +1,14 @@
 """Build recipes for the CPU oracle (test infrastructure only).
 
-Two artefacts are produced here; neither is part of the shipped product:
+Three artefacts are produced here; none is part of the shipped product:
 
 * ``oracle/_build/libfg_oracle.so`` -- the plain-C restatement of FastGeodis'
   raster scan (``oracle/fg_oracle.c``), compiled with ``gcc`` and OpenMP.  It
   runs on any host (x86 container or the Arm GPU host) and is the parity
   checker and the timed CPU baseline.
+* ``oracle/_ref/libfg_fastmarch.so`` -- the fast-marching accuracy harness
+  (``oracle/fg_fastmarch.cpp``) over the reference's vendored solver header
+  (``dependency/fmm``), compiled where that header is available.
 * ``oracle/_ref/fastgeodis_ref_cpu*.so`` -- the reference's own CPU sources
   (``FastGeodis/*.cpp`` of masadcv/FastGeodis 1.0.5), compiled file by file with
   ``g++`` against the installed torch headers, without running the reference's
@@ -236,6 +239,39 @@ def load_reference_install():
     return FastGeodis
 
 
+FMM_SRC = os.path.join(HERE, "fg_fastmarch.cpp")
+FMM_LIB = os.path.join(REF_DIR, "libfg_fastmarch.so")
+
+
+def fmm_include_dir() -> str | None:
+    """The reference's vendored fast-marching header (dependency/fmm/include):
+    in the mounted reference tree, else in its staged copy."""
+    for root in (DEFAULT_REF_ROOT, STAGE_DIR):
+        d = os.path.join(root, "dependency", "fmm", "include")
+        if os.path.isfile(os.path.join(d, "thinks", "fast_marching_method", "fast_marching_method.hpp")):
+            return d
+    return None
+
+
+def build_fastmarch(force: bool = False, verbose: bool = False) -> str | None:
+    """Compile the fast-marching accuracy harness (oracle/fg_fastmarch.cpp over
+    the reference's vendored solver header) into oracle/_ref; None when the
+    header is not available."""
+    inc = fmm_include_dir()
+    if inc is None:
+        return None
+    hdr = os.path.join(inc, "thinks", "fast_marching_method", "fast_marching_method.hpp")
+    if not force and _newer(FMM_LIB, FMM_SRC, hdr):
+        return FMM_LIB
+    os.makedirs(REF_DIR, exist_ok=True)
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", f"-I{inc}", FMM_SRC, "-o", FMM_LIB + ".tmp"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(FMM_LIB + ".tmp", FMM_LIB)
+    return FMM_LIB
+
+
 def load_reference():
     """Import the compiled reference CPU module (None if it was not built)."""
     path = reference_module_path()
@@ -254,6 +290,7 @@ if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_port(force=force, verbose=True))
     print(build_reference(force=force, verbose=True))
+    print(build_fastmarch(force=force, verbose=True))
     if "--install" in sys.argv:  # the reference as installed, for the benchmark's reference arm
         print(stage_reference())
         print(build_reference_install(force=force, verbose=True))
