@@ -993,10 +993,35 @@ def b256_record(args, dev, rank, world, dist, n=8, steps=5):
     plans = sorted({str(fg_plan) for fg_plan in b._pinned})
     b.release_plans()
     ms = _max_over_ranks(tot / steps, dist, dev)
-    del b, imgs, msks
+    streamed = [o.clone() for o in b.outputs]
+    del b
+    # the same batch in one persistent launch (a job queue over co-resident clusters)
+    pb = fg.PersistentBatch3d([(1,) + shape] * len(imgs), iterations=4, use_graph=True, inputs=(imgs, msks),
+                              device=dev)
+    pb.v, pb.lambs, pb.spacings = 1e10, lambs, [(1.0, 1.0, 1.0)] * len(imgs)
+    for _ in range(2):
+        pb.run()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    tot1 = 0.0
+    for k in range(steps):
+        flush.fill_(float(k))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pb.run()
+        e1.record(stream)
+        e1.synchronize()
+        tot1 += e0.elapsed_time(e1)
+    pb.check()
+    same = all(torch.equal(a.view(torch.int32), o.view(torch.int32)) for a, o in zip(streamed, pb.outputs))
+    ms1 = _max_over_ranks(tot1 / steps, dist, dev)
+    pinfo = dict(pb.info)
+    del pb, imgs, msks, streamed
     torch.cuda.empty_cache()
     vp = float(n) * float(np.prod(shape)) * 6 * 4
     value = vp / (ms * 1e-3) / 1e9
+    value1 = vp / (ms1 * 1e-3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     return {"workload": "8 volumes 1x1x256x256x256, smoothed (sigma 2) uniform[0,1] noise generated on the device, "
                         "one 6^3 seed cube each, spacing 1, v 1e10, iterations 4, lamb cycling 0/0.5/1",
@@ -1005,7 +1030,12 @@ def b256_record(args, dev, rank, world, dist, n=8, steps=5):
             "value": round(value, 2), "unit": "Gvoxel-passes/s",
             "hbm_achieved_gbs": round(value * 12, 1), "hbm_frac": round(value * 12 / peak, 4),
             "peak_gbs": peak, "peak_source": peak_kind, "target_frac": 0.6,
-            "bytes_per_voxel_pass": 12, "l2": "flushed between steps"}
+            "bytes_per_voxel_pass": 12, "l2": "flushed between steps",
+            "one_launch": {"api": "PersistentBatch3d: every volume's prologue and passes in one job queue, one "
+                                  "persistent launch of co-resident clusters, one CUDA graph per step",
+                           "ms_per_step": round(ms1, 3), "value": round(value1, 2),
+                           "hbm_frac": round(value1 * 12 / peak, 4), "launch": pinfo,
+                           "bits_equal_to_streamed": bool(same)}}
 
 
 def c3_record(args, dev, rank, world, dist, steps=5):

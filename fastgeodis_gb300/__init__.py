@@ -35,6 +35,7 @@ __all__ = [
     "generalised_geodesic2d_batch",
     "signed_generalised_geodesic2d_batch",
     "GeodesicBatch3d",
+    "PersistentBatch3d",
     "generalised_geodesic3d_batch",
     "signed_generalised_geodesic3d_batch",
     "generalised_geodesic2d",
@@ -329,5 +330,6 @@ def GSF3d_toivanen(image: torch.Tensor, softmask: torch.Tensor, theta: float, sp
 
 
 from .batch import GeodesicBatch2d, generalised_geodesic2d_batch, signed_generalised_geodesic2d_batch  # noqa: E402
-from .batch3d import GeodesicBatch3d, generalised_geodesic3d_batch, signed_generalised_geodesic3d_batch  # noqa: E402
+from .batch3d import (GeodesicBatch3d, PersistentBatch3d, generalised_geodesic3d_batch,  # noqa: E402
+                      signed_generalised_geodesic3d_batch)
 from .autograd import generalised_geodesic2d_differentiable  # noqa: E402

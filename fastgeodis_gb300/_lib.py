@@ -38,6 +38,7 @@ EXPORTED = (
     "fg_generalised_geodesic2d_toivanen", "fg_generalised_geodesic3d_toivanen",
     "fg_signed_generalised_geodesic2d_toivanen", "fg_signed_generalised_geodesic3d_toivanen",
     "fg_GSF2d_toivanen", "fg_GSF3d_toivanen",
+    "fg_batch3d_job_bytes", "fg_batch3d_plan", "fg_batch3d_launch", "fg_batch3d_capacity",
 )
 
 _lib = None
@@ -97,6 +98,11 @@ def load():
     L.fg_grad_geodesic2d_forward_pass.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.fg_grad_geodesic2d_backward_pass.argtypes = [vp, i, i, i, i, i, i, vp, vp]
     L.fg_GSF3d.argtypes = [vp, i, i, i, i, vp, i, f, fp, f, f, i, vp, vp, sz, vp]
+    L.fg_batch3d_job_bytes.argtypes = []
+    L.fg_batch3d_job_bytes.restype = sz
+    L.fg_batch3d_plan.argtypes = [vp, i, i, i, vp, vp, sz, ctypes.POINTER(ctypes.c_int)]
+    L.fg_batch3d_launch.argtypes = [vp, i, i, i, i, i, i, sz, vp, vp, vp]
+    L.fg_batch3d_capacity.argtypes = [i, i, i, i, sz, ctypes.POINTER(ctypes.c_int)]
     for name in ("fg_generalised_geodesic2d", "fg_generalised_geodesic3d", "fg_signed_generalised_geodesic2d",
                  "fg_signed_generalised_geodesic3d", "fg_GSF2d", "fg_GSF3d"):
         getattr(L, name + "_toivanen").argtypes = getattr(L, name).argtypes  # same arguments

@@ -219,6 +219,185 @@ class GeodesicBatch3d:
                 _lib.check(L.fg_workspace_status(ws.data_ptr(), int(s.cuda_stream)))
 
 
+class _Item3d(ctypes.Structure):
+    """fg_batch3d_item (include/fastgeodis_gb300.h)."""
+    _fields_ = [("image", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("image_t", ctypes.c_void_p), ("t1", ctypes.c_void_p), ("d2", ctypes.c_void_p),
+                ("t2", ctypes.c_void_p), ("C", ctypes.c_int), ("D", ctypes.c_int), ("H", ctypes.c_int),
+                ("W", ctypes.c_int), ("flags", ctypes.c_int), ("v", ctypes.c_float), ("l_grad", ctypes.c_float),
+                ("l_eucl", ctypes.c_float), ("spacing", ctypes.c_float * 3), ("reserved1", ctypes.c_float)]
+
+
+FG_BATCH_SIGNED = 1
+CLUSTER_SIZES = (16, 8, 4, 2, 1)
+
+
+class PersistentBatch3d:
+    """A batch of volumes in ONE persistent launch (fg_batch3d_plan /
+    fg_batch3d_launch).
+
+    Every volume's transform is a chain of jobs in one queue -- initial
+    distances and the transposed image, its passes in order, and for the
+    signed form the difference -- and the launch holds as many thread-block
+    clusters as the device co-schedules; each cluster runs one job at a time
+    (a pass: the cross-section's rows split into strips over the cluster's
+    CTAs, rows exchanged through distributed shared memory), a job starting
+    once its volume's previous one has finished.  Volumes of any sizes that
+    fit a cluster; per volume the result is bit-identical to
+    :func:`fastgeodis_gb300.generalised_geodesic3d` /
+    :func:`fastgeodis_gb300.signed_generalised_geodesic3d`.
+
+    Args:
+        shapes: list of ``(C, D, H, W)``; C = 1 (the cluster body reads one
+            image channel; C > 1 is accepted when every lamb is 0).
+        signed: every volume signed, or every volume plain.
+        iterations: raster-scan iterations (the reference's ``iter``).
+        device: CUDA device.
+        use_graph: replay the launch from a captured CUDA graph.
+        inputs: optional caller-owned ``(images, masks)`` lists, used in place.
+        cluster_size: CTAs per cluster (1-16); default: the largest size whose
+            co-resident clusters still number at least the volumes, else the
+            smallest that holds every cross-section.
+
+    Fill ``images[i]`` / ``masks[i]`` (in place), set ``v`` / ``lambs`` /
+    ``spacings``, call :meth:`run`; results are in ``outputs[i]``.
+    """
+
+    def __init__(self, shapes: Sequence[Sequence[int]], signed: bool = False, iterations: int = 4, device=None,
+                 use_graph: bool = True, inputs=None, cluster_size: Optional[int] = None):
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.signed = bool(signed)
+        self.iterations = int(iterations)
+        self.shapes = [tuple(int(x) for x in s) for s in shapes]
+        for s in self.shapes:
+            if len(s) != 4 or min(s) < 1:
+                raise ValueError(f"batch item shapes are (C, D, H, W) with positive extents, got {s}")
+        n = len(self.shapes)
+        dev = self.device
+        L = _lib.load()
+        with torch.cuda.device(dev):
+            if inputs is not None:
+                self.images, self.masks = list(inputs[0]), list(inputs[1])
+            else:
+                self.images = [torch.zeros((1,) + s, device=dev) for s in self.shapes]
+                self.masks = [torch.ones((1, 1) + s[1:], device=dev) for s in self.shapes]
+            self.outputs = [torch.empty((1, 1) + s[1:], device=dev) for s in self.shapes]
+            self._scratch = []
+            for C, D, H, W in self.shapes:
+                sc = {"image_t": torch.empty((C, W, D, H), device=dev), "t1": torch.empty((W, D, H), device=dev)}
+                if self.signed:
+                    sc["d2"] = torch.empty((D, H, W), device=dev)
+                    sc["t2"] = torch.empty((W, D, H), device=dev)
+                self._scratch.append(sc)
+            self._counters = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+            self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.job_bytes = int(L.fg_batch3d_job_bytes())
+        self.v = 1e10
+        self.lambs = [0.5] * n
+        self.spacings = [(1.0, 1.0, 1.0)] * n
+        self.use_graph = bool(use_graph)
+        self._graph = None
+        self._key = None
+        self._jobs = None
+        self.info = None
+        self.cluster_size = int(cluster_size) if cluster_size else None
+
+    def _items(self):
+        items = (_Item3d * max(1, len(self.shapes)))()
+        for i, (C, D, H, W) in enumerate(self.shapes):
+            sc = self._scratch[i]
+            it = items[i]
+            it.image, it.mask, it.out = self.images[i].data_ptr(), self.masks[i].data_ptr(), self.outputs[i].data_ptr()
+            it.image_t, it.t1 = sc["image_t"].data_ptr(), sc["t1"].data_ptr()
+            it.d2 = sc["d2"].data_ptr() if self.signed else None
+            it.t2 = sc["t2"].data_ptr() if self.signed else None
+            it.C, it.D, it.H, it.W = C, D, H, W
+            it.flags = FG_BATCH_SIGNED if self.signed else 0
+            lamb = float(self.lambs[i])
+            it.v, it.l_grad, it.l_eucl = float(self.v), lamb, 1.0 - lamb  # FastGeodis/__init__.py:93-96
+            for k in range(3):
+                it.spacing[k] = float(self.spacings[i][k])
+        return items
+
+    def _plan_with(self, items, G):
+        L = _lib.load()
+        n = len(self.shapes)
+        cap = max(1, n * (2 + 6 * max(self.iterations, 0)))
+        buf = (ctypes.c_ubyte * (cap * self.job_bytes))()
+        info = (ctypes.c_int * 5)()
+        rc = L.fg_batch3d_plan(items, n, self.iterations, G, self._status.data_ptr(), buf, len(buf), info)
+        return rc, buf, [int(x) for x in info]
+
+    def _plan(self):
+        """Job records for the current v / lambs / spacings, copied to the device."""
+        L = _lib.load()
+        items = self._items()
+        sizes = [self.cluster_size] if self.cluster_size else list(CLUSTER_SIZES)
+        fits = []
+        for G in sizes:
+            rc, buf, info = self._plan_with(items, G)
+            if rc == _lib.FG_OK:
+                fits.append((G, buf, info))
+            elif self.cluster_size:
+                _lib.check(rc)
+        if not fits:
+            raise _lib.EngineError("no cluster size holds every cross-section of this batch: " + _lib.last_error())
+        choice = fits[-1]  # the smallest size that holds every cross-section
+        n = len(self.shapes)
+        with torch.cuda.device(self.device):
+            for G, buf, info in fits:  # largest first: enough co-resident clusters for every volume
+                c = ctypes.c_int()
+                _lib.check(L.fg_batch3d_capacity(info[3], info[4], G, info[1], info[2], ctypes.byref(c)))
+                if c.value >= n:
+                    choice = (G, buf, info)
+                    break
+            G, buf, info = choice
+            host = torch.frombuffer(bytearray(bytes(buf)[: info[0] * self.job_bytes]), dtype=torch.uint8)
+            self._jobs = host.to(self.device) if info[0] else torch.zeros(1, dtype=torch.uint8, device=self.device)
+        self.cluster_size_used = G
+        self.info = {"jobs": info[0], "threads": info[1], "smem": info[2], "maps": info[3], "mode": info[4],
+                     "cluster_size": G}
+
+    def _launch(self):
+        L = _lib.load()
+        i = self.info
+        rc = L.fg_batch3d_launch(self._jobs.data_ptr(), i["jobs"], len(self.shapes), i["maps"], i["mode"],
+                                 i["cluster_size"], i["threads"], i["smem"], self._counters.data_ptr(),
+                                 self._status.data_ptr(), int(torch.cuda.current_stream(self.device).cuda_stream))
+        _lib.check(rc)
+
+    def run(self):
+        """Compute all outputs (asynchronously on the current stream)."""
+        if not self.shapes:
+            return self.outputs
+        with torch.cuda.device(self.device):
+            key = (float(self.v), tuple(float(x) for x in self.lambs),
+                   tuple(tuple(float(y) for y in s) for s in self.spacings))
+            if key != self._key:
+                self._plan()  # the job records hold v, the weights and the step lengths
+                self._graph = None
+                self._key = key
+            if not self.use_graph:
+                self._launch()
+                return self.outputs
+            if self._graph is None:
+                self._launch()  # outside capture first: kernel attributes, cluster capacity
+                torch.cuda.synchronize(self.device)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._launch()
+                self._graph = g
+            self._graph.replay()
+            return self.outputs
+
+    def check(self) -> None:
+        """Synchronise and raise if a wait of the launch ran out (its results are void)."""
+        code = int(self._status.item())
+        if code:
+            self._status.zero_()
+            raise _lib.EngineError(f"fastgeodis_gb300 batch3d error {code}")
+
+
 def _as_list(x, n, name) -> list:
     if isinstance(x, (list, tuple)) and len(x) > 0 and isinstance(x[0], (list, tuple)):
         if len(x) != n:

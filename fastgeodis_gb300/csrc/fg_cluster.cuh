@@ -32,8 +32,11 @@
 
 namespace fgi {
 
-template <int CT, int M, int MODE, bool WT, int RPT>
+// WTT: 0 / 1 the transposed write off / on at compile time, 2 read from a.wt
+// (the batched volume kernel, whose jobs mix both).
+template <int CT, int M, int MODE, int WTT, int RPT>
 __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
+  const bool WT = WTT == 2 ? a.wt != 0 : WTT == 1;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
@@ -347,7 +350,7 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
 template <int CT, int M, int MODE, bool WT, int RPT>
 __global__ void __launch_bounds__(512) fg_sweep_cluster_kernel(const PassArgs a) {
   extern __shared__ __align__(16) float sm[];
-  cluster_body<CT, M, MODE, WT, RPT>(a, sm);
+  cluster_body<CT, M, MODE, WT ? 1 : 0, RPT>(a, sm);
 }
 
 }  // namespace fgi

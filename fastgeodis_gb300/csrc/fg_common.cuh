@@ -62,6 +62,7 @@ struct PassArgs {
   int rowf;                       // floats per ring row (ring_pitch: 4 mod 32)
   int vec;                        // runs may use 16-byte global loads and stores
   int P;                          // steps of own inputs staged ahead (2, 4 or 8)
+  int wt;                         // the pass writes transposed (read by kernels that take it at run time)
   // Halo exchange between tiles: 64-bit words [2 parities][kMaxMaps][N1*N2],
   // each a cell's distance bits (low half) and the epoch of the chunk whose
   // last row it holds (high half).  One aligned 64-bit access carries both,

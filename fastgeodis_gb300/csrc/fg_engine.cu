@@ -34,6 +34,7 @@
 #include <tuple>
 #include <vector>
 
+#include "fg_batch3d.cuh"
 #include "fg_common.cuh"
 
 namespace fgi {
@@ -587,14 +588,17 @@ void axes_for(const Geometry &g, Axis *ax, int *nax) {
   *nax = 3;
 }
 
-// Runs `iterations` of the full pass sequence on the maps of `ms`, whose
-// original-layout planes hold the initial distances.  img_r / img_t: the image
-// in the original and the transposed layout.
-int run_transform(const Geometry &g, const float *img_r, const float *img_t, const MapSet &ms, int iterations,
-                  Workspace &w, unsigned *launch_counter, cudaStream_t s) {
+// The pass sequence of `iterations` iterations on the maps of `ms`, whose
+// original-layout planes hold the initial distances (img_r / img_t: the image
+// in the original and the transposed layout), in launch order: for each pass
+// and group of at most kMaxMaps maps, `plan_fn(cross, N1, N2, Cimg, M, mode,
+// wt, &plan)` picks the plan and `emit(args, plan, cross, M, mode, wt)` gets
+// the pass's arguments (all but the halo exchange fields).  Returns the first
+// non-FG_OK code of either.
+template <typename PlanFn, typename Emit>
+int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, const MapSet &ms, int iterations,
+                  PlanFn plan_fn, Emit emit) {
   if (g.P == 0 || iterations <= 0) return FG_OK;
-  DeviceInfo di = device_info();
-  if (!di.ok) return fail(FG_ERR_CUDA, "cannot query the current CUDA device");
   Axis ax[3];
   int nax = 0;
   axes_for(g, ax, &nax);
@@ -612,16 +616,11 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
         const bool to_r = A.transposed && dir < 0;
         const bool wt = to_t || to_r;
         if (A.L <= 1 && !wt) continue;
-        if (*launch_counter >= 0xFFFFu) {  // epochs would repeat: clear the exchange words
-          FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
-          *launch_counter = 0;
-        }
         for (int m0 = 0; m0 < ms.M; m0 += kMaxMaps) {
           const int M = std::min(kMaxMaps, ms.M - m0);
           Plan p;
-          if (!make_plan(cross, A.N1, A.N2, Cimg, M, mode, wt, std::min(di.sms, kMaxTiles), &p))
-            return fail(FG_ERR_UNSUPPORTED, "no tiling for a cross-section of " + std::to_string(A.N1) + "x" +
-                                                std::to_string(A.N2));
+          int rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, wt, &p);
+          if (rc != FG_OK) return rc;
           PassArgs a{};
           a.img = A.transposed ? img_t : img_r;
           a.img_cs = g.P;
@@ -668,17 +667,41 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
                   (reinterpret_cast<uintptr_t>(a.ddst[m]) & 15) == 0;
           a.vec = vec ? 1 : 0;
           a.P = p.P;
-          a.xch = w.xch;
-          a.epoch_base = (*launch_counter) << 16;  // chunk epochs of this launch: base + 1 ... base + L/S
-          a.status = w.status;
-          (*launch_counter)++;
-          int rc = launch_pass(a, p, cross, M, mode, wt, s);
+          a.wt = wt ? 1 : 0;
+          rc = emit(a, p, cross, M, mode, wt);
           if (rc != FG_OK) return rc;
         }
       }
     }
   }
   return FG_OK;
+}
+
+// Runs `iterations` of the full pass sequence on the maps of `ms`, one launch
+// per pass on the planner's tiles (or a pinned plan).
+int run_transform(const Geometry &g, const float *img_r, const float *img_t, const MapSet &ms, int iterations,
+                  Workspace &w, unsigned *launch_counter, cudaStream_t s) {
+  if (g.P == 0 || iterations <= 0) return FG_OK;
+  DeviceInfo di = device_info();
+  if (!di.ok) return fail(FG_ERR_CUDA, "cannot query the current CUDA device");
+  auto plan_fn = [&](int cross, int N1, int N2, int Cimg, int M, int mode, bool wt, Plan *p) {
+    if (!make_plan(cross, N1, N2, Cimg, M, mode, wt, std::min(di.sms, kMaxTiles), p))
+      return fail(FG_ERR_UNSUPPORTED, "no tiling for a cross-section of " + std::to_string(N1) + "x" +
+                                          std::to_string(N2));
+    return FG_OK;
+  };
+  auto emit = [&](PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt) {
+    if (*launch_counter >= 0xFFFFu) {  // epochs would repeat: clear the exchange words
+      FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
+      *launch_counter = 0;
+    }
+    a.xch = w.xch;
+    a.epoch_base = (*launch_counter) << 16;  // chunk epochs of this launch: base + 1 ... base + L/S
+    a.status = w.status;
+    (*launch_counter)++;
+    return launch_pass(a, p, cross, M, mode, wt, s);
+  };
+  return for_each_pass(g, img_r, img_t, ms, iterations, plan_fn, emit);
 }
 
 int check_common(const float *image, int C, int D, int H, int W, const float *mask, int Cm, const float *out) {
@@ -1056,6 +1079,159 @@ int fg_GSF3d_toivanen(const float *image, int C, int D, int H, int W, const floa
   const float le = 1.0f - lambda;
   return run_op(FG_OP_GSF, g, image, mask, Cm, out, v, lambda, le, theta, iterations, workspace, workspace_bytes,
                 stream, true);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// a batch of volumes in one persistent launch (fg_batch3d.cu)
+// ---------------------------------------------------------------------------
+
+size_t fg_batch3d_job_bytes(void) { return sizeof(fgi::Batch3dJob); }
+
+int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int cluster_size, int *status, void *jobs,
+                    size_t jobs_bytes, int *info) {
+  using namespace fgi;
+  if (n < 0 || iterations < 0 || cluster_size < 1 || cluster_size > kMaxCluster || !info || (n > 0 && !items))
+    return fail(FG_ERR_INVALID_ARGUMENT, "batch3d plan: bad arguments");
+  const int G = cluster_size;
+  const bool sg = n > 0 && (items[0].flags & FG_BATCH_SIGNED);
+  const int M = sg ? 2 : 1;
+  // the launch's arithmetic: the mode every volume shares, else the general
+  // expression (exact for all of them)
+  int lmode = -1;
+  for (int v = 0; v < n; v++) {
+    const fg_batch3d_item &it = items[v];
+    if (((it.flags & FG_BATCH_SIGNED) != 0) != sg)
+      return fail(FG_ERR_INVALID_ARGUMENT, "batch3d plan: every volume must be plain, or every volume signed");
+    if (it.C < 1 || it.D < 1 || it.H < 1 || it.W < 1)
+      return fail(FG_ERR_INVALID_ARGUMENT, "batch3d plan: volumes need at least one channel and one cell");
+    if (!it.image || !it.mask || !it.out || !it.image_t || !it.t1 || (sg && (!it.d2 || !it.t2)))
+      return fail(FG_ERR_INVALID_ARGUMENT, "batch3d plan: null buffer");
+    const int mode = select_mode(it.l_grad, it.l_eucl);
+    if (mode != MODE_EUCLID && it.C != 1)
+      return fail(FG_ERR_UNSUPPORTED, "batch3d plan: volumes read at most one image channel");
+    if ((long long)it.D * it.H * it.W * std::max(it.C, 1) >= (1LL << 31))
+      return fail(FG_ERR_UNSUPPORTED, "batch3d plan: tensors of 2^31 or more elements are not supported");
+    lmode = lmode < 0 ? mode : (lmode == mode ? mode : MODE_GENERAL);
+  }
+  if (lmode < 0) lmode = MODE_GENERAL;
+  const int cimg = lmode == MODE_EUCLID ? 0 : 1;  // image channels the launch's body stages
+  std::vector<Batch3dJob> out;
+  int threads = 32;
+  for (int v = 0; v < n; v++) {
+    const fg_batch3d_item &it = items[v];
+    Geometry g;
+    int rc = geom3d(it.C, it.D, it.H, it.W, it.spacing, &g);
+    if (rc != FG_OK) return rc;
+    MapSet ms{M, {it.out, it.d2, nullptr, nullptr}, {it.t1, it.t2, nullptr, nullptr}, it.l_grad, it.l_eucl};
+    int seq = 0;
+    Batch3dJob pro{};
+    pro.kind = JOB3_PROLOGUE;
+    pro.vol = v;
+    pro.seq = seq++;
+    pro.image = it.image;
+    pro.image_t = cimg ? it.image_t : nullptr;
+    pro.mask = it.mask;
+    pro.out = it.out;
+    pro.d2 = sg ? it.d2 : nullptr;
+    pro.C = it.C, pro.D = it.D, pro.H = it.H, pro.W = it.W;
+    pro.v = it.v;
+    pro.is_signed = sg ? 1 : 0;
+    out.push_back(pro);
+    auto plan_fn = [&](int, int N1, int N2, int, int, int, bool, Plan *p) {
+      int T1 = (N1 + G - 1) / G;
+      T1 = (T1 + 1) & ~1;  // two runs per thread: whole row pairs
+      const int rpr = (N2 + 3) / 4;
+      const int nt = std::max(32, ((T1 / 2) * rpr + 31) / 32 * 32);
+      if (nt > kThreads)
+        return fail(FG_ERR_UNSUPPORTED, "batch3d plan: a cross-section of " + std::to_string(N1) + "x" +
+                                            std::to_string(N2) + " does not fit a cluster of " + std::to_string(G) +
+                                            " CTAs");
+      const int B2 = 4 * rpr + 8;
+      *p = Plan{T1, N2, 0, 0, (N1 + T1 - 1) / T1, 1, 8, nt, B2, ring_pitch((T1 + 2) * B2), 8, 0, false, true, 2};
+      threads = std::max(threads, nt);
+      return FG_OK;
+    };
+    auto emit = [&](PassArgs &a, const Plan &, int, int, int mode, bool wt) {
+      Batch3dJob j{};
+      a.xch = nullptr;
+      a.epoch_base = 0;
+      a.status = status;
+      j.a = a;
+      j.kind = JOB3_PASS;
+      j.mode = mode;
+      j.wt = wt ? 1 : 0;
+      j.vol = v;
+      j.seq = seq++;
+      out.push_back(j);
+      return FG_OK;
+    };
+    rc = for_each_pass(g, it.image, it.image_t, ms, iterations, plan_fn, emit);
+    if (rc != FG_OK) return rc;
+    if (sg) {
+      Batch3dJob epi = pro;
+      epi.kind = JOB3_EPILOGUE;
+      epi.seq = seq++;
+      out.push_back(epi);
+    }
+  }
+  // staging depth and flush period of each pass for the launch's CTA size
+  size_t smem = 32 * 33 * 4;  // the prologue's transpose tile
+  for (Batch3dJob &j : out) {
+    if (j.kind != JOB3_PASS) continue;
+    PassArgs &a = j.a;
+    bool fit = false;
+    for (int S = j.wt ? 8 : 8; S >= 2 && !fit; S = j.wt ? S / 2 : 0) {
+      for (int P = 8; P >= 2 && !fit; P /= 2) {
+        const ClusterLayout ly = cluster_layout(cimg, M, j.wt ? S : 2, a.T1, a.N2, threads, 2, P, j.wt != 0);
+        if ((size_t)ly.bytes <= kSmemBudget) {
+          a.S = S;
+          a.P = P;
+          smem = std::max(smem, (size_t)ly.bytes);
+          fit = true;
+        }
+      }
+    }
+    if (!fit) return fail(FG_ERR_UNSUPPORTED, "batch3d plan: a pass's rings do not fit the shared memory");
+  }
+  // queue order: by position in the chains, larger volumes first at each position
+  std::stable_sort(out.begin(), out.end(), [&](const Batch3dJob &x, const Batch3dJob &y) {
+    if (x.seq != y.seq) return x.seq < y.seq;
+    const long long cx = (long long)items[x.vol].D * items[x.vol].H * items[x.vol].W;
+    const long long cy = (long long)items[y.vol].D * items[y.vol].H * items[y.vol].W;
+    if (cx != cy) return cx > cy;
+    return x.vol < y.vol;
+  });
+  info[0] = (int)out.size();
+  info[1] = threads;
+  info[2] = (int)smem;
+  info[3] = M;
+  info[4] = lmode;
+  if (out.size() * sizeof(Batch3dJob) > jobs_bytes || (!jobs && !out.empty()))
+    return fail(FG_ERR_WORKSPACE, "batch3d plan: the job buffer holds " + std::to_string(jobs_bytes) +
+                                      " bytes, the batch needs " + std::to_string(out.size() * sizeof(Batch3dJob)));
+  if (!out.empty()) memcpy(jobs, out.data(), out.size() * sizeof(Batch3dJob));
+  return FG_OK;
+}
+
+int fg_batch3d_launch(const void *jobs, int njobs, int n, int maps, int mode, int cluster_size, int threads,
+                      size_t smem, unsigned *counters, int *status, void *stream) {
+  if (njobs < 0 || n < 0 || (njobs > 0 && (!jobs || !counters || !status)))
+    return fail(FG_ERR_INVALID_ARGUMENT, "batch3d launch: bad arguments");
+  if (smem > kSmemBudget) return fail(FG_ERR_INVALID_ARGUMENT, "batch3d launch: shared memory too large");
+  if (njobs == 0) return FG_OK;
+  std::lock_guard<std::mutex> g(g_launch_mu);
+  return fgi::launch_batch3d(static_cast<const fgi::Batch3dJob *>(jobs), njobs, n, maps, mode, cluster_size, threads,
+                             smem, counters, status, static_cast<cudaStream_t>(stream));
+}
+
+int fg_batch3d_capacity(int maps, int mode, int cluster_size, int threads, size_t smem, int *clusters) {
+  if (!clusters) return fail(FG_ERR_INVALID_ARGUMENT, "batch3d capacity: null output");
+  std::lock_guard<std::mutex> g(g_launch_mu);
+  return fgi::batch3d_capacity(maps, mode, cluster_size, threads, smem, clusters);
 }
 
 }  // extern "C"

@@ -280,6 +280,56 @@ FG_API int fg_batch_geodesic2d_tiled(const fg_batch2d_item *items, const int *ti
                                      int iterations, void *scratch, size_t scratch_bytes, int *status,
                                      void *stream);
 
+/* One volume of a batch run in one persistent launch (fg_batch3d_plan /
+ * fg_batch3d_launch; no counterpart in the reference, which transforms one
+ * volume per call).  Device pointers, float32, contiguous. */
+typedef struct fg_batch3d_item {
+  const float *image; /* [C][D][H][W] */
+  const float *mask;  /* [D][H][W] soft mask (one channel) */
+  float *out;         /* [D][H][W] result: D(mask), or D(mask) - D(1 - mask) when signed */
+  float *image_t;     /* scratch [C][W][D][H] */
+  float *t1;          /* scratch [W][D][H] */
+  float *d2;          /* scratch [D][H][W] (signed only) */
+  float *t2;          /* scratch [W][D][H] (signed only) */
+  int C, D, H, W;
+  int flags;          /* FG_BATCH_SIGNED, the same for every item of a batch */
+  float v, l_grad, l_eucl;
+  float spacing[3];   /* (z, y, x), as the drop-in's spacing */
+  float reserved1;
+} fg_batch3d_item;
+
+/* Batched generalised_geodesic3d / signed_generalised_geodesic3d in ONE
+ * persistent launch (no counterpart in the reference).  Every volume's
+ * transform becomes a chain of jobs -- initial distances and the transposed
+ * image copy, its passes in order, and for the signed form the difference --
+ * in one queue; the launch holds as many thread-block clusters of
+ * `cluster_size` CTAs (1-16) as the device co-schedules, and each cluster
+ * runs one job at a time (a pass: the cross-section's rows split into strips
+ * over the cluster, rows exchanged through distributed shared memory), a job
+ * starting once its volume's previous job has finished.  Results are
+ * bit-identical to fg_generalised_geodesic3d / fg_signed_generalised_geodesic3d.
+ * Volumes read at most one image channel (C = 1, or l_grad = 0); a
+ * cross-section must fit the cluster (at most 512 threads of 2 x 4 cells per
+ * CTA).
+ *
+ * fg_batch3d_plan builds the job records on the host into `jobs` (host
+ * memory, `jobs_bytes` bytes; fg_batch3d_job_bytes() each, at most
+ * n * (2 + 6 * iterations) jobs) and writes info[0] = jobs, info[1] =
+ * threads per CTA, info[2] = shared-memory bytes per CTA, info[3] = maps per
+ * pass, info[4] = arithmetic mode of the launch; `status` is the device word
+ * a wait that runs out writes FG_ERR_TIMEOUT to.  FG_ERR_WORKSPACE when
+ * `jobs_bytes` is too small (info[0] then holds the jobs needed).
+ * fg_batch3d_launch runs the jobs after they were copied to device memory
+ * (`jobs`), with `counters` device memory of (n + 1) 32-bit words that it
+ * clears on `stream` first; capturable in a CUDA graph. */
+FG_API size_t fg_batch3d_job_bytes(void);
+FG_API int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int cluster_size, int *status,
+                           void *jobs, size_t jobs_bytes, int *info);
+FG_API int fg_batch3d_launch(const void *jobs, int njobs, int n, int maps, int mode, int cluster_size, int threads,
+                             size_t smem, unsigned *counters, int *status, void *stream);
+/* How many clusters of that shape the launch co-schedules on the current device. */
+FG_API int fg_batch3d_capacity(int maps, int mode, int cluster_size, int threads, size_t smem, int *clusters);
+
 /* One image of a differentiable 2D transform (fg_grad_geodesic2d_forward /
  * _backward; no counterpart in the reference, which is not differentiable).
  * Device pointers, float32 unless noted, contiguous; scratch belongs to the
