@@ -120,6 +120,7 @@ __global__ void __maxnreg__(128) fg_batch3d_kernel(const Batch3dJob *jobs, int n
       s_claim[0] = j;
       s_claim[1] = ok;
     }
+    __syncwarp();  // the cluster barrier is .aligned: warp 0 converges after its first thread's wait
     cl_sync();
     const unsigned a0 = cl_map(smem_u32(s_claim), 0);
     const int j = ld_cluster_s32(a0);

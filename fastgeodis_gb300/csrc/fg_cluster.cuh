@@ -89,14 +89,15 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
   const bool push_dn = rank < G - 1 && k_dn >= 0 && k_dn < RPT && ((vmask >> (4 * k_dn)) & 0xFu) != 0;
   const unsigned rsm_up = push_up ? cl_map(lsm, rank - 1) : 0u;
   const unsigned rsm_dn = push_dn ? cl_map(lsm, rank + 1) : 0u;
-  const bool waits = tid == 0 || (active && (rf == 0 || rf + RPT >= T1));  // the window reads an apron row
+  // a strip with no neighbour (one strip) never waits: its mbarriers stay unused
+  const bool waits = G > 1 && (tid == 0 || (active && (rf == 0 || rf + RPT >= T1)));  // the window reads an apron row
   bool dead = false;
   if (tid == 0) {
     mbar_init(cbar, 1);
     mbar_init(cbar + 8, 1);
     mbar_fence_init();
-    if (L >= 2) mbar_expect(cbar, cl_bytes);      // step 0
-    if (L >= 3) mbar_expect(cbar + 8, cl_bytes);  // step 1
+    if (G > 1 && L >= 2) mbar_expect(cbar, cl_bytes);      // step 0
+    if (G > 1 && L >= 3) mbar_expect(cbar + 8, cl_bytes);  // step 1
   }
   cl_sync();  // rings filled and mbarriers armed in every CTA before the first push
 
@@ -345,6 +346,12 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
   }
   cp_async_wait<0>();
   cl_sync();  // no CTA leaves while a neighbour may still address its shared memory
+  // the mbarriers' memory may serve other data next (a kernel running several
+  // passes in turn): invalidate them first, as an mbarrier object requires
+  if (tid == 0) {
+    mbar_inval(cbar);
+    mbar_inval(cbar + 8);
+  }
 }
 
 template <int CT, int M, int MODE, bool WT, int RPT>

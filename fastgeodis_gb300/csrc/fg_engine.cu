@@ -1205,6 +1205,13 @@ int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int clu
     if (cx != cy) return cx > cy;
     return x.vol < y.vol;
   });
+  static const bool debug = getenv("FASTGEODIS_GB300_DEBUG_PLAN") != nullptr;
+  if (debug)
+    for (const Batch3dJob &j : out)
+      fprintf(stderr, "[fg batch3d] kind=%d vol=%d seq=%d mode=%d wt=%d L=%d dir=%d N=%dx%d T1=%d tiles1=%d S=%d P=%d "
+                      "s_str=%lld st1=%lld ws=%lld,%lld,%lld vec=%d\n",
+              j.kind, j.vol, j.seq, j.mode, j.wt, j.a.L, j.a.dir, j.a.N1, j.a.N2, j.a.T1, j.a.tiles1, j.a.S, j.a.P,
+              j.a.s_str, j.a.st1, j.a.ws_str, j.a.wst1, j.a.wst2, j.a.vec);
   info[0] = (int)out.size();
   info[1] = threads;
   info[2] = (int)smem;

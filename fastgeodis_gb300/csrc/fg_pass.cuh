@@ -88,6 +88,9 @@ __device__ __forceinline__ void mbar_init(unsigned a, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
 }
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_inval(unsigned a) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(a) : "memory");
+}
 // one arrival that also expects `tx` bytes of asynchronous stores in this phase
 __device__ __forceinline__ void mbar_expect(unsigned a, unsigned tx) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(tx) : "memory");
