@@ -92,7 +92,16 @@ __device__ void run_epilogue(const Batch3dJob &jb, unsigned rank, unsigned G) {
 // The transposed write is read from the job (one body, no spills).
 template <int M, int MODE>
 __device__ void run_pass(const Batch3dJob &jb, float *sm, unsigned rank) {
-  const PassArgs &a = jb.a;
+  // the pass's arguments in shared memory: the step loop reads them there
+  // (a kernel parameter would sit in the constant bank; a job's do not)
+  __shared__ PassArgs s_args;
+  {
+    const int *src = reinterpret_cast<const int *>(&jb.a);
+    int *dst = reinterpret_cast<int *>(&s_args);
+    for (int i = threadIdx.x; i < (int)(sizeof(PassArgs) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+  }
+  const PassArgs &a = s_args;
   if ((int)rank >= a.tiles1) {
     // no strip of this cross-section: take part in the body's two cluster barriers only
     cl_sync();
@@ -169,7 +178,9 @@ cudaLaunchConfig_t config(int G, int threads, size_t smem, cudaStream_t s, cudaL
 }
 
 int set_attributes(const void *fn) {
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 64);
+  // dynamic shared memory up to the planner's budget (227 KB less 1 KB: the
+  // kernel's static shared memory, the claim and the pass arguments, fits)
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 1024);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   return FG_OK;
