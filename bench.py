@@ -131,24 +131,52 @@ def batch_workload(seed: int = 3, n: int = 64):
     return items
 
 
-def batch_cpu_sample(images, masks, lambs, budget_s=15.0):
-    """CPU baseline of the uneven batch: the C restatement of the reference's
-    CPU path (the `port`), plain and signed transform of images taken in a
-    fixed spread over the batch (each once before any twice), until about
-    `budget_s` seconds.  images[i]: [C, H, W], masks[i]: [1, H, W] (numpy).
-    Returns (Gvoxel-passes/s, kind, cores, sample description)."""
+def batch_cpu_sample(images, masks, lambs, budget_s=15.0, kind_pref="port", build=False):
+    """CPU baseline of the uneven batch: plain and signed transform of images
+    taken in a fixed spread over the batch (each once before any twice), until
+    about `budget_s` seconds.  kind_pref "reference": the reference's own
+    installed package (its public API, OpenMP CPU path; its signed transform
+    runs the second map in a std::async thread) where it is built here, else
+    the C restatement of its CPU path (the `port`).  images[i]: [C, H, W],
+    masks[i]: [1, H, W] (numpy).  Returns (Gvoxel-passes/s, kind, cores, sample
+    description)."""
     from math import gcd
 
     from oracle import oracle
 
+    FG = reference_install(build=build) if kind_pref == "reference" else None
+    if FG is not None:
+        import torch
+
+        cores = host_threads()
+
+        def plain(i):
+            FG.generalised_geodesic2d(torch.from_numpy(images[i])[None], torch.from_numpy(masks[i])[None], 1e10,
+                                      lambs[i], 2)
+
+        def signed(i):
+            FG.signed_generalised_geodesic2d(torch.from_numpy(images[i])[None], torch.from_numpy(masks[i])[None],
+                                             1e10, lambs[i], 2)
+
+        kind = "reference"
+    else:
+        cores = oracle.max_threads()
+
+        def plain(i):
+            oracle.geodesic2d(images[i], masks[i], 1e10, lambs[i], 2)
+
+        def signed(i):
+            oracle.signed2d(images[i], masks[i], 1e10, lambs[i], 2)
+
+        kind = "port"
     n = len(images)
     stride = 37 if gcd(37, n) == 1 else 1
     t_total, vp, done = 0.0, 0.0, 0
     for k in range(4 * n):
         i = (k * stride) % n
         t0 = time.perf_counter()
-        oracle.geodesic2d(images[i], masks[i], 1e10, lambs[i], 2)
-        oracle.signed2d(images[i], masks[i], 1e10, lambs[i], 2)
+        plain(i)
+        signed(i)
         t_total += time.perf_counter() - t0
         H, W = images[i].shape[1:]
         vp += float(H) * W * 4 * 2 * 3  # 4 passes x 2 iterations; plain + signed (two maps)
@@ -156,12 +184,13 @@ def batch_cpu_sample(images, masks, lambs, budget_s=15.0):
         if t_total >= budget_s:
             break
     sample = f"{done} images of the batch, plain + signed transform each (iterations 2), {t_total:.1f} s"
-    return vp / t_total / 1e9, "port", oracle.max_threads(), sample
+    return vp / t_total / 1e9, kind, cores, sample
 
 
 def run_batch_reference_arm(args, rank, world=1):
-    """The uneven batch on the reference's CPU path (its C restatement, all
-    host threads): a bounded sample of the batch's plain + signed transforms."""
+    """The uneven batch on the reference's CPU path (its installed package where
+    it builds here, else its C restatement; all host threads): a bounded sample
+    of the batch's plain + signed transforms."""
     import torch
 
     if rank != 0:
@@ -171,7 +200,8 @@ def run_batch_reference_arm(args, rank, world=1):
     images = [im[0].cpu().numpy() for im, _, _ in items]
     masks = [m[0].cpu().numpy() for _, m, _ in items]
     t0 = time.perf_counter()
-    value, kind, cores, sample = batch_cpu_sample(images, masks, [l for _, _, l in items], budget_s=args.cpu_budget)
+    value, kind, cores, sample = batch_cpu_sample(images, masks, [l for _, _, l in items], budget_s=args.cpu_budget,
+                                                  kind_pref="reference", build=True)
     wall = time.perf_counter() - t0
     line = {
         "impl": "reference", "metric": "generalised_geodesic2d uneven batch throughput", "value": round(value, 4),
@@ -268,7 +298,7 @@ def run_batch_arm(args, rank, world):
     f64["image"] = "the smallest of the batch, plain transform"
     cpu_val, cpu_kind, cpu_cores, cpu_sample = batch_cpu_sample(
         [im[0].cpu().numpy() for im, _, _ in items], [m[0].cpu().numpy() for _, m, _ in items],
-        [l for _, _, l in items], budget_s=args.cpu_budget)
+        [l for _, _, l in items], budget_s=args.cpu_budget, kind_pref="reference")
     line = {
         "metric": "generalised_geodesic2d uneven batch throughput", "value": round(vp / ms_b / 1e6, 4),
         "unit": "Gvoxel-passes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
