@@ -141,6 +141,11 @@ FG_ONE_LAUNCH_SIDE = 512  # plain / signed 2D transforms of images up to this si
 FG_PLAN_LEAN = 1      # plan flag: the 64-register kernel
 FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-section
 FG_PLAN_RUNS2 = 4     # plan flag: cluster sweep kernel, 2 runs of 4 cells per thread
+
+
+def FG_PLAN_MODE(m: int) -> int:
+    """fg_plan_override flag: the plan applies to passes of arithmetic mode m only."""
+    return (m + 1) << 4
 # the last field holds the plan flags (FG_PLAN_LEAN | FG_PLAN_CLUSTER)
 PLAN_FIELDS = ("S", "T1", "T2", "K1", "K2", "tiles1", "tiles2", "threads", "depth", "smem", "lean")
 

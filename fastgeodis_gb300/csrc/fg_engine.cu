@@ -233,10 +233,18 @@ double cone_avg_runs(int cross, int R1, int R2, int K1, int K2, int S) {
 // that fg_plan_override and fg_set_tuning still reach the pass kernel).
 bool one_launch_image(int H, int W);
 
-// Plan overrides set by the autotuner (fg_plan_override): cross-section shape
-// -> (S, T1, T2, flags); flags: FG_PLAN_LEAN, FG_PLAN_CLUSTER.
+// Plan overrides set by the autotuner (fg_plan_override): (cross-section
+// shape, mode key) -> (S, T1, T2, flags); flags: FG_PLAN_LEAN, FG_PLAN_CLUSTER,
+// FG_PLAN_RUNS2.  Mode key 0 applies to every arithmetic mode, 1 + mode to
+// that mode only (and wins over key 0).
 std::mutex g_override_mu;
-std::map<std::tuple<int, int, int>, std::tuple<int, int, int, int>> g_overrides;
+std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int, int>> g_overrides;
+
+bool has_override(int cross, int N1, int N2) {  // under g_override_mu
+  for (int k = 0; k <= 3; k++)
+    if (g_overrides.find(std::make_tuple(cross, N1, N2, k)) != g_overrides.end()) return true;
+  return false;
+}
 
 // A cluster plan for a volume pass: ceil(N1 / T1) strips of T1 whole rows,
 // one CTA each, 2 to 16 CTAs in one cluster.  S is the transposed write's
@@ -284,8 +292,7 @@ std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older c
 bool one_launch_image(int H, int W) {
   if (std::max(H, W) > kOneLaunchSide || g_tune_region.load() < kMaxRegion || g_tune_tiles.load() > 0) return false;
   std::lock_guard<std::mutex> g(g_override_mu);
-  return g_overrides.find(std::make_tuple(1, 1, W)) == g_overrides.end() &&
-         g_overrides.find(std::make_tuple(1, 1, H)) == g_overrides.end();
+  return !has_override(1, 1, W) && !has_override(1, 1, H);
 }
 
 bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int max_tiles, Plan *out) {
@@ -351,7 +358,8 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   int ovS = 0, ovT1 = 0, ovT2 = 0, ovLean = 0;
   {
     std::lock_guard<std::mutex> g(g_override_mu);
-    auto it = g_overrides.find(std::make_tuple(cross, N1, N2));
+    auto it = g_overrides.find(std::make_tuple(cross, N1, N2, 1 + mode));
+    if (it == g_overrides.end()) it = g_overrides.find(std::make_tuple(cross, N1, N2, 0));
     if (it != g_overrides.end()) std::tie(ovS, ovT1, ovT2, ovLean) = it->second;
   }
   if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
@@ -905,8 +913,10 @@ int fg_profile_launch_times(float *ms, int *steps, int cap, int *n) {
 
 int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean) {
   if (cross < 1 || cross > 2 || N1 < 1 || N2 < 1) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad shape");
+  const int mkey = (lean & FG_PLAN_MODE_MASK) >> 4;  // 0: every mode, 1 + mode: that mode only
+  lean &= ~FG_PLAN_MODE_MASK;
   std::lock_guard<std::mutex> g(g_override_mu);
-  auto key = std::make_tuple(cross, N1, N2);
+  auto key = std::make_tuple(cross, N1, N2, mkey);
   if (S == 0) {
     g_overrides.erase(key);
   } else {

@@ -17,6 +17,13 @@ share the GPU.  Volume passes also try cluster plans: one thread-block
 cluster of up to 16 CTAs owns the whole cross-section (no halo, no hand-off
 through global memory), so concurrent transforms each take a few SMs.
 
+Transforms of one shape that differ in arithmetic mode (l_grad = 0, l_eucl =
+0 with l_grad = 1, or the general expression -- e.g. the lambdas 0, 1 and 0.5
+of one image) cost different amounts per step, and the slowest sets the
+time of the group.  Their plans are tuned per mode (``FG_PLAN_MODE``): the
+costliest mode first, so that it may take more SMs while the cheaper ones
+make do with fewer.
+
 Every plan computes the same bits; only the time changes.  Pinned plans hold
 for the process (all calls with that cross-section) until `clear`.
 """
@@ -36,7 +43,7 @@ from . import _lib
 THREADS = 512
 THREADS_LEAN = 1024
 
-Key = Tuple[int, int, int]        # (cross, N1, N2)
+Key = Tuple[int, ...]             # (cross, N1, N2), or (cross, N1, N2, mode) for a per-mode plan
 Choice = Tuple[int, int, int]     # (S, T1, T2)
 # A pinned plan: (S, T1, T2, flags); flags FG_PLAN_LEAN asks for the
 # 64-register kernel, FG_PLAN_CLUSTER for a cluster plan (fg_plan_override).
@@ -134,31 +141,58 @@ def pass_keys(shape: Sequence[int]) -> List[Key]:
     return list(dict.fromkeys(keys))
 
 
+MODE_GENERAL, MODE_EUCLID, MODE_GEO = 0, 1, 2
+
+
+def mode_of(lamb: float) -> int:
+    """The engine's arithmetic mode of a transform with this lamb: the
+    weights as the drop-in narrows them (l_grad = lamb, l_eucl = 1 - lamb)."""
+    import numpy as np
+
+    lg, le = np.float32(lamb), np.float32(1.0 - float(lamb))
+    if lg == 0.0:
+        return MODE_EUCLID
+    if le == 0.0 and lg == 1.0:
+        return MODE_GEO
+    return MODE_GENERAL
+
+
+def _mode_flag(key: Key) -> int:
+    return _lib.FG_PLAN_MODE(key[3]) if len(key) == 4 else 0
+
+
 def pin(choices: Dict[Key, Tuple[int, int, int, int]]) -> None:
-    """Pin plans {(cross, N1, N2): (S, T1, T2, lean)}."""
+    """Pin plans {(cross, N1, N2[, mode]): (S, T1, T2, flags)}."""
     L = _lib.load()
-    for (cross, N1, N2), (S, T1, T2, lean) in choices.items():
-        _lib.check(L.fg_plan_override(cross, N1, N2, S, T1, T2, lean))
+    for key, (S, T1, T2, lean) in choices.items():
+        _lib.check(L.fg_plan_override(*key[:3], S, T1, T2, lean | _mode_flag(key)))
 
 
 def clear(shape: Sequence[int]) -> None:
-    """Unpin the plans of a shape's cross-sections (the cost model decides again)."""
+    """Unpin the plans of a shape's cross-sections, for every mode (the cost
+    model decides again)."""
     L = _lib.load()
     for cross, N1, N2 in pass_keys(shape):
         _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0, 0))
+        for m in (MODE_GENERAL, MODE_EUCLID, MODE_GEO):
+            _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0, _lib.FG_PLAN_MODE(m)))
 
 
 def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing=(1.0, 1.0, 1.0),
              iterations: int = 1, repeats: int = 3, device=None, max_per_step: int = 24,
-             lambs: Optional[Sequence[float]] = None, verbose: bool = False) -> Dict[Key, Tuple[int, int, int, int, float]]:
+             lambs: Optional[Sequence[float]] = None, verbose: bool = False,
+             per_mode: bool = True) -> Dict[Key, Tuple[int, int, int, int, float]]:
     """Measure candidate plans for a 2D (H, W) or 3D (D, H, W) transform of
     `channels` image channels and pin the fastest for each cross-section.
 
     `lambs`: the workload's transforms that run at the same time, one per
     stream (default: one transform with `lamb`).  With several, the 64-register
-    kernel is tried too (two CTAs of different transforms per SM).  Returns
-    {(cross, N1, N2): (S, T1, T2, lean, best ms of the workload)}; the model's
-    own plan competes as the unpinned entry (S = 0)."""
+    kernel is tried too (two CTAs of different transforms per SM), and when
+    they differ in arithmetic mode (`per_mode`) each mode's passes get their
+    own plan, the costliest mode (general, then l_eucl = 0, then l_grad = 0)
+    tuned first.  Returns {(cross, N1, N2[, mode]): (S, T1, T2, flags, best
+    ms of the workload)}; the model's own plan competes as the unpinned entry
+    (S = 0)."""
     import fastgeodis_gb300 as fg
 
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -203,9 +237,14 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         fracs = (1.0,) if len(lambs) == 1 else (1.0, 0.75, 0.5, 0.34)
         lean = channels <= 1
-        for key in pass_keys(shape):
-            cross, N1, N2 = key
-            _lib.check(L.fg_plan_override(cross, N1, N2, 0, 0, 0, 0))
+        present = {mode_of(x) for x in lambs}
+        modes = [m for m in (MODE_GENERAL, MODE_GEO, MODE_EUCLID) if m in present]
+        clear(shape)
+        tuned = [k + (m,) for k in pass_keys(shape) for m in modes] if per_mode and len(modes) > 1 \
+            else pass_keys(shape)
+        for key in tuned:
+            cross, N1, N2 = key[:3]
+            mflag = _mode_flag(key)
             best_c, best_t = (0, 0, 0, 0), measure()
             if verbose:
                 print(f"[tune] {key} model plan: {best_t:.3f} ms")
@@ -219,7 +258,7 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
             # off when several transforms share the GPU
             trials += cluster_candidates(cross, N1, N2, lean_capable=lean, one_channel=channels <= 1)
             for c in trials:
-                _lib.check(L.fg_plan_override(cross, N1, N2, *c))
+                _lib.check(L.fg_plan_override(cross, N1, N2, *c[:3], c[3] | mflag))
                 try:
                     t = measure()
                 except _lib.EngineError:
@@ -233,7 +272,7 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
                     print(f"[tune] {key} S={c[0]} T={c[1]}x{c[2]} lean={c[3]}: {t:.3f} ms")
                 if t < best_t:
                     best_c, best_t = c, t
-            _lib.check(L.fg_plan_override(cross, N1, N2, *best_c))
+            _lib.check(L.fg_plan_override(cross, N1, N2, *best_c[:3], best_c[3] | mflag))
             result[key] = best_c + (best_t,)
         fg.check_status(dev)
     return result

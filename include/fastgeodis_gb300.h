@@ -69,6 +69,12 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 #define FG_PLAN_LEAN 1    /* the 64-register kernel */
 #define FG_PLAN_CLUSTER 2 /* a cluster plan: one thread-block cluster owns the cross-section */
 #define FG_PLAN_RUNS2 4   /* cluster plan on the cluster sweep kernel, 2 runs of 4 cells per thread */
+/* fg_plan_override only: the plan applies to passes of arithmetic mode m
+ * alone (0: general, 1: l_grad == 0, 2: l_eucl == 0 and l_grad == 1), and
+ * wins over a plan without this flag; without it a plan applies to every
+ * mode. */
+#define FG_PLAN_MODE(m) (((m) + 1) << 4)
+#define FG_PLAN_MODE_MASK 0x30
 
 /* Plan override (no counterpart in the reference): for passes whose
  * cross-section is N1 x N2 (cross = 1 for 2D images, N1 = 1; cross = 2 for
@@ -84,7 +90,10 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * transposed write's flush period.  With FG_PLAN_RUNS2 (and at most one image
  * channel read) the strips run on the cluster sweep kernel, each thread
  * owning 2 vertically adjacent runs (T1 is rounded up to an even number), at
- * most 512 threads per CTA.  S = 0 removes the override.  Used by the
+ * most 512 threads per CTA.  FG_PLAN_MODE(m) restricts the plan to passes
+ * of one arithmetic mode (several transforms of one shape with different
+ * weights, e.g. the lambdas of one image, may then get different plans).
+ * S = 0 removes the override of that mode key.  Used by the
  * autotuner (fastgeodis_gb300.tune); results do not depend on it.  A plan
  * that does not fit the device falls back to the planner's choice, and a
  * cluster plan that the device cannot co-schedule fails with

@@ -135,14 +135,41 @@ def test_autotune_pins_plans_and_keeps_results():
 
     shape = (36, 80, 96)
     try:
+        # two modes (lamb 0: no image term; 0.5: general): one plan per cross-section and mode
         res = tune.autotune(shape, channels=1, lambs=[0.0, 0.5], iterations=1, repeats=2, max_per_step=4)
-        assert set(res) == set(tune.pass_keys(shape))
-        for S, T1, T2, lean, ms in res.values():
-            assert ms > 0 and S in (0, 4, 8) and lean in (0, 1, 2, 3)  # flags: lean, cluster
+        assert set(res) == {k + (m,) for k in tune.pass_keys(shape) for m in (tune.MODE_GENERAL, tune.MODE_EUCLID)}
+        for S, T1, T2, flags, ms in res.values():
+            assert ms > 0 and S in (0, 4, 8)
+            assert flags & ~(_lib.FG_PLAN_LEAN | _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2) == 0
         img, m = _case(shape, 1, 5)
-        got = fg.generalised_geodesic3d(torch.from_numpy(img)[None].cuda(), torch.from_numpy(m)[None].cuda(),
-                                        [1.0, 1.0, 1.0], 1e10, 0.5, 2)[0].cpu().numpy()
-        assert bits_equal(got, oracle.geodesic3d(img, m, [1.0, 1.0, 1.0], 1e10, 0.5, 2))
+        for lamb in (0.0, 0.5):
+            got = fg.generalised_geodesic3d(torch.from_numpy(img)[None].cuda(), torch.from_numpy(m)[None].cuda(),
+                                            [1.0, 1.0, 1.0], 1e10, lamb, 2)[0].cpu().numpy()
+            assert bits_equal(got, oracle.geodesic3d(img, m, [1.0, 1.0, 1.0], 1e10, lamb, 2)), lamb
+        res1 = tune.autotune(shape, channels=1, lambs=[0.5, 0.5], iterations=1, repeats=1, max_per_step=2)
+        assert set(res1) == set(tune.pass_keys(shape))  # one mode: plans for every mode
         fg.check_status()
     finally:
         tune.clear(shape)
+
+
+def test_per_mode_overrides():
+    """A plan pinned for one arithmetic mode serves that mode's passes only
+    and wins over a plan pinned for every mode; clearing removes both."""
+    L = _lib.load()
+    key = (2, 256, 256)
+    model = [_lib.plan_describe(*key, C=1, maps=1, mode=m) for m in range(3)]
+    try:
+        _lib.check(L.fg_plan_override(*key, 8, 16, 256, _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2
+                                      | _lib.FG_PLAN_MODE(tune.MODE_GENERAL)))
+        _lib.check(L.fg_plan_override(*key, 4, 32, 64, 0))  # every mode
+        general = _lib.plan_describe(*key, C=1, maps=1, mode=tune.MODE_GENERAL)
+        assert general["tiles1"] == 16 and general["lean"] & _lib.FG_PLAN_CLUSTER
+        for m in (tune.MODE_EUCLID, tune.MODE_GEO):
+            p = _lib.plan_describe(*key, C=1, maps=1, mode=m)
+            assert (p["S"], p["T1"], p["T2"]) == (4, 32, 64) and not p["lean"] & _lib.FG_PLAN_CLUSTER
+        assert tune.mode_of(0.0) == tune.MODE_EUCLID and tune.mode_of(1.0) == tune.MODE_GEO
+        assert tune.mode_of(0.5) == tune.MODE_GENERAL
+    finally:
+        tune.clear((256, 256, 256))
+    assert [_lib.plan_describe(*key, C=1, maps=1, mode=m) for m in range(3)] == model
