@@ -136,8 +136,9 @@ def test_autotune_pins_plans_and_keeps_results():
     shape = (36, 80, 96)
     try:
         # two modes (lamb 0: no image term; 0.5: general): one plan per cross-section and mode
-        res = tune.autotune(shape, channels=1, lambs=[0.0, 0.5], iterations=1, repeats=2, max_per_step=4)
-        assert set(res) == {k + (m,) for k in tune.pass_keys(shape) for m in (tune.MODE_GENERAL, tune.MODE_EUCLID)}
+        res = tune.autotune(shape, channels=1, lambs=[0.0, 0.5], iterations=1, repeats=2, max_per_step=4, per_mode=True)
+        keys = tune.pass_keys(shape)
+        assert set(res) == set(keys) | {k + (m,) for k in keys for m in (tune.MODE_GENERAL, tune.MODE_EUCLID)}
         for S, T1, T2, flags, ms in res.values():
             assert ms > 0 and S in (0, 4, 8)
             assert flags & ~(_lib.FG_PLAN_LEAN | _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2) == 0
