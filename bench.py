@@ -914,14 +914,16 @@ def sweep_kernel_name(w, tuned):
         return "fg_toivanen_kernel"
     if w["dims"] == 2 and max(w["image"].shape[2:]) <= _one_launch_side():
         return "fg_row2d_kernel"
-    flags = [int(v[3]) for v in (tuned or {}).get("plans", {}).values() if int(v[0]) > 0]
     from fastgeodis_gb300 import _lib
 
-    if any(f & _lib.FG_PLAN_RUNS2 for f in flags):
-        return "fg_sweep_cluster_kernel"
-    if any(f & _lib.FG_PLAN_CLUSTER for f in flags):
-        return "fg_pass_cluster_kernel"
-    return "fg_pass_kernel"
+    names = []
+    for v in (tuned or {}).get("plans", {}).values() or [[0, 0, 0, 0]]:
+        f = int(v[3]) if int(v[0]) > 0 else 0
+        name = ("fg_sweep_cluster_kernel" if f & _lib.FG_PLAN_RUNS2 else
+                "fg_pass_cluster_kernel" if f & _lib.FG_PLAN_CLUSTER else "fg_pass_kernel")
+        if name not in names:
+            names.append(name)
+    return " + ".join(names)  # the sweep kernels of the pinned plans (the passes of one transform)
 
 
 def metric_name(w):
