@@ -70,8 +70,10 @@ def workload(name: str, seed: int = 1):
                      "iterations 4, lamb cycling 0.0 / 0.5 / 1.0; one transform per volume")
         return w
     rng = np.random.default_rng(seed)
-    if name in ("c2", "vol256"):
-        shape = (128, 256, 256) if name == "c2" else (256, 256, 256)
+    if name in ("c2", "vol256", "slab"):
+        # slab: 64 slices of 1024 x 1024, a cross-section larger than the
+        # resident tiles hold (the sweep along the slices runs chunked)
+        shape = {"c2": (128, 256, 256), "vol256": (256, 256, 256), "slab": (64, 1024, 1024)}[name]
         vol = smooth_noise(rng, shape, 2.0, 0.0, 1.0)
         mask = np.ones(shape, np.float32)
         c = [int(rng.integers(0, n - 6)) for n in shape]
@@ -1489,7 +1491,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "b256", "c3", "c4", "c5", "t1", "t2"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "vol256", "slab", "b256", "c3", "c4", "c5", "t1", "t2"])
     ap.add_argument("--requests", type=int, default=300, help="requests of the served stream (c5)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--no-tune", dest="tune", action="store_false",

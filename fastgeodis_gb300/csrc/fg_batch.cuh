@@ -142,6 +142,7 @@ __device__ inline void batch_pass_args(const fg_batch2d_item &it, int M, int fir
   a.status = status;
   a.tape = nullptr;
   a.P = depth;
+  a.t_begin = 0, a.t_end = 0;
   *pa = a;
 }
 

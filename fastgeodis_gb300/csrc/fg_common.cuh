@@ -63,6 +63,12 @@ struct PassArgs {
   int vec;                        // runs may use 16-byte global loads and stores
   int P;                          // steps of own inputs staged ahead (2, 4 or 8)
   int wt;                         // the pass writes transposed (read by kernels that take it at run time)
+  // Steps [t_begin, t_end) of the pass run in this launch (t_end == 0: all L).
+  // A chunked plan runs one chunk of S steps per ordinary launch (t_begin a
+  // multiple of S), for cross-sections whose tiles cannot all be resident at
+  // once: its CTAs start from the previous row's exchange words, which the
+  // launch before published, so no CTA waits on another.
+  int t_begin, t_end;
   // Halo exchange between tiles: 64-bit words [2 parities][kMaxMaps][N1*N2],
   // each a cell's distance bits (low half) and the epoch of the chunk whose
   // last row it holds (high half).  One aligned 64-bit access carries both,
@@ -84,6 +90,7 @@ struct LaunchCfg {
   size_t smem;
   bool lean;  // the 64-register kernel (required above 512 threads)
   int rpt;    // cluster sweep kernel: 4-cell runs per thread (0: the pass kernel)
+  bool chunked = false;  // an ordinary launch of any number of tiles (t_begin / t_end), not a cooperative one
 };
 
 // Pitch of the shared rings' rows: at least `floats`, a multiple of 4 (float4

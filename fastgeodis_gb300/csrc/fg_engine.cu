@@ -189,6 +189,7 @@ struct Plan {
   bool lean;     // 64-register kernel
   bool cluster;  // one thread-block cluster of tiles1 strips of whole rows (fg_pass3d_cluster.cu)
   int rpt;       // cluster plans: runs per thread of the cluster sweep kernel (0: the pass kernel)
+  bool chunked = false;  // one ordinary launch per chunk of S steps, any number of tiles
 };
 
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
@@ -202,6 +203,10 @@ std::atomic<int> g_tune_tiles{0};            // cap on tiles per pass (0: the SM
 // S steps of a chunk.
 constexpr double kStepBase = 620.0, kCyclesPerRunGeneral = 2.4, kCyclesPerRunEuclid = 1.3;
 constexpr double kHandoffBase = 2000.0, kHandoffPerTile = 8.0;
+// Chunked plans: a launch's start-up (launch latency, prefetch and the
+// previous row's exchange words) in the same cycles, and the shared memory of an SM.
+constexpr double kChunkLaunch = 12000.0;
+constexpr size_t kSmemPerSm = 228 * 1024;
 
 // Runs computed per step, averaged over the S steps of a chunk and rounded up
 // to whole warps: the kernel orders runs innermost first and skips, at chunk
@@ -315,7 +320,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   const int max_threads = pass_max_threads(cross, mode == MODE_EUCLID ? 0 : C, M);
   const bool lean_capable = pass_lean(cross, mode == MODE_EUCLID ? 0 : C, M);
   // returns 1 if the plan is valid, 0 if not, -1 if it is too large (so is every larger T1)
-  auto consider = [&](int S, int T1, int T2, int t1, int t2, bool want_lean) -> int {
+  auto consider = [&](int S, int T1, int T2, int t1, int t2, bool want_lean, bool chunked = false) -> int {
     const bool multi = t1 * t2 > 1;
     int K1 = (cross == 2 && t1 > 1) ? S : 0, K2 = t2 > 1 ? S : 0;
     if ((t1 > 1 && T1 < K1) || (t2 > 1 && T2 < K2)) return 0;
@@ -348,8 +353,17 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (lean) cost += 0.13 * per_run * avg_runs;  // the 64-register kernel's extra instructions
     // one CTA per SM (shared memory or registers): no room for a concurrent transform
     if (sm > kSmemBudget / 2 || nt > kThreads) cost *= 1.05;
+    if (chunked) {
+      // tiles run in waves of the CTAs the SMs hold at once (max_tiles is the
+      // SM count here); each launch's start-up is spread over its S steps
+      const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(kSmemPerSm / (sm + 1024), 2048 / nt));
+      const long long slots = (long long)max_tiles * per_sm, tiles = (long long)t1 * t2;
+      const long long waves = (tiles + slots - 1) / slots;
+      const double conc = (double)std::min<long long>(per_sm, (tiles + max_tiles - 1) / max_tiles);
+      cost = (double)waves * std::max(kStepBase, conc * per_run * avg_runs * (lean ? 1.13 : 1.0)) + kChunkLaunch / S;
+    }
     if (!found || cost < best_cost - 1e-9) {
-      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean, false, 0};
+      best = Plan{T1, T2, K1, K2, t1, t2, S, nt, B2, rowf, depth, sm, lean, false, 0, chunked && multi};
       best_cost = cost;
       found = true;
     }
@@ -372,7 +386,8 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   } else if (ovS > 0) {
     const int T1 = cross == 2 ? std::min(ovT1, N1) : 1, T2 = std::min(ovT2, N2);
     const int t1 = (N1 + T1 - 1) / T1, t2 = (N2 + T2 - 1) / T2;
-    if ((long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, ovLean != 0);
+    const bool chunked = (ovLean & FG_PLAN_CHUNKED) != 0;
+    if (chunked || (long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, (ovLean & FG_PLAN_LEAN) != 0, chunked);
   }
   for (int S : {8, 4, 2, 1}) {
     if (found) break;  // an override that fits wins
@@ -397,6 +412,36 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
       }
     }
   }
+  // No plan whose tiles are all resident at once (a cross-section larger than
+  // the SMs' regions): a chunked plan, one ordinary launch per chunk of S
+  // steps over as many tiles as it takes.  Volumes: for each tile width, the
+  // tallest tile that fits, evened out over the cross-section; rows: the
+  // longest tile, evened out.
+  const bool need_chunks = !found;
+  const int lim = std::min(max_region, 4 * max_threads);
+  for (int S : {8, 4, 2}) {
+    if (!need_chunks) break;
+    if (cross == 1) {
+      int T2 = std::min(lim, 4 * max_threads) - 2 * S;
+      T2 &= ~3;
+      if (T2 < S || T2 >= N2) continue;
+      const int t2 = (N2 + T2 - 1) / T2;
+      T2 = (((N2 + t2 - 1) / t2) + 3) & ~3;
+      consider(S, 1, T2, 1, (N2 + T2 - 1) / T2, false, true);
+      continue;
+    }
+    for (int T2 = std::min(N2, 4);; T2 = std::min(N2, T2 + 4)) {
+      const int t2 = (N2 + T2 - 1) / T2, K2 = t2 > 1 ? S : 0, R2 = T2 + 2 * K2;
+      const int R1max = std::min(lim / R2, max_threads / ((R2 + 3) / 4));
+      int T1 = N1;
+      if (R1max < N1) {
+        const int T1max = R1max - 2 * S;
+        T1 = T1max >= S ? (N1 + (N1 + T1max - 1) / T1max - 1) / ((N1 + T1max - 1) / T1max) : 0;
+      }
+      if (T1 > 0 && (long long)((N1 + T1 - 1) / T1) * t2 > 1) consider(S, T1, T2, (N1 + T1 - 1) / T1, t2, false, true);
+      if (T2 >= N2) break;
+    }
+  }
   if (found) {
     std::lock_guard<std::mutex> g(mu);
     cache[key] = best;
@@ -405,9 +450,9 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (debug)
       fprintf(stderr,
               "[fg plan] cross=%d N=%dx%d C=%d M=%d mode=%d wt=%d -> T=%dx%d K=%d,%d tiles=%dx%d S=%d NT=%d "
-              "P=%d smem=%zu lean=%d cluster=%d cost=%.0f\n",
+              "P=%d smem=%zu lean=%d cluster=%d chunked=%d cost=%.0f\n",
               cross, N1, N2, C, M, mode, (int)wt, best.T1, best.T2, best.K1, best.K2, best.tiles1, best.tiles2,
-              best.S, best.NT, best.P, best.smem, (int)best.lean, (int)best.cluster, best_cost);
+              best.S, best.NT, best.P, best.smem, (int)best.lean, (int)best.cluster, (int)best.chunked, best_cost);
   }
   return found;
 }
@@ -533,10 +578,20 @@ int profiled_launch(cudaStream_t s, long long vp, int steps, Launch launch) {
 }
 
 int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt, cudaStream_t s) {
-  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean, p.rpt};
+  LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean, p.rpt, p.chunked};
   return profiled_launch(s, (long long)a.L * a.N1 * a.N2 * M, a.L, [&] {
     if (p.cluster) return launch_pass_cluster(a, c, M, mode, wt, s);
-    return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
+    if (!p.chunked)
+      return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
+    // one ordinary launch per chunk of S steps, in stream order
+    for (int t0 = 0; t0 < a.L; t0 += p.S) {
+      PassArgs b = a;
+      b.t_begin = t0;
+      b.t_end = std::min(a.L, t0 + p.S);
+      const int rc = cross == 2 ? launch_pass_cross2(b, c, M, mode, wt, s) : launch_pass_cross1(b, c, M, mode, wt, s);
+      if (rc != FG_OK) return rc;
+    }
+    return FG_OK;
   });
 }
 
@@ -922,8 +977,10 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
   } else {
     if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2;
+    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_CHUNKED;
     if (lean < 0 || (lean & ~all)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
+    if ((lean & FG_PLAN_CHUNKED) && (lean & FG_PLAN_CLUSTER))
+      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: a chunked plan is a tile plan");
     if ((lean & FG_PLAN_RUNS2) && !(lean & FG_PLAN_CLUSTER))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: runs per thread apply to cluster plans");
     if ((lean & FG_PLAN_CLUSTER) && (cross != 2 || S < 2))
@@ -945,7 +1002,7 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
     return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
   const int v[11] = {p.S,  p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem,
                      (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0) |
-                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0)};
+                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0) | (p.chunked ? FG_PLAN_CHUNKED : 0)};
   for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }

@@ -234,6 +234,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const int C = USE_IMG && !WIDE ? (CT == 0 ? a.C : CT) : 0;  // channels staged in shared memory
   const int CW = WIDE ? a.C : 0;                                // channels read through L1
   const int L = a.L, S = a.S, lgS = __ffs(S) - 1;  // S is a power of two
+  const int tb = a.t_begin, te = a.t_end > 0 ? a.t_end : L;  // steps of this launch
   const int SR = WT ? S : 2;                        // distance rows kept in shared memory
   const int ti1 = tile / a.tiles2, ti2 = tile - ti1 * a.tiles2;
   const int R1 = CROSS == 2 ? a.T1 + 2 * a.K1 : 1, R2 = a.T2 + 2 * a.K2;
@@ -341,9 +342,9 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   const long long wstep = a.dir > 0 ? a.ws_str : -a.ws_str;
   const long long r0 = (a.dir > 0 ? 0 : (long long)(L - 1) * a.s_str) + (long long)g1 * a.st1 + g20;
   const long long w0 = (a.dir > 0 ? 0 : (long long)(L - 1) * a.ws_str) + (long long)g1 * a.wst1 + (long long)g20 * a.wst2;
-  long long rnext = r0;  // read offset of the next step to stage
-  long long rcur = r0;   // read offset of the current step
-  long long wcur = w0;   // write offset of the current step
+  long long rnext = r0 + (long long)tb * rstep;  // read offset of the next step to stage
+  long long rcur = rnext;                         // read offset of the current step
+  long long wcur = w0 + (long long)tb * wstep;    // write offset of the current step
 
   // stage the own inputs of step `step` into ring slot `slot` (one commit group per step)
   // A run outside a step's cone still needs its image values at a chunk's
@@ -380,11 +381,11 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
   };
 
   for (int k = 0; k < P; k++) {
-    if (k < L) stage(k, k);
+    if (tb + k < te) stage((tb + k) & (P - 1), tb + k);
     else cp_async_commit();
   }
 
-  for (int t = 0; t < L; t++) {
+  for (int t = tb; t < te; t++) {
     const int slot = t & (P - 1);
     if (CL && t > 0 && cl_waits) {
       // the neighbour strips' rows of step t-1 have landed in the apron rows
@@ -393,9 +394,12 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         cl_dead = true;  // results are void; later steps no longer wait
       if (tid == 0 && !cl_dead && t + 1 <= L - 2) mbar_expect(bar, cl_bytes);  // the same parity's next step
     }
-    // exact halo values of the previous row from the neighbour tiles
+    // exact halo values of the previous row from the neighbour tiles; the
+    // first step of a chunk launch takes the whole previous row (own cells
+    // too) from the words the launch before published, and its image values
     if (has_nb && t > 0 && (t & (S - 1)) == 0) {
-      if (halo) {
+      const unsigned need = t == tb ? valid : halo;
+      if (need) {
         const unsigned want = a.epoch_base + (unsigned)(t >> lgS);
         const unsigned long long *xw = xrun + (long long)((t >> lgS) & 1) * kMaxMaps * xplane;
         float *pr = dring + ((t - 1) & (SR - 1)) * M * rowf + cb;
@@ -404,12 +408,12 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         for (int m = 0; m < M; m++)
 #pragma unroll
           for (int i = 0; i < 4; i++)
-            if (halo & (1u << i)) wd[m][i] = ld_word(xw + m * xplane + i);  // all in flight at once
+            if (need & (1u << i)) wd[m][i] = ld_word(xw + m * xplane + i);  // all in flight at once
 #pragma unroll
         for (int m = 0; m < M; m++)
 #pragma unroll
           for (int i = 0; i < 4; i++)
-            if (halo & (1u << i)) {
+            if (need & (1u << i)) {
               wd[m][i] = wait_word(xw + m * xplane + i, want, wd[m][i], a.status, kSpinLimit);
               const float hv = __uint_as_float((unsigned)wd[m][i]);
               pr[m * rowf + i] = hv;
@@ -418,6 +422,20 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
               if (EDGES && i == 0) pe[e0 - 1] = hv;
               if (EDGES && i == 3) pe[e0 + 2] = hv;
             }
+      }
+      if (t == tb && NCH > 0 && active) {
+        float *ic = iring + ((t - 1) & 1) * C * rowf + cb;
+        float *ice = iedge + ((t - 1) & 1) * C * edgef;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+          if (c < C) {
+            float4 v = make_float4(qnan, qnan, qnan, qnan);
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              if (valid & (1u << i)) f4set(v, i, __ldg(a.img + c * a.img_cs + (rcur - rstep) + i));
+            *reinterpret_cast<float4 *>(ic + c * rowf) = v;
+            put_edges(ice + c * edgef, v);
+          }
       }
       __syncthreads();
     }
@@ -650,7 +668,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
         }
     }
     // the slot's values are consumed (they are in registers): refill it with step t+P
-    if (t + P < L) stage(slot, t + P);
+    if (t + P < te) stage(slot, t + P);
     else cp_async_commit();
     wcur += wstep;
     rcur += rstep;
@@ -746,7 +764,8 @@ inline int launch_one_cluster(const void *fn, unsigned long long &configured, co
 }
 
 // Launch of one variant.  CLU: the cluster plan (one cluster of c.tiles CTAs);
-// otherwise a cooperative launch of c.tiles CTAs.
+// otherwise a cooperative launch of c.tiles CTAs, or an ordinary one for a
+// chunk of a chunked plan.
 template <int CROSS, int CT, int M, int MODE, bool WT, bool LEAN, bool CLU>
 int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
   void (*fn)(const PassArgs);
@@ -763,10 +782,10 @@ int launch_variant(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
     configured |= 1ull << dev;
   }
   void *args[] = {const_cast<PassArgs *>(&a)};
-  if (c.tiles > 1)
+  if (c.tiles > 1 && !c.chunked)
     e = cudaLaunchCooperativeKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
-  else
-    e = cudaLaunchKernel((const void *)fn, dim3(1), dim3(c.threads), args, c.smem, s);
+  else  // one tile, or a chunk launch (its CTAs never wait on one another)
+    e = cudaLaunchKernel((const void *)fn, dim3(c.tiles), dim3(c.threads), args, c.smem, s);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
   return FG_OK;
 }

@@ -69,6 +69,7 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 #define FG_PLAN_LEAN 1    /* the 64-register kernel */
 #define FG_PLAN_CLUSTER 2 /* a cluster plan: one thread-block cluster owns the cross-section */
 #define FG_PLAN_RUNS2 4   /* cluster plan on the cluster sweep kernel, 2 runs of 4 cells per thread */
+#define FG_PLAN_CHUNKED 8 /* a tile plan run as one ordinary launch per chunk of S steps */
 /* fg_plan_override only: the plan applies to passes of arithmetic mode m
  * alone (0: general, 1: l_grad == 0, 2: l_eucl == 0 and l_grad == 1), and
  * wins over a plan without this flag; without it a plan applies to every
@@ -90,7 +91,13 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * transposed write's flush period.  With FG_PLAN_RUNS2 (and at most one image
  * channel read) the strips run on the cluster sweep kernel, each thread
  * owning 2 vertically adjacent runs (T1 is rounded up to an even number), at
- * most 512 threads per CTA.  FG_PLAN_MODE(m) restricts the plan to passes
+ * most 512 threads per CTA.  With FG_PLAN_CHUNKED a tile plan runs as one
+ * ordinary launch per chunk of S steps instead of one cooperative launch, so
+ * its tiles need not all be resident at once: each launch's CTAs start from
+ * the previous row that the launch before published.  The planner takes a
+ * chunked plan by itself only for cross-sections whose tiles cannot all be
+ * resident (volumes with slices beyond about 600 thousand cells).
+ * FG_PLAN_MODE(m) restricts the plan to passes
  * of one arithmetic mode (several transforms of one shape with different
  * weights, e.g. the lambdas of one image, may then get different plans).
  * S = 0 removes the override of that mode key.  Used by the
@@ -112,8 +119,8 @@ FG_API int fg_cluster_capacity(int cluster_size, int threads, size_t smem, int *
  * general, 1 l_grad == 0, 2 l_eucl == 0 and l_grad == 1), transposed write
  * or not, on a GPU of `sms` SMs.  Writes 11 ints to `plan`: S, T1, T2, K1,
  * K2, tiles1, tiles2, threads, staging depth, shared-memory bytes, flags
- * (FG_PLAN_LEAN, FG_PLAN_CLUSTER).  Needs no GPU; honours fg_set_tuning and
- * fg_plan_override. */
+ * (FG_PLAN_LEAN, FG_PLAN_CLUSTER, FG_PLAN_RUNS2, FG_PLAN_CHUNKED).  Needs
+ * no GPU; honours fg_set_tuning and fg_plan_override. */
 FG_API int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int transposed_write, int sms,
                             int *plan);
 

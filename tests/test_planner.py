@@ -214,3 +214,42 @@ def test_cluster_capacity_arguments():
     assert L.fg_cluster_capacity(17, 512, 1024, ctypes.byref(n)) == _lib.FG_ERR_INVALID_ARGUMENT
     assert L.fg_cluster_capacity(16, 1024, 1024, ctypes.byref(n)) == _lib.FG_ERR_INVALID_ARGUMENT
     assert L.fg_cluster_capacity(16, 512, 1024, None) == _lib.FG_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("cross,N1,N2,C,maps,mode", [(2, 1024, 1024, 1, 1, 0), (2, 800, 900, 1, 2, 2),
+                                                     (2, 2048, 2048, 3, 1, 0), (2, 1024, 1024, 9, 1, 0),
+                                                     (1, 1, 800000, 1, 1, 0)])
+def test_chunked_plan_for_sections_beyond_the_resident_tiles(cross, N1, N2, C, maps, mode):
+    """A cross-section whose tiles cannot all be resident gets a chunked plan
+    (one ordinary launch per chunk of S steps): more tiles than SMs, each
+    region within the kernel's limits, halos of S."""
+    p = _lib.plan_describe(cross, N1, N2, C=C, maps=maps, mode=mode)
+    assert p["lean"] & _lib.FG_PLAN_CHUNKED and not p["lean"] & _lib.FG_PLAN_CLUSTER
+    t1, t2 = -(-N1 // p["T1"]), -(-N2 // p["T2"])
+    assert (t1, t2) == (p["tiles1"], p["tiles2"]) and t1 * t2 > 152
+    assert p["K2"] == p["S"] and p["K1"] == (p["S"] if cross == 2 and t1 > 1 else 0)
+    R1 = p["T1"] + 2 * p["K1"] if cross == 2 else 1
+    assert R1 * (p["T2"] + 2 * p["K2"]) <= 4096 and p["smem"] <= 227 * 1024
+    assert p["T2"] % 4 == 0 and p["T1"] >= p["K1"] and p["T2"] >= p["K2"]
+
+
+def test_sections_that_fit_keep_cooperative_plans():
+    for key in [(2, 256, 256), (2, 512, 512), (2, 128, 1024), (1, 1, 4096)]:
+        assert not _lib.plan_describe(*key)["lean"] & _lib.FG_PLAN_CHUNKED, key
+
+
+def test_chunked_override():
+    L = _lib.load()
+    CH = _lib.FG_PLAN_CHUNKED
+    assert L.fg_plan_override(2, 64, 64, 4, 16, 16, CH | _lib.FG_PLAN_CLUSTER) == _lib.FG_ERR_INVALID_ARGUMENT
+    try:
+        _lib.check(L.fg_plan_override(2, 64, 64, 4, 16, 16, CH))
+        p = _lib.plan_describe(2, 64, 64)
+        assert p["lean"] & CH and (p["T1"], p["T2"], p["tiles1"], p["tiles2"]) == (16, 16, 4, 4)
+        # a chunked override may use more tiles than the SMs
+        _lib.check(L.fg_plan_override(2, 64, 64, 2, 4, 4, CH))
+        p = _lib.plan_describe(2, 64, 64, sms=8)
+        assert p["lean"] & CH and p["tiles1"] * p["tiles2"] == 256
+    finally:
+        _lib.check(L.fg_plan_override(2, 64, 64, 0, 0, 0, 0))
+    assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
