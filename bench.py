@@ -1251,6 +1251,7 @@ def run_gpu_arm(args, w, rank, world):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     pass_ms, pass_launches, pass_vp = _lib.profile_end()
+    aux_launches = _lib.profile_aux_launches()
     if dist:
         dist.barrier()
     fg.check_status()
@@ -1385,7 +1386,12 @@ def run_gpu_arm(args, w, rank, world):
         achieved = bytes_alone / (avg_alone * 1e-3) / 1e9
     else:
         avg_alone, bytes_alone, achieved = avg_launch_ms, alg_bytes_launch, achieved_step
-    init_launches = n_calls * args.steps  # v*mask initialisation, one per transform
+    # per transform besides the passes: the v*mask initialisation and the
+    # image transpose (Toivanen's scan: initialisation only; a 2D image in one
+    # launch: none, its one kernel is the pass launch)
+    per_call = (0 if sweep_kernel_name(w, tuned) == "fg_row2d_kernel" else
+                1 if w.get("method") == "toivanen" else 2)
+    init_launches = n_calls * args.steps * per_call
     cpu_val, cpu_kind, cpu_cores, cpu_sample = time_cpu_sample(w, "reference", budget_s=args.cpu_budget)
     f64 = None
     if w.get("method") != "toivanen":
@@ -1435,7 +1441,7 @@ def run_gpu_arm(args, w, rank, world):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": f"public API with pinned host tensors, {n_calls} calls per step from {n_calls} host threads"},
         "clocks": clk,
-        "gpu_launches": int((pass_launches + init_launches) / args.steps),
+        "gpu_launches": int((pass_launches + aux_launches + init_launches) / args.steps),
         **({"north_star": extra} if extra else {}),
     }
     print(json.dumps(line), flush=True)

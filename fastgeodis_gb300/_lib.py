@@ -26,7 +26,7 @@ FG_OP_GSF = 2
 # every symbol include/fastgeodis_gb300.h declares
 EXPORTED = (
     "fg_abi_version", "fg_last_error", "fg_set_tuning", "fg_plan_override", "fg_plan_describe",
-    "fg_profile_begin", "fg_profile_end", "fg_profile_launch_times",
+    "fg_profile_begin", "fg_profile_end", "fg_profile_launch_times", "fg_profile_aux_launches",
     "fg_workspace_bytes", "fg_workspace_status", "fg_selftest_wait", "fg_cluster_capacity",
     "fg_generalised_geodesic2d", "fg_generalised_geodesic3d",
     "fg_signed_generalised_geodesic2d", "fg_signed_generalised_geodesic3d",
@@ -70,6 +70,7 @@ def load():
                                  ctypes.POINTER(ctypes.c_double)]
     L.fg_profile_launch_times.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), i,
                                           ctypes.POINTER(ctypes.c_int)]
+    L.fg_profile_aux_launches.argtypes = [ctypes.POINTER(ctypes.c_int)]
     L.fg_click_mask.argtypes = [vp, i, i, i, ctypes.POINTER(ctypes.c_int), i, i, vp]
     L.fg_set_tuning.argtypes = [i, i]
     L.fg_plan_override.argtypes = [i, i, i, i, i, i, i]
@@ -124,6 +125,14 @@ def profile_end():
     ms, n, vp = ctypes.c_double(), ctypes.c_int(), ctypes.c_double()
     check(load().fg_profile_end(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(vp)))
     return ms.value, n.value, vp.value
+
+
+def profile_aux_launches() -> int:
+    """Kernel launches of the window closed by profile_end() besides one per
+    pass (chunk launches after a pass's first, map transposes)."""
+    n = ctypes.c_int()
+    check(load().fg_profile_aux_launches(ctypes.byref(n)))
+    return n.value
 
 
 def profile_launch_times():

@@ -155,6 +155,31 @@ __global__ void fg_transpose_kernel(const float *src, float *dst, int D, int H, 
   }
 }
 
+// A row-major rows x cols matrix to its transpose (dst[c][r] = src[r][c]):
+// a map between the original layout [D][H][W] = [(D H)][W] and the layout of
+// the W passes [W][D][H] = [W][(D H)] (2D: [H][W] and [W][H]).  32x32 tiles
+// through shared memory, full 128-byte lines read and written; one block per
+// tile on a 1D grid (rows / 32 may exceed a grid's y extent).
+__global__ void fg_transpose2d_kernel(const float *__restrict__ src, float *__restrict__ dst, long long rows,
+                                      int cols) {
+  __shared__ float tile[32][33];
+  const long long tc = (cols + 31) / 32;
+  const long long b = blockIdx.x;
+  const long long r0 = (b / tc) * 32;
+  const int c0 = (int)(b % tc) * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const long long r = r0 + y;
+    const int c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[y][threadIdx.x] = src[r * cols + c];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int c = c0 + y;
+    const long long r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[(long long)c * rows + r] = tile[threadIdx.x][y];
+  }
+}
+
 dim3 ew_grid(long long n) {
   long long b = (n + 255) / 256;
   return dim3((unsigned)std::min<long long>(std::max<long long>(b, 1), 152 * 16));
@@ -539,6 +564,7 @@ struct ProfileState {
   std::vector<int> steps;     // pass length of each recorded launch
   std::vector<float> last_ms; // per-launch times of the last closed window
   std::vector<int> last_steps;
+  int aux = 0, last_aux = 0;  // kernel launches besides one per pass (chunks after the first, map transposes)
 };
 ProfileState &profile() {
   static ProfileState p;
@@ -546,6 +572,12 @@ ProfileState &profile() {
 }
 
 std::mutex g_launch_mu;  // serialises the per-device function attribute set-up
+
+void count_aux_launches(int n) {
+  ProfileState &ps = profile();
+  std::lock_guard<std::mutex> g(ps.mu);
+  if (ps.on) ps.aux += n;
+}
 
 // Runs `launch` on stream s, bracketed by timing events while profiling is on;
 // vp: cells x maps the launch updates, steps: its sequential steps.
@@ -584,6 +616,7 @@ int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bo
     if (!p.chunked)
       return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
     // one ordinary launch per chunk of S steps, in stream order
+    count_aux_launches((a.L + p.S - 1) / p.S - 1);
     for (int t0 = 0; t0 < a.L; t0 += p.S) {
       PassArgs b = a;
       b.t_begin = t0;
@@ -658,9 +691,18 @@ void axes_for(const Geometry &g, Axis *ax, int *nax) {
 // wt, &plan)` picks the plan and `emit(args, plan, cross, M, mode, wt)` gets
 // the pass's arguments (all but the halo exchange fields).  Returns the first
 // non-FG_OK code of either.
-template <typename PlanFn, typename Emit>
+//
+// A pass that changes layout on a cluster plan (a strip of whole rows per
+// SM, thousands of own cells) would write S-element segments of every own
+// cell at each flush, one memory transaction each: measured, that doubles
+// the pass.  With `emit_t` such a pass writes in place and
+// `emit_t(src, dst, rows, cols)` then transposes each map (a rows x cols
+// matrix) into the other layout at full-line width.  Without it (nullptr)
+// every pass writes its own layout change.
+using NoTranspose = int (*)(const float *, float *, long long, long long);
+template <typename PlanFn, typename Emit, typename EmitT>
 int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, const MapSet &ms, int iterations,
-                  PlanFn plan_fn, Emit emit) {
+                  PlanFn plan_fn, Emit emit, EmitT *emit_t) {
   if (g.P == 0 || iterations <= 0) return FG_OK;
   Axis ax[3];
   int nax = 0;
@@ -684,6 +726,12 @@ int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, con
           Plan p;
           int rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, wt, &p);
           if (rc != FG_OK) return rc;
+          const bool split = wt && emit_t != nullptr && p.cluster;  // in place, then a transpose
+          if (split) {
+            rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, false, &p);
+            if (rc != FG_OK) return rc;
+          }
+          const bool pwt = wt && !split;  // this launch changes layout itself
           PassArgs a{};
           a.img = A.transposed ? img_t : img_r;
           a.img_cs = g.P;
@@ -691,7 +739,7 @@ int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, con
           for (int m = 0; m < M; m++) {
             float *rbuf = ms.r[m0 + m], *tbuf = ms.t[m0 + m];
             a.dsrc[m] = A.transposed ? tbuf : rbuf;
-            a.ddst[m] = to_t ? tbuf : (to_r ? rbuf : const_cast<float *>(a.dsrc[m]));
+            a.ddst[m] = pwt ? (to_t ? tbuf : rbuf) : const_cast<float *>(a.dsrc[m]);
             a.lg[m] = ms.lg;
             for (int n = 0; n < 9; n++) a.e[m][n] = ms.le * A.ld[n];
           }
@@ -701,7 +749,11 @@ int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, con
           a.st1 = A.st1;
           a.N1 = A.N1;
           a.N2 = A.N2;
-          if (to_t) {  // write [W][H] / [W][D][H]: element (step, c1, c2 = w)
+          if (!pwt) {
+            a.ws_str = A.s_str;
+            a.wst1 = A.st1;
+            a.wst2 = 1;
+          } else if (to_t) {  // write [W][H] / [W][D][H]: element (step, c1, c2 = w)
             a.ws_str = 1;
             a.wst1 = g.is3d ? g.H : 0;
             a.wst2 = g.is3d ? DH : g.H;
@@ -730,9 +782,19 @@ int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, con
                   (reinterpret_cast<uintptr_t>(a.ddst[m]) & 15) == 0;
           a.vec = vec ? 1 : 0;
           a.P = p.P;
-          a.wt = wt ? 1 : 0;
-          rc = emit(a, p, cross, M, mode, wt);
+          a.wt = pwt ? 1 : 0;
+          rc = emit(a, p, cross, M, mode, pwt);
           if (rc != FG_OK) return rc;
+          if (split) {
+            // [(D H)][W] -> [W][(D H)] after the pass that hands over to the W
+            // passes, back after the last W pass (2D: [H][W] and [W][H])
+            const long long DHr = g.is3d ? DH : g.H;
+            for (int m = 0; m < M; m++) {
+              rc = to_t ? (*emit_t)(ms.r[m0 + m], ms.t[m0 + m], DHr, g.W)
+                        : (*emit_t)(ms.t[m0 + m], ms.r[m0 + m], (long long)g.W, DHr);
+              if (rc != FG_OK) return rc;
+            }
+          }
         }
       }
     }
@@ -764,7 +826,14 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
     (*launch_counter)++;
     return launch_pass(a, p, cross, M, mode, wt, s);
   };
-  return for_each_pass(g, img_r, img_t, ms, iterations, plan_fn, emit);
+  auto emit_t = [&](const float *src, float *dst, long long rows, long long cols) {
+    const long long tiles = ((rows + 31) / 32) * ((cols + 31) / 32);
+    fg_transpose2d_kernel<<<dim3((unsigned)tiles), dim3(32, 8), 0, s>>>(src, dst, rows, (int)cols);
+    FG_CUDA(cudaGetLastError());
+    count_aux_launches(1);
+    return FG_OK;
+  };
+  return for_each_pass(g, img_r, img_t, ms, iterations, plan_fn, emit, &emit_t);
 }
 
 int check_common(const float *image, int C, int D, int H, int W, const float *mask, int Cm, const float *out) {
@@ -922,6 +991,7 @@ int fg_profile_begin(void) {
   ps.ev.clear();
   ps.vp.clear();
   ps.steps.clear();
+  ps.aux = 0;
   ps.on = true;
   return FG_OK;
 }
@@ -951,7 +1021,17 @@ int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_passes) {
   ps.ev.clear();
   ps.vp.clear();
   ps.steps.clear();
+  ps.last_aux = ps.aux;
+  ps.aux = 0;
   return rc;
+}
+
+int fg_profile_aux_launches(int *n) {
+  if (!n) return fail(FG_ERR_INVALID_ARGUMENT, "profile query: null output");
+  ProfileState &ps = profile();
+  std::lock_guard<std::mutex> g(ps.mu);
+  *n = ps.last_aux;
+  return FG_OK;
 }
 
 int fg_profile_launch_times(float *ms, int *steps, int cap, int *n) {
@@ -1236,7 +1316,7 @@ int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int clu
       out.push_back(j);
       return FG_OK;
     };
-    rc = for_each_pass(g, it.image, it.image_t, ms, iterations, plan_fn, emit);
+    rc = for_each_pass(g, it.image, it.image_t, ms, iterations, plan_fn, emit, static_cast<NoTranspose *>(nullptr));
     if (rc != FG_OK) return rc;
     if (sg) {
       Batch3dJob epi = pro;

@@ -136,6 +136,10 @@ FG_API int fg_profile_end(double *pass_ms, int *pass_launches, double *voxel_pas
  * order: up to `cap` entries of ms and of steps swept (the pass length);
  * *n receives the number recorded. */
 FG_API int fg_profile_launch_times(float *ms, int *steps, int cap, int *n);
+/* Kernel launches of the window closed by the last fg_profile_end besides
+ * one per pass: the launches after the first of a chunked pass, and the map
+ * transposes that follow a layout-changing pass on a cluster plan. */
+FG_API int fg_profile_aux_launches(int *n);
 
 /* Reads (and clears) the device status word of a workspace after
  * synchronising `stream`: FG_OK, or FG_ERR_TIMEOUT if a kernel gave up. */
