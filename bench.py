@@ -604,8 +604,13 @@ def fp64_check(got, image, mask, v, lamb, iters, spacing=None):
     got = np.asarray(got, np.float64)
     err = np.abs(got - ref)
     rel = err / np.maximum(np.abs(ref), 1e-30)
+    # a distance is a sum of up to about (sum of the extents) rounded float32
+    # additions, each off by at most 2^-24 of the running value
+    path = int(sum(got.shape[-3:] if spacing is not None else got.shape[-2:]))
+    bound = path * 2.0 ** -23
     return {"lamb": lamb, "max_abs_err": float(err.max()), "max_rel_err": float(rel.max()),
-            "within_1e-5_rel_1e-4_abs": bool(np.all(err <= 1e-4 + 1e-5 * np.abs(ref))),
+            "rel_bound": bound, "within_bound": bool(np.all(err <= 1e-4 + bound * np.abs(ref))),
+            "bound_note": "1e-4 + (sum of extents) * 2^-23 relative: float32 rounding along a path",
             "reference": "oracle float64 scan of the same inputs", "seconds": round(time.perf_counter() - t0, 2)}
 
 
@@ -1201,22 +1206,34 @@ def run_gpu_arm(args, w, rank, world):
                  "seconds": round(time.perf_counter() - t_tune, 2)}
 
     # the step's transforms are independent: one CUDA stream each, so their
-    # passes share the SMs (each call runs on the current stream)
+    # passes share the SMs (each call runs on the current stream); the
+    # costliest arithmetic goes first, on the highest-priority stream, since
+    # the step ends with its slowest transform
+    from fastgeodis_gb300.batch3d import priority_streams, transform_cost
+
     main = torch.cuda.current_stream()
-    streams = [torch.cuda.Stream() for _ in w["lambs"]]
+    n_tr = len(w["lambs"])
+    vol = tuple(int(x) for x in d_in[0][0].shape[1:])
+    vol = vol if len(vol) == 4 else (vol[0], 1) + vol[1:]
+    order = sorted(range(n_tr), key=lambda i: -transform_cost(vol, w["lambs"][i]))
+    by_rank = priority_streams(n_tr)
+    streams = [None] * n_tr
+    for r, i in enumerate(order):
+        streams[i] = by_rank[r]
 
     f3, f2 = transform_fns(fg, w)
 
     def step(inputs):
-        outs = []
+        outs = [None] * n_tr
         for s in streams:
             s.wait_stream(main)
-        for lamb, s, (im, mk) in zip(w["lambs"], streams, inputs):
+        for i in order:
+            lamb, s, (im, mk) = w["lambs"][i], streams[i], inputs[i]
             with torch.cuda.stream(s):
                 if w["dims"] == 3:
-                    outs.append(f3(im, mk, w["spacing"], w["v"], lamb, w["iters"]))
+                    outs[i] = f3(im, mk, w["spacing"], w["v"], lamb, w["iters"])
                 else:
-                    outs.append(f2(im, mk, w["v"], lamb, w["iters"]))
+                    outs[i] = f2(im, mk, w["v"], lamb, w["iters"])
         for s in streams:
             main.wait_stream(s)
         return outs
