@@ -353,7 +353,7 @@ class PersistentBatch3d:
     def _plan_with(self, items, G):
         L = _lib.load()
         n = len(self.shapes)
-        cap = max(1, n * (2 + 6 * max(self.iterations, 0)))
+        cap = max(1, n * (2 + 10 * max(self.iterations, 0)))  # fg_batch3d_plan's bound
         buf = (ctypes.c_ubyte * (cap * self.job_bytes))()
         info = (ctypes.c_int * 5)()
         rc = L.fg_batch3d_plan(items, n, self.iterations, G, self._status.data_ptr(), buf, len(buf), info)

@@ -38,6 +38,39 @@ __device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
+// dst[c][r] = src[r][c] for a rows x cols matrix, shared out over the
+// cluster's CTAs: each warp moves one 32 x 32 tile at a time through its own
+// padded shared tile (32 independent row loads in flight per lane, full
+// 128-byte lines read and written, no block barrier).
+__device__ void transpose_tiles(const float *src, float *dst, long long rows, int cols, float *sm, unsigned rank,
+                                unsigned G) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  float(*tile)[33] = reinterpret_cast<float(*)[33]>(sm + warp * 32 * 33);
+  const long long tc = (cols + 31) / 32, ntiles = ((rows + 31) / 32) * tc;
+  for (long long k = (long long)rank * nwarps + warp; k < ntiles; k += (long long)G * nwarps) {
+    const long long r0 = (k / tc) * 32;
+    const int c0 = (int)(k % tc) * 32;
+    const int c = c0 + lane;
+    // all 32 row loads of the lane in flight before the first store
+    float v[32];
+#pragma unroll
+    for (int y = 0; y < 32; y++) {
+      const long long r = r0 + y;
+      v[y] = (r < rows && c < cols) ? __ldg(src + r * cols + c) : 0.0f;
+    }
+#pragma unroll
+    for (int y = 0; y < 32; y++) tile[y][lane] = v[y];
+    __syncwarp();
+    const long long r = r0 + lane;
+#pragma unroll
+    for (int y = 0; y < 32; y++) {
+      const int cc = c0 + y;
+      if (r < rows && cc < cols) dst[(long long)cc * rows + r] = tile[lane][y];
+    }
+    __syncwarp();
+  }
+}
+
 // Initial distances (v*M, and v*(1-M) for the signed form's second map) and
 // the transposed image copy [C][W][D][H], shared out over the cluster's CTAs.
 __device__ void run_prologue(const Batch3dJob &jb, float *sm, unsigned rank, unsigned G) {
@@ -50,32 +83,9 @@ __device__ void run_prologue(const Batch3dJob &jb, float *sm, unsigned rank, uns
     if (jb.is_signed) jb.d2[i] = __fmul_rn(v, __fsub_rn(1.0f, m));
   }
   if (!jb.image_t) return;
-  // 32 x 32 tiles of each [H][W] slice, through a padded shared tile
-  float(*tile)[33] = reinterpret_cast<float(*)[33]>(sm);
-  const int D = jb.D, H = jb.H, W = jb.W;
-  const int ntw = (W + 31) / 32, nth = (H + 31) / 32;
-  const long long ntiles = (long long)jb.C * D * nth * ntw;
-  const int x = tid & 31, y0 = tid >> 5, ys = NT >> 5;
-  for (long long k = rank; k < ntiles; k += G) {
-    const int tw = (int)(k % ntw);
-    const long long r1 = k / ntw;
-    const int th = (int)(r1 % nth);
-    const long long cd = r1 / nth;  // channel * D + d
-    const int c = (int)(cd / D), d = (int)(cd - (long long)c * D);
-    const float *s = jb.image + c * P + (long long)d * H * W;
-    float *o = jb.image_t + c * P + (long long)d * H;
-    const int w0 = tw * 32, h0 = th * 32;
-    for (int y = y0; y < 32; y += ys) {
-      const int h = h0 + y, w = w0 + x;
-      if (h < H && w < W) tile[y][x] = s[(long long)h * W + w];
-    }
-    __syncthreads();
-    for (int y = y0; y < 32; y += ys) {
-      const int w = w0 + y, h = h0 + x;
-      if (h < H && w < W) o[(long long)w * D * H + h] = tile[x][y];
-    }
-    __syncthreads();
-  }
+  // each channel [(D H)][W] -> [W][(D H)]
+  for (int c = 0; c < jb.C; c++)
+    transpose_tiles(jb.image + c * P, jb.image_t + c * P, (long long)jb.D * jb.H, jb.W, sm, rank, G);
 }
 
 // D(M) - D(1 - M) of the signed form.
@@ -89,7 +99,7 @@ __device__ void run_epilogue(const Batch3dJob &jb, unsigned rank, unsigned G) {
 // MODE: the batch's arithmetic mode when every pass shares it, else
 // MODE_GENERAL, whose candidate expression gives the other modes' bits too
 // (l_grad = 0 adds +0, l_eucl = 0 adds +0 and l_grad = 1 multiplies by 1).
-// The transposed write is read from the job (one body, no spills).
+// No pass writes transposed (layout changes are transpose jobs).
 template <int M, int MODE>
 __device__ void run_pass(const Batch3dJob &jb, float *sm, unsigned rank) {
   // the pass's arguments in shared memory: the step loop reads them there
@@ -108,7 +118,7 @@ __device__ void run_pass(const Batch3dJob &jb, float *sm, unsigned rank) {
     cl_sync();
     return;
   }
-  cluster_body<1, M, MODE, 2, 2>(a, sm);
+  cluster_body<1, M, MODE, 0, 2>(a, sm);
 }
 
 template <int M, int MODE>
@@ -144,6 +154,7 @@ __global__ void __maxnreg__(128) fg_batch3d_kernel(const Batch3dJob *jobs, int n
       __syncthreads();
       if (jb.kind == JOB3_PASS) run_pass<M, MODE>(jb, sm, rank);
       else if (jb.kind == JOB3_PROLOGUE) run_prologue(jb, sm, rank, G);
+      else if (jb.kind == JOB3_TRANSPOSE) transpose_tiles(jb.tsrc, jb.tdst, jb.trows, jb.tcols, sm, rank, G);
       else run_epilogue(jb, rank, G);
     }
     __threadfence();

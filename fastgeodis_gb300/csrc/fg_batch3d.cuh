@@ -6,15 +6,17 @@
 // the transposed image copy), its passes in order (each a cluster-plan pass:
 // the cluster's CTAs own strips of whole rows of the cross-section, rows
 // exchanged through distributed shared memory), and for the signed form an
-// epilogue (D(M) - D(1 - M)).  Job k of a volume may start once its job k - 1
-// has finished (a per-volume progress counter).
+// epilogue (D(M) - D(1 - M)).  A pass that hands over to the passes along W,
+// and the last of those, run in place and are followed by a transpose job
+// ([(D H)][W] <-> [W][(D H)]).  Job k of a volume may start once its job
+// k - 1 has finished (a per-volume progress counter).
 #pragma once
 
 #include "fg_common.cuh"
 
 namespace fgi {
 
-enum Batch3dJobKind { JOB3_PROLOGUE = 0, JOB3_PASS = 1, JOB3_EPILOGUE = 2 };
+enum Batch3dJobKind { JOB3_PROLOGUE = 0, JOB3_PASS = 1, JOB3_EPILOGUE = 2, JOB3_TRANSPOSE = 3 };
 
 struct Batch3dJob {
   PassArgs a;         // JOB3_PASS: the pass (tiles1 strips; rank >= tiles1 idles)
@@ -29,6 +31,11 @@ struct Batch3dJob {
   int C, D, H, W;
   float v;
   int is_signed;
+  // transpose: tdst[c][r] = tsrc[r][c] for a trows x tcols matrix
+  const float *tsrc;
+  float *tdst;
+  long long trows;
+  int tcols;
 };
 
 // Launch of the persistent kernel for maps per pass M (1 plain, 2 signed)

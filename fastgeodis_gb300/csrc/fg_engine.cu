@@ -699,7 +699,6 @@ void axes_for(const Geometry &g, Axis *ax, int *nax) {
 // `emit_t(src, dst, rows, cols)` then transposes each map (a rows x cols
 // matrix) into the other layout at full-line width.  Without it (nullptr)
 // every pass writes its own layout change.
-using NoTranspose = int (*)(const float *, float *, long long, long long);
 template <typename PlanFn, typename Emit, typename EmitT>
 int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, const MapSet &ms, int iterations,
                   PlanFn plan_fn, Emit emit, EmitT *emit_t) {
@@ -1316,7 +1315,19 @@ int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int clu
       out.push_back(j);
       return FG_OK;
     };
-    rc = for_each_pass(g, it.image, it.image_t, ms, iterations, plan_fn, emit, static_cast<NoTranspose *>(nullptr));
+    auto emit_t = [&](const float *src, float *dst, long long rows, long long cols) {
+      Batch3dJob j{};
+      j.kind = JOB3_TRANSPOSE;
+      j.vol = v;
+      j.seq = seq++;
+      j.tsrc = src;
+      j.tdst = dst;
+      j.trows = rows;
+      j.tcols = (int)cols;
+      out.push_back(j);
+      return FG_OK;
+    };
+    rc = for_each_pass(g, it.image, it.image_t, ms, iterations, plan_fn, emit, &emit_t);
     if (rc != FG_OK) return rc;
     if (sg) {
       Batch3dJob epi = pro;
@@ -1325,21 +1336,21 @@ int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int clu
       out.push_back(epi);
     }
   }
-  // staging depth and flush period of each pass for the launch's CTA size
-  size_t smem = 32 * 33 * 4;  // the prologue's transpose tile
+  // staging depth of each pass for the launch's CTA size (no pass writes
+  // transposed: the layout changes are transpose jobs)
+  size_t smem = (size_t)(threads / 32) * 32 * 33 * 4;  // a transpose tile per warp
   for (Batch3dJob &j : out) {
     if (j.kind != JOB3_PASS) continue;
+    if (j.wt) return fail(FG_ERR_UNSUPPORTED, "batch3d plan: a pass writes transposed");
     PassArgs &a = j.a;
     bool fit = false;
-    for (int S = j.wt ? 8 : 8; S >= 2 && !fit; S = j.wt ? S / 2 : 0) {
-      for (int P = 8; P >= 2 && !fit; P /= 2) {
-        const ClusterLayout ly = cluster_layout(cimg, M, j.wt ? S : 2, a.T1, a.N2, threads, 2, P, j.wt != 0);
-        if ((size_t)ly.bytes <= kSmemBudget) {
-          a.S = S;
-          a.P = P;
-          smem = std::max(smem, (size_t)ly.bytes);
-          fit = true;
-        }
+    for (int P = 8; P >= 2 && !fit; P /= 2) {
+      const ClusterLayout ly = cluster_layout(cimg, M, 2, a.T1, a.N2, threads, 2, P, false);
+      if ((size_t)ly.bytes <= kSmemBudget) {
+        a.S = 8;
+        a.P = P;
+        smem = std::max(smem, (size_t)ly.bytes);
+        fit = true;
       }
     }
     if (!fit) return fail(FG_ERR_UNSUPPORTED, "batch3d plan: a pass's rings do not fit the shared memory");
@@ -1356,9 +1367,9 @@ int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int clu
   if (debug)
     for (const Batch3dJob &j : out)
       fprintf(stderr, "[fg batch3d] kind=%d vol=%d seq=%d mode=%d wt=%d L=%d dir=%d N=%dx%d T1=%d tiles1=%d S=%d P=%d "
-                      "s_str=%lld st1=%lld ws=%lld,%lld,%lld vec=%d\n",
+                      "s_str=%lld st1=%lld ws=%lld,%lld,%lld vec=%d transpose=%lldx%d\n",
               j.kind, j.vol, j.seq, j.mode, j.wt, j.a.L, j.a.dir, j.a.N1, j.a.N2, j.a.T1, j.a.tiles1, j.a.S, j.a.P,
-              j.a.s_str, j.a.st1, j.a.ws_str, j.a.wst1, j.a.wst2, j.a.vec);
+              j.a.s_str, j.a.st1, j.a.ws_str, j.a.wst1, j.a.wst2, j.a.vec, j.trows, j.tcols);
   info[0] = (int)out.size();
   info[1] = threads;
   info[2] = (int)smem;

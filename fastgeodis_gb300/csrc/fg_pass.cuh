@@ -819,6 +819,13 @@ int launch_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStream_t s)
 
 template <int CROSS, bool CLU = false>
 int launch_cross(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
+  if constexpr (CLU) {
+    // a cluster plan changes layout as an in-place pass and a transpose (the engine's pass generator)
+    if (wt) return set_error(FG_ERR_UNSUPPORTED, "cluster plans do not write transposed");
+    if (M == 1) return launch_mode<CROSS, 1, false, CLU>(a, c, mode, s);
+    if (M == 2) return launch_mode<CROSS, 2, false, CLU>(a, c, mode, s);
+    return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
+  }
   if (M == 1)
     return wt ? launch_mode<CROSS, 1, true, CLU>(a, c, mode, s) : launch_mode<CROSS, 1, false, CLU>(a, c, mode, s);
   if (M == 2)

@@ -58,9 +58,12 @@ int cluster_capacity(int size, int threads, size_t smem, int *out) {
   return FG_OK;
 }
 
+// A cluster plan changes layout as an in-place pass followed by a transpose
+// (the engine's pass generator): no variant here writes transposed.
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
-  if (M == 1) return wt ? launch_sweep_mode<1, true>(a, c, mode, s) : launch_sweep_mode<1, false>(a, c, mode, s);
-  if (M == 2) return wt ? launch_sweep_mode<2, true>(a, c, mode, s) : launch_sweep_mode<2, false>(a, c, mode, s);
+  if (wt) return set_error(FG_ERR_UNSUPPORTED, "cluster plans do not write transposed");
+  if (M == 1) return launch_sweep_mode<1, false>(a, c, mode, s);
+  if (M == 2) return launch_sweep_mode<2, false>(a, c, mode, s);
   return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
 }
 

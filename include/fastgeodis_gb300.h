@@ -87,8 +87,9 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * only, S >= 2) asks for a cluster plan instead: ceil(N1 / T1) CTAs (2 to
  * 16) of one thread-block cluster each own T1 whole rows, and exchange their
  * boundary rows every step through distributed shared memory, with no halo
- * and no hand-off through global memory; T2 is ignored and S is the
- * transposed write's flush period.  With FG_PLAN_RUNS2 (and at most one image
+ * and no hand-off through global memory; T2 is ignored, and so is S (a
+ * pass that changes layout runs in place on a cluster plan and a tiled
+ * transpose then moves the map).  With FG_PLAN_RUNS2 (and at most one image
  * channel read) the strips run on the cluster sweep kernel, each thread
  * owning 2 vertically adjacent runs (T1 is rounded up to an even number), at
  * most 512 threads per CTA.  With FG_PLAN_CHUNKED a tile plan runs as one
@@ -334,7 +335,9 @@ typedef struct fg_batch3d_item {
  *
  * fg_batch3d_plan builds the job records on the host into `jobs` (host
  * memory, `jobs_bytes` bytes; fg_batch3d_job_bytes() each, at most
- * n * (2 + 6 * iterations) jobs) and writes info[0] = jobs, info[1] =
+ * n * (2 + 10 * iterations) jobs: a prologue, six passes and a transpose of
+ * each map before and after the passes along W per iteration, an epilogue)
+ * and writes info[0] = jobs, info[1] =
  * threads per CTA, info[2] = shared-memory bytes per CTA, info[3] = maps per
  * pass, info[4] = arithmetic mode of the launch; `status` is the device word
  * a wait that runs out writes FG_ERR_TIMEOUT to.  FG_ERR_WORKSPACE when

@@ -72,25 +72,27 @@ def _plan(shapes, lambs, signed=False, C=1, G=16, iterations=4):
 
     L = _lib.load()
     info = (ctypes.c_int * 5)()
-    buf = (ctypes.c_ubyte * (len(shapes) * (2 + 6 * iterations) * L.fg_batch3d_job_bytes()))()
+    buf = (ctypes.c_ubyte * (len(shapes) * (2 + 10 * iterations) * L.fg_batch3d_job_bytes()))()
     rc = L.fg_batch3d_plan(_items(shapes, lambs, signed, C), len(shapes), iterations, G, None, buf, len(buf), info)
     return rc, list(info)
 
 
 def test_one_launch_plan_jobs_and_shape():
     """The one-launch batch's job list (built on the host, no GPU): a prologue,
-    every pass and (signed) an epilogue per volume; the launch's arithmetic
-    mode is the shared one or the general expression; refusals."""
+    every pass, a transpose of each map after the pass that hands over to the
+    passes along W and after the last of those, and (signed) an epilogue per
+    volume; the launch's arithmetic mode is the shared one or the general
+    expression; refusals."""
     from fastgeodis_gb300 import _lib
 
     rc, info = _plan([(20, 33, 27), (7, 18, 40)], [0.5, 0.0])
-    assert rc == 0 and info[0] == 2 * (1 + 24) and info[3] == 1 and info[4] == 0
+    assert rc == 0 and info[0] == 2 * (1 + 24 + 2 * 4) and info[3] == 1 and info[4] == 0
     rc, info = _plan([(8, 8, 8)], [1.0], signed=True, G=4)
-    assert rc == 0 and info[0] == 1 + 24 + 1 and info[3] == 2 and info[4] == 2
+    assert rc == 0 and info[0] == 1 + 24 + 4 * 4 + 1 and info[3] == 2 and info[4] == 2
     rc, info = _plan([(16, 16, 16)] * 3, [0.0] * 3)
     assert rc == 0 and info[4] == 1 and info[1] <= 512 and info[2] <= 227 * 1024
     rc, info = _plan([(1, 9, 13)], [0.5], iterations=2)  # D = 1: the passes along D move no data
-    assert rc == 0 and info[0] == 1 + 2 * 4
+    assert rc == 0 and info[0] == 1 + 2 * (4 + 2)
     assert _plan([(8, 8, 8)], [0.5], C=2)[0] == _lib.FG_ERR_UNSUPPORTED  # one image channel read
     assert _plan([(8, 8, 8)], [0.0], C=3)[0] == 0                        # ... unless lamb = 0
     assert _plan([(64, 256, 256)], [0.5], G=2)[0] == _lib.FG_ERR_UNSUPPORTED  # section too large for 2 CTAs
