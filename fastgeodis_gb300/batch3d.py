@@ -33,6 +33,24 @@ def _voxels(shape: Sequence[int]) -> int:
     return shape[1] * shape[2] * shape[3]
 
 
+def _slot_key(shape: Sequence[int]):
+    return (-_voxels(shape), tuple(shape))
+
+
+def slot_order(shapes: Sequence[Sequence[int]]) -> List[int]:
+    """Order of a batch's stream slots: largest volumes first, equal shapes
+    together (a slot's workspace depends on the shape only)."""
+    return sorted(range(len(shapes)), key=lambda i: _slot_key(shapes[i]))
+
+
+def launch_order(shapes: Sequence[Sequence[int]], lambs: Sequence[float]) -> List[int]:
+    """The order a batch launches its transforms in: the slot order, and
+    among equal shapes the costlier arithmetic first (on the higher-priority
+    streams).  Position k holds a volume of the same shape as in
+    :func:`slot_order`, so the slots' workspaces fit whatever the weights."""
+    return sorted(range(len(shapes)), key=lambda i: (_slot_key(shapes[i]), -transform_cost(shapes[i], lambs[i])))
+
+
 def _check_item(image: torch.Tensor, mask: torch.Tensor, device) -> None:
     if image.dim() != 5 or mask.dim() != 5:
         raise ValueError("batch items must be [1, C, D, H, W] volumes with [1, 1, D, H, W] soft masks")
@@ -137,7 +155,7 @@ class GeodesicBatch3d:
             self.outputs = [torch.empty((1, 1) + s[1:], device=dev) for s in self.shapes]
             self.streams = priority_streams(max(1, min(int(streams), n)), dev)
             # largest first, so that the pool finishes with the short transforms
-            self.order = sorted(range(n), key=lambda i: -_voxels(self.shapes[i]))
+            self.order = slot_order(self.shapes)
             op = _lib.FG_OP_SIGNED if self.signed else _lib.FG_OP_PLAIN
             need = [0] * len(self.streams)
             for slot, i in enumerate(self.order):
@@ -201,10 +219,7 @@ class GeodesicBatch3d:
         main = torch.cuda.current_stream(self.device)
         for s in self.streams:
             s.wait_stream(main)
-        # largest first (the slots' workspaces are sized in that order); among
-        # equal sizes the costlier arithmetic first, on the higher-priority streams
-        order = sorted(range(len(self.shapes)), key=lambda i: (-_voxels(self.shapes[i]),
-                                                               -transform_cost(self.shapes[i], self.lambs[i])))
+        order = launch_order(self.shapes, self.lambs)
         for slot, i in enumerate(order):
             k = slot % len(self.streams)
             C, D, H, W = self.shapes[i]

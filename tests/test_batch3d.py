@@ -98,3 +98,25 @@ def test_one_launch_plan_jobs_and_shape():
     assert _plan([(64, 256, 256)], [0.5], G=2)[0] == _lib.FG_ERR_UNSUPPORTED  # section too large for 2 CTAs
     rc, info = _plan([(8, 8, 8)] * 2, [0.5, 0.5], G=16, iterations=1)
     assert rc == 0
+
+
+def test_launch_order_keeps_each_slot_shape():
+    """The launch order (costliest arithmetic first among equal shapes) puts
+    a volume of the same shape at every slot position as the order the slots'
+    workspaces were sized in, whatever the weights; the costliest mode leads
+    its shape group."""
+    import numpy as np
+
+    from fastgeodis_gb300.batch3d import launch_order, slot_order, transform_cost
+
+    rng = np.random.default_rng(5)
+    pool = [(1, 16, 32, 64), (1, 64, 32, 16), (1, 32, 32, 32), (3, 16, 32, 64), (1, 8, 8, 8)]
+    for _ in range(50):
+        shapes = [pool[int(k)] for k in rng.integers(0, len(pool), 9)]
+        lambs = [float(x) for x in rng.choice([0.0, 0.3, 0.5, 1.0], 9)]
+        a, b = slot_order(shapes), launch_order(shapes, lambs)
+        assert sorted(b) == list(range(9))
+        assert [shapes[i] for i in a] == [shapes[i] for i in b]
+        for k in range(8):
+            if shapes[b[k]] == shapes[b[k + 1]]:
+                assert transform_cost(shapes[b[k]], lambs[b[k]]) >= transform_cost(shapes[b[k + 1]], lambs[b[k + 1]])
