@@ -107,3 +107,42 @@ def test_planner_chunks_a_volume_with_large_slices():
     got = fg.signed_generalised_geodesic3d(ti, tm, SP, 1e10, 0.5, 1)[0].cpu().numpy()
     assert bits_equal(got, oracle.signed3d(img, m, SP, 1e10, 0.5, 1))
     fg.check_status()
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_shapes_chunked_and_cluster_plans(seed):
+    """Seeded random volumes, each pass cross-section pinned to a random
+    chunked tile plan or cluster plan (whose layout-changing passes run in
+    place and are followed by a transpose), random weights, plain or signed:
+    the oracle's bits."""
+    rng = np.random.default_rng(100 + seed)
+    shape = tuple(int(x) for x in rng.integers(5, 41, 3))
+    C = int(rng.choice([1, 1, 2, 5]))
+    lamb = float(rng.choice([0.0, 0.35, 1.0]))
+    signed = bool(rng.integers(0, 2))
+    img, m = _case(shape, C, 200 + seed, soft=True)
+    plans = {}
+    for key in tune.pass_keys(shape):
+        _, N1, N2 = key
+        if rng.integers(0, 2) and N1 >= 2 and C == 1:
+            G = int(rng.integers(2, min(N1, 16) + 1))
+            plans[key] = (8, -(-N1 // G), N2, _lib.FG_PLAN_CLUSTER | (_lib.FG_PLAN_RUNS2 if rng.integers(0, 2) else 0))
+        else:
+            S = int(rng.choice([2, 4, 8]))
+            T1 = max(S, int(rng.integers(S, max(S + 1, N1))))
+            T2 = max(4, (int(rng.integers(S, max(S + 1, N2))) + 3) // 4 * 4)
+            plans[key] = (S, T1, T2, CH)
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    try:
+        tune.pin(plans)
+        if signed:
+            got = fg.signed_generalised_geodesic3d(ti, tm, SP, 1e10, lamb, 2)
+            want = oracle.signed3d(img, m, SP, 1e10, lamb, 2)
+        else:
+            got = fg.generalised_geodesic3d(ti, tm, SP, 1e10, lamb, 2)
+            want = oracle.geodesic3d(img, m, SP, 1e10, lamb, 2)
+        got = got[0].cpu().numpy()
+        assert bits_equal(got, want), (shape, C, lamb, signed, plans)
+        fg.check_status()
+    finally:
+        tune.clear(shape)
