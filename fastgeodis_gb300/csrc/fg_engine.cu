@@ -815,14 +815,18 @@ int run_transform(const Geometry &g, const float *img_r, const float *img_t, con
     return FG_OK;
   };
   auto emit = [&](PassArgs &a, const Plan &p, int cross, int M, int mode, bool wt) {
-    if (*launch_counter >= 0xFFFFu) {  // epochs would repeat: clear the exchange words
+    // chunk epochs of this pass: base + 1 ... base + L/S; a pass of 65536 or
+    // more chunks takes as many counter values as its epochs need, so no two
+    // passes of the call share an epoch
+    const unsigned slots = (unsigned)(((long long)a.L + a.S - 1) / a.S / 65536) + 1;
+    if (*launch_counter + slots > 0xFFFFu) {  // epochs would repeat: clear the exchange words
       FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
       *launch_counter = 0;
     }
     a.xch = w.xch;
-    a.epoch_base = (*launch_counter) << 16;  // chunk epochs of this launch: base + 1 ... base + L/S
+    a.epoch_base = (*launch_counter) << 16;
     a.status = w.status;
-    (*launch_counter)++;
+    *launch_counter += slots;
     return launch_pass(a, p, cross, M, mode, wt, s);
   };
   auto emit_t = [&](const float *src, float *dst, long long rows, long long cols) {

@@ -146,3 +146,22 @@ def test_random_shapes_chunked_and_cluster_plans(seed):
         fg.check_status()
     finally:
         tune.clear(shape)
+
+
+def test_pass_of_more_than_65536_chunks():
+    """A 70000 x 64 image on two tiles with a hand-off every step: the passes
+    along H have 70000 chunks, more epochs than one counter value spans; each
+    pass reserves its own range, so no pass reads another's exchange words."""
+    shape = (70000, 64)
+    img, m = _case(shape, 1, 31)
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    L = _lib.load()
+    try:
+        _lib.check(L.fg_plan_override(1, 1, 64, 1, 1, 32, 0))
+        p = _lib.plan_describe(1, 1, 64)
+        assert (p["S"], p["tiles2"]) == (1, 2)
+        got = fg.generalised_geodesic2d(ti, tm, 1e10, 0.7, 2)[0].cpu().numpy()
+        assert bits_equal(got, oracle.geodesic2d(img, m, 1e10, 0.7, 2))
+        fg.check_status()
+    finally:
+        tune.clear(shape)
