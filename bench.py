@@ -1009,29 +1009,37 @@ def b256_record(args, dev, rank, world, dist, n=8, steps=5):
         imgs.append(vol[None, None])
         msks.append(m[None, None])
         lambs.append([0.0, 0.5, 1.0][k % 3])
-    b = fg.GeodesicBatch3d([(1,) + shape] * len(imgs), iterations=4, use_graph=True, streams=max(1, len(imgs)),
+    b = fg.GeodesicBatch3d([(1,) + shape] * len(imgs), iterations=4, use_graph=False, streams=max(1, len(imgs)),
                            inputs=(imgs, msks), device=dev)
     b.v, b.lambs, b.spacings = 1e10, lambs, [(1.0, 1.0, 1.0)] * len(imgs)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
-    for _ in range(2):
-        b.run()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    tot = 0.0
-    for k in range(steps):
-        flush.fill_(float(k))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        b.run()
-        e1.record(stream)
-        e1.synchronize()
-        tot += e0.elapsed_time(e1)
+
+    def timed_batch(run):
+        for _ in range(2):
+            run()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        tot = 0.0
+        for k in range(steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return _max_over_ranks(tot / steps, dist, dev)
+
+    # launched from the host each step (the block scheduler honours the
+    # streams' priorities), then replayed from one captured CUDA graph
+    ms = timed_batch(b.run)
+    b.use_graph = True
+    ms_graph = timed_batch(b.run)
     b.check()
     plans = sorted({str(fg_plan) for fg_plan in b._pinned})
     b.release_plans()
-    ms = _max_over_ranks(tot / steps, dist, dev)
     streamed = [o.clone() for o in b.outputs]
     del b
     # the same batch in one persistent launch (a job queue over co-resident clusters)
@@ -1064,9 +1072,13 @@ def b256_record(args, dev, rank, world, dist, n=8, steps=5):
     peak, peak_kind = measured_peak_hbm()
     return {"workload": "8 volumes 1x1x256x256x256, smoothed (sigma 2) uniform[0,1] noise generated on the device, "
                         "one 6^3 seed cube each, spacing 1, v 1e10, iterations 4, lamb cycling 0/0.5/1",
-            "api": "GeodesicBatch3d, one CUDA graph per step, cluster plans pinned by the batch",
+            "api": "GeodesicBatch3d, 8 priority streams launched from the host each step, cluster plans pinned "
+                   "by the batch",
             "plans_pinned_for": plans, "steps": steps, "ms_per_step": round(ms, 3),
             "value": round(value, 2), "unit": "Gvoxel-passes/s",
+            "graph_replay": {"ms_per_step": round(ms_graph, 3),
+                             "value": round(vp / (ms_graph * 1e-3) / 1e9, 2),
+                             "note": "the same batch replayed from one captured CUDA graph"},
             "hbm_achieved_gbs": round(value * 12, 1), "hbm_frac": round(value * 12 / peak, 4),
             "peak_gbs": peak, "peak_source": peak_kind, "target_frac": 0.6,
             "bytes_per_voxel_pass": 12, "l2": "flushed between steps",

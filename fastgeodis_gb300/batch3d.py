@@ -88,6 +88,22 @@ def batch_plan_for(key, channels: int = 1):
     return max(cands, key=lambda c: (c[1], bool(c[3] & _lib.FG_PLAN_RUNS2)))
 
 
+def batch_general_plan_for(key, channels: int = 1):
+    """The plan a batch pins for passes of the general arithmetic (0 < lamb
+    < 1) on a cross-section whose batch plan runs the cluster sweep kernel:
+    the same strips with one run per thread (twice the warps), or None.
+    Measured on eight 256^3 volumes with mixed lambdas: 12.92 -> 12.70 ms per
+    batch (the l_eucl = 0 and l_grad = 0 passes are faster on the sweep kernel)."""
+    c = batch_plan_for(key, channels)
+    if c is None or not c[3] & _lib.FG_PLAN_RUNS2 or channels > 1:
+        return None
+    S, T1, N2 = c[0], c[1], key[2]
+    threads = T1 * -(-N2 // 4)
+    if threads > tune.THREADS_LEAN:
+        return None
+    return (S, T1, N2, _lib.FG_PLAN_CLUSTER | (_lib.FG_PLAN_LEAN if threads > tune.THREADS else 0))
+
+
 # Relative time of a pass per cell by arithmetic mode, measured on GB300
 # (256^3 passes on the cluster plan: 0.261 / 0.395 / 0.471 ms for l_grad = 0,
 # l_eucl = 0 and l_grad = 1, general).
@@ -119,7 +135,10 @@ class GeodesicBatch3d:
         signed: compute ``D(M) - D(1 - M)`` instead of ``D(M)``.
         iterations: raster-scan iterations (the reference's ``iter``).
         device: CUDA device.
-        use_graph: replay the batch from a captured CUDA graph.
+        use_graph: replay the batch from a captured CUDA graph (worth it for
+            many small volumes; on eight 256^3 volumes host launches were 5%
+            faster, 12.9 against 13.6 ms: the replay's kernels do not follow
+            the streams' priorities).
         streams: size of the stream pool (transform i runs on stream
             i mod streams; transforms on one stream share its workspace).
         plans: ``"cluster"`` pins plans for concurrent transforms on the
@@ -191,6 +210,9 @@ class GeodesicBatch3d:
             if c is not None:
                 _lib.check(L.fg_plan_override(*key, *c))
                 self._pinned.add(key)
+            g = batch_general_plan_for(key, C)
+            if g is not None:
+                _lib.check(L.fg_plan_override(*key, *g[:3], g[3] | _lib.FG_PLAN_MODE(tune.MODE_GENERAL)))
         self._graph = None
 
     def tune_plans(self, repeats: int = 2) -> None:
@@ -209,6 +231,8 @@ class GeodesicBatch3d:
         L = _lib.load()
         for key in self._pinned:
             _lib.check(L.fg_plan_override(*key, 0, 0, 0, 0))
+            for m in (tune.MODE_GENERAL, tune.MODE_EUCLID, tune.MODE_GEO):
+                _lib.check(L.fg_plan_override(*key, 0, 0, 0, _lib.FG_PLAN_MODE(m)))
         self._pinned.clear()
         self._graph = None
 

@@ -120,3 +120,24 @@ def test_launch_order_keeps_each_slot_shape():
         for k in range(8):
             if shapes[b[k]] == shapes[b[k + 1]]:
                 assert transform_cost(shapes[b[k]], lambs[b[k]]) >= transform_cost(shapes[b[k + 1]], lambs[b[k + 1]])
+
+
+def test_general_mode_batch_plans():
+    """Passes of the general arithmetic take the cluster plan's strips with
+    one run per thread where the batch plan runs the two-run sweep kernel
+    (one image channel, at most 1024 threads per CTA)."""
+    from fastgeodis_gb300 import _lib
+    from fastgeodis_gb300.batch3d import batch_general_plan_for, batch_plan_for
+
+    for key in [(2, 256, 256), (2, 128, 256), (2, 200, 300), (2, 64, 64), (2, 40, 600)]:
+        c, g = batch_plan_for(key), batch_general_plan_for(key)
+        if c is None or not c[3] & _lib.FG_PLAN_RUNS2:
+            assert g is None
+            continue
+        if g is None:
+            continue
+        assert g[:3] == c[:3] and g[3] & _lib.FG_PLAN_CLUSTER and not g[3] & _lib.FG_PLAN_RUNS2
+        threads = g[1] * -(-key[2] // 4)
+        assert threads <= 1024 and bool(g[3] & _lib.FG_PLAN_LEAN) == (threads > 512)
+        assert batch_general_plan_for(key, channels=3) is None
+    assert batch_general_plan_for((2, 256, 256)) == (8, 16, 256, _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_LEAN)

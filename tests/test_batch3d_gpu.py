@@ -67,12 +67,18 @@ def test_batch_matches_single_calls_and_oracle(signed, use_graph):
 def test_batch_pins_plans_for_concurrency_and_releases_them():
     b = fg.GeodesicBatch3d([(1, 12, 256, 256), (1, 8, 48, 40)], iterations=1, use_graph=False, streams=2)
     try:
-        d = _lib.plan_describe(2, 256, 256)
-        assert d["lean"] & _lib.FG_PLAN_CLUSTER and d["lean"] & _lib.FG_PLAN_RUNS2
+        # l_grad = 0 and l_eucl = 0 passes: the cluster sweep kernel (two runs per thread)
+        for mode in (1, 2):
+            d = _lib.plan_describe(2, 256, 256, mode=mode)
+            assert d["lean"] & _lib.FG_PLAN_CLUSTER and d["lean"] & _lib.FG_PLAN_RUNS2
+        # general passes: the same strips, one run per thread
+        d = _lib.plan_describe(2, 256, 256, mode=0)
+        assert d["lean"] & _lib.FG_PLAN_CLUSTER and not d["lean"] & _lib.FG_PLAN_RUNS2 and d["tiles1"] == 16
         assert _lib.plan_describe(2, 48, 40)["tiles1"] * _lib.plan_describe(2, 48, 40)["tiles2"] == 1
     finally:
         b.release_plans()
-    assert not _lib.plan_describe(2, 256, 256)["lean"] & _lib.FG_PLAN_CLUSTER
+    for mode in (0, 1, 2):
+        assert not _lib.plan_describe(2, 256, 256, mode=mode)["lean"] & _lib.FG_PLAN_CLUSTER
 
 
 def test_functional_batch_api():
