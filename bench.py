@@ -984,7 +984,7 @@ def _max_over_ranks(x, dist, dev):
 
 
 def b256_record(args, dev, rank, world, dist, n=8, steps=5):
-    """Spec target 1 (>= 60% of the HBM roofline on 256^3): a batch of
+    """The batched-volume target (>= 60% of the HBM roofline on 256^3): a batch of
     8 volumes 256^3 (smoothed noise generated on the device, one 6^3 seed cube
     each, spacing 1, iterations 4, lamb cycling 0 / 0.5 / 1), one transform per
     volume, through GeodesicBatch3d (cluster plans pinned by the batch,
@@ -1090,7 +1090,7 @@ def b256_record(args, dev, rank, world, dist, n=8, steps=5):
 
 
 def c3_record(args, dev, rank, world, dist, steps=5):
-    """Spec target 2 (>= 5x the plain per-call drop-in on the uneven 2D
+    """The uneven-batch target (>= 5x the plain per-call drop-in on the uneven 2D
     batch): the 64-image batch, plain and signed of every image, through
     GeodesicBatch2d (one CUDA graph) against the same transforms called one
     by one through the drop-in API.  Images are split across ranks."""
@@ -1389,7 +1389,7 @@ def run_gpu_arm(args, w, rank, world):
         alone = {"lamb": w["lambs"][ka], "transforms": n_alone, "pass_ms": a_ms, "launches": a_launches, "vp": a_vp}
     extra = {}
     if w["name"] == "c2" and not args.no_extras:
-        # the benchmark spec's targets, measured in the same run (outside the timed steps)
+        # the batch targets, measured in the same run (outside the timed steps)
         extra["b256"] = b256_record(args, dev, rank, world, dist)
         extra["c3"] = c3_record(args, dev, rank, world, dist)
     clk = clocks.stop()
@@ -1471,7 +1471,7 @@ def run_gpu_arm(args, w, rank, world):
                 "path": f"public API with pinned host tensors, {n_calls} calls per step from {n_calls} host threads"},
         "clocks": clk,
         "gpu_launches": int((pass_launches + aux_launches + init_launches) / args.steps),
-        **({"north_star": extra} if extra else {}),
+        **({"batch_targets": extra} if extra else {}),
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -1536,7 +1536,7 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="run warm-up and timed GPU steps only (no end-to-end or CPU legs): for profiler captures")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the north-star records (batch of 256^3 volumes, uneven 2D batch) of the default run")
+                    help="skip the batch-target records (batch of 256^3 volumes, uneven 2D batch) of the default run")
     ap.add_argument("--no-signed-gsf", action="store_true",
                     help="reference arm: skip the signed / GSF timings of the reference's CPU path")
     ap.add_argument("--dry-run", action="store_true",

@@ -4,7 +4,7 @@
 //   D[t][x] = min(D[t][x], min_n D[t-1][x+n] + l_eucl*ld[n] + l_grad*L1(I[t][x], I[t-1][x+n]))
 //   (reference: FastGeodis/fastgeodis_cpu.cpp:203-340)
 //
-// Design (this build's own):
+// Design:
 //   * One thread-block cluster of G <= 16 CTAs owns the whole cross-section;
 //     CTA `rank` owns the strip of T1 whole rows starting at rank * T1 (T1 a
 //     multiple of RPT).  No halo, no hand-off through global memory.

@@ -655,7 +655,7 @@ struct Axis {
   long long s_str, st1;  // read strides (cross 2 has stride 1)
   int N1, N2;
   bool transposed;       // reads the [W]-major layout
-  float ld[9];           // step lengths in this build's neighbour numbering
+  float ld[9];           // step lengths in the engine's neighbour numbering (n = 3*(d1+1) + (d2+1))
 };
 
 void axes_for(const Geometry &g, Axis *ax, int *nax) {
@@ -675,7 +675,7 @@ void axes_for(const Geometry &g, Axis *ax, int *nax) {
   ax[1] = Axis{g.H, g.W, HW, g.D, g.W, false, {}};
   table3(s[1], s[0], s[2], ax[1].ld);
   // along W over [W][D][H]: cross (d, h); the reference transposes to [W, H, D],
-  // whose i runs over h (this build's cross 2) and j over d (cross 1)
+  // whose i runs over h (the engine's cross 2) and j over d (cross 1)
   ax[2] = Axis{g.W, DH, g.H, g.D, g.H, true, {}};
   float t[9];
   table3(s[2], s[1], s[0], t);

@@ -4,7 +4,7 @@
 //   D[t][x] = min(D[t][x], min_n D[t-1][x+n] + l_eucl*ld[n] + l_grad*L1(I[t][x], I[t-1][x+n]))
 //   (reference: FastGeodis/fastgeodis_cpu.cpp:53-162 and :203-340)
 //
-// Design (this build's own):
+// Design:
 //   * A CTA owns a tile of the cross-section plus a halo of K cells per side
 //     and walks every step of the pass.  Each thread owns a run of 4
 //     consecutive cells along the innermost cross dimension.

@@ -45,7 +45,7 @@ extern "C" {
 #define FG_ERR_CUDA 2             /* a CUDA runtime call failed */
 #define FG_ERR_WORKSPACE 3        /* workspace missing or too small */
 #define FG_ERR_TIMEOUT 4          /* a bounded inter-CTA wait expired (recorded on the device) */
-#define FG_ERR_UNSUPPORTED 5      /* size beyond what this build plans for */
+#define FG_ERR_UNSUPPORTED 5      /* a size or form the engine does not handle */
 
 /* Operation codes for fg_workspace_bytes. */
 #define FG_OP_PLAIN 0
