@@ -4,8 +4,8 @@ Three artefacts are produced here; none is part of the shipped product:
 
 * ``oracle/_build/libfg_oracle.so`` -- the plain-C restatement of FastGeodis'
   raster scan (``oracle/fg_oracle.c``), compiled with ``gcc`` and OpenMP.  It
-  runs on any host (x86 container or the Arm GPU host) and is the parity
-  checker and the timed CPU baseline.
+  runs on any host (x86 or Arm) and is the oracle of the parity tests and
+  the timed CPU baseline.
 * ``oracle/_ref/libfg_fastmarch.so`` -- the fast-marching accuracy harness
   (``oracle/fg_fastmarch.cpp``) over the reference's vendored solver header
   (``dependency/fmm``), compiled where that header is available.
