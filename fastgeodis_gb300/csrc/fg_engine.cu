@@ -414,11 +414,12 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     const bool chunked = (ovLean & FG_PLAN_CHUNKED) != 0;
     if (chunked || (long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, (ovLean & FG_PLAN_LEAN) != 0, chunked);
   }
-  // Rows (2D passes) of 1024 cells or more: tiles of 128 cells, S = 8.  The
-  // cost model prefers one-warp tiles there, but measured on GB300 (images of
-  // 1024^2 to 4096^2, lamb 0.5, widths 64 to 2048 and S = 4 or 8) 128-cell
-  // tiles were the fastest for every size, 6-16% ahead of the model's pick.
-  if (!found && cross == 1 && N2 >= 1024 && (N2 + 127) / 128 <= max_tiles)
+  // Rows (2D passes) of more than 512 cells: tiles of 128 cells, S = 8.  The
+  // cost model prefers one tile, or one-warp tiles, there; measured on GB300
+  // (images of 640^2 to 4096^2, lamb 0.5, widths 64 to 2048 and S = 4 or 8)
+  // 128-cell tiles were the fastest for every size: 1.5-5% ahead of one tile
+  // below 1024 cells, 6-16% ahead of the model's pick from 1024 on.
+  if (!found && cross == 1 && N2 > 512 && (N2 + 127) / 128 <= max_tiles)
     consider(8, 1, 128, 1, (N2 + 127) / 128, false);
   for (int S : {8, 4, 2, 1}) {
     if (found) break;  // an override that fits wins
