@@ -118,7 +118,7 @@ __device__ void run_pass(const Batch3dJob &jb, float *sm, unsigned rank) {
     cl_sync();
     return;
   }
-  cluster_body<1, M, MODE, 0, 2>(a, sm);
+  cluster_body<1, M, MODE, 2>(a, sm);
 }
 
 template <int M, int MODE>

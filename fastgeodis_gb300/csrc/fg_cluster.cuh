@@ -23,38 +23,33 @@
 //     receiver's reads (it needs the receiver's rows of the step before), so
 //     rings of two steps suffice.
 //   * Own inputs (old distances, image values) are staged P steps ahead with
-//     per-thread cp.async; the transposed write (the pass that changes
-//     layout) goes through S ring rows flushed as S-element segments; the
-//     arithmetic is the pass kernel's, operation by operation.
+//     per-thread cp.async; results are written in place (a pass that changes
+//     layout is followed by a transpose of the map); the arithmetic is the
+//     pass kernel's, operation by operation.
 #pragma once
 
 #include "fg_pass.cuh"
 
 namespace fgi {
 
-// WTT: 0 / 1 the transposed write off / on at compile time, 2 read from a.wt
-// (the batched volume kernel, whose jobs mix both).
-template <int CT, int M, int MODE, int WTT, int RPT>
+template <int CT, int M, int MODE, int RPT>
 __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
-  const bool WT = WTT == 2 ? a.wt != 0 : WTT == 1;
   constexpr bool USE_IMG = MODE != MODE_EUCLID;
   constexpr int NCH = pass_nch(CT, MODE);
   constexpr int NCHR = NCH > 0 ? NCH : 1;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int NT = blockDim.x, nwarps = NT >> 5;
+  const int tid = threadIdx.x, NT = blockDim.x;
   const int C = USE_IMG ? (CT == 0 ? a.C : CT) : 0;
-  const int P = a.P, L = a.L, S = a.S, lgS = __ffs(S) - 1;  // P, S: powers of two
-  const int SR = WT ? S : 2;                                // distance rows kept per map
+  const int P = a.P, L = a.L;  // P: a power of two
+  constexpr int SR = 2;        // distance rows kept per map
   const int rank = (int)cl_rank(), G = a.tiles1;
   const int T1 = a.T1, N2 = a.N2;
-  const ClusterLayout ly = cluster_layout(C, M, SR, T1, N2, NT, RPT, P, WT);
+  const ClusterLayout ly = cluster_layout(C, M, T1, N2, NT, RPT, P);
   const int rpr = ly.rpr, B2 = ly.B2, rowf = ly.rowf, edgef = ly.edgef, EP2 = (rpr + 2) * 2;
   float *const dring = sm + ly.dring;
   float *const iring = sm + ly.iring;
   float *const dedge = sm + ly.dedge;
   float *const iedge = sm + ly.iedge;
   float4 *const oring = reinterpret_cast<float4 *>(sm + ly.oring);  // [P][M + C][RPT][NT]
-  int2 *const otab = reinterpret_cast<int2 *>(sm + ly.otab);
   const unsigned lsm = smem_u32(sm), cbar = lsm + ly.bar;
   const int row0 = rank * T1, nrows = max(0, min(T1, a.N1 - row0));
   const int AR = M + C, NTR = NT * RPT;
@@ -71,17 +66,8 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
   const bool active = vmask != 0;
   const bool vec = a.vec != 0;
 
-  // --- set-up: rings NaN (cells outside the image never win a min), own-cell table ---
-  for (int i = tid; i < ly.otab; i += NT) sm[i] = qnan;
-  int nown = 0;
-  if (WT) {
-    nown = nrows * N2;
-    for (int i = tid; i < nown; i += NT) {
-      const int o1 = i / N2, o2 = i - o1 * N2;
-      const long long g = (long long)(row0 + o1) * a.wst1 + (long long)o2 * a.wst2;
-      otab[i] = make_int2((o1 + 1) * B2 + 4 + o2, (int)g);
-    }
-  }
+  // --- set-up: rings NaN (cells outside the image never win a min) ---
+  for (int i = tid; i < ly.bar / 4; i += NT) sm[i] = qnan;
   // neighbour strips: bytes this CTA receives per step, and where this thread sends
   const unsigned cl_bytes = (unsigned)(((rank > 0 ? 1 : 0) + (rank < G - 1 ? 1 : 0)) * rpr * 24 * AR);
   const int k_dn = T1 - 1 - rf;  // the run of this thread on the strip's last row, if any
@@ -306,7 +292,7 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
           if (k == 0 && push_up) push(rsm_up, T1 + 1, t, out, ic);  // the upper strip's lower apron
           if (k == k_dn && push_dn) push(rsm_dn, 0, t, out, ic);     // the lower strip's upper apron
         }
-        if (!WT && t > 0) {
+        if (t > 0) {
           const int w = wcur + k * kwst;
 #pragma unroll
           for (int m = 0; m < M; m++) {
@@ -326,23 +312,6 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
     else cp_async_commit();
     wcur += wstep;
     __syncthreads();
-    if (WT && (((t + 1) & (S - 1)) == 0 || t == L - 1)) {
-      // transposed write-back of the chunk's own cells: S consecutive
-      // positions of one cell are contiguous in the write layout
-      const int t0 = t & ~(S - 1), Sn = t - t0 + 1;
-      const int cpw = 32 / S, j = lane & (S - 1);
-      if (j < Sn) {
-        const long long so = (a.dir > 0 ? (long long)(t0 + j) : (long long)(L - 1 - t0 - j)) * a.ws_str;
-        const float *src = dring + j * M * rowf;
-#pragma unroll
-        for (int m = 0; m < M; m++)
-          for (int i = warp * cpw + (lane >> lgS); i < nown; i += nwarps * cpw) {
-            const int2 e = otab[i];
-            a.ddst[m][so + e.y] = src[m * rowf + e.x];
-          }
-      }
-      __syncthreads();
-    }
   }
   cp_async_wait<0>();
   cl_sync();  // no CTA leaves while a neighbour may still address its shared memory
@@ -354,10 +323,10 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
   }
 }
 
-template <int CT, int M, int MODE, bool WT, int RPT>
+template <int CT, int M, int MODE, int RPT>
 __global__ void __launch_bounds__(512) fg_sweep_cluster_kernel(const PassArgs a) {
   extern __shared__ __align__(16) float sm[];
-  cluster_body<CT, M, MODE, WT ? 1 : 0, RPT>(a, sm);
+  cluster_body<CT, M, MODE, RPT>(a, sm);
 }
 
 }  // namespace fgi

@@ -117,25 +117,22 @@ __host__ __device__ constexpr int pass_edge_floats(int cross, int R1, int R2) {
 // and a 4-cell apron left and right, as in the pass kernel.
 struct ClusterLayout {
   int rpr, B2, rowf, edgef;               // runs per row, floats per ring row, ring and edge-array pitches
-  int dring, iring, dedge, iedge, oring;  // distances [SR][M], image [2][C], their edge arrays, staging [P][M+C][RPT][NT]
-  int otab;                               // own-cell table of the transposed write (int2 per cell)
+  int dring, iring, dedge, iedge, oring;  // distances [2][M], image [2][C], their edge arrays, staging [P][M+C][RPT][NT]
   int bar;                                // two mbarriers (bytes)
   int bytes;
 };
-__host__ __device__ inline ClusterLayout cluster_layout(int C, int M, int SR, int T1, int N2, int NT, int RPT, int P,
-                                                        bool wt) {
+__host__ __device__ inline ClusterLayout cluster_layout(int C, int M, int T1, int N2, int NT, int RPT, int P) {
   ClusterLayout l;
   l.rpr = (N2 + 3) / 4;
   l.B2 = 4 * l.rpr + 8;
   l.rowf = ring_pitch((T1 + 2) * l.B2);
   l.edgef = ring_pitch((T1 + 2) * (l.rpr + 2) * 2);
   l.dring = 0;
-  l.iring = SR * M * l.rowf;
+  l.iring = 2 * M * l.rowf;
   l.dedge = l.iring + 2 * C * l.rowf;
-  l.iedge = l.dedge + SR * M * l.edgef;
+  l.iedge = l.dedge + 2 * M * l.edgef;
   l.oring = l.iedge + 2 * C * l.edgef;  // every pitch is a multiple of 4 floats: 16-byte aligned
-  l.otab = l.oring + P * (M + C) * RPT * NT * 4;
-  l.bar = (l.otab + (wt ? 2 * T1 * N2 : 0)) * 4;
+  l.bar = (l.oring + P * (M + C) * RPT * NT * 4) * 4;
   l.bytes = l.bar + 16;
   return l;
 }

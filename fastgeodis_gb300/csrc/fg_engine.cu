@@ -277,13 +277,16 @@ bool has_override(int cross, int N1, int N2) {  // under g_override_mu
 }
 
 // A cluster plan for a volume pass: ceil(N1 / T1) strips of T1 whole rows,
-// one CTA each, 2 to 16 CTAs in one cluster.  S is the transposed write's
-// flush period (halved until the rings fit; at least 2, the apron rings'
-// depth); the staging depth is the largest that fits one CTA per SM.
-// rpt = 2: the cluster sweep kernel, 2 vertically adjacent runs per thread
-// (T1 rounded up to an even number, at most 512 threads, at most one image
-// channel read); rpt = 0: the pass kernel, one run per thread.
+// one CTA each, 2 to 16 CTAs in one cluster.  Its passes write in place (a
+// pass that changes layout is followed by a transpose: the pass generator
+// splits it), so `wt` and S play no part; the staging depth is the largest
+// that fits one CTA per SM.  rpt = 2: the cluster sweep kernel, 2 vertically
+// adjacent runs per thread (T1 rounded up to an even number, at most 512
+// threads, at most one image channel read); rpt = 0: the pass kernel, one
+// run per thread.
 bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1, int rpt, bool want_lean, Plan *out) {
+  (void)wt;
+  (void)S;
   const int cimg = mode == MODE_EUCLID ? 0 : C;
   if (rpt != 0 && (cimg > 1 || rpt != 2)) return false;
   if (cimg > kMaxChannels) return false;  // wide images run on tile plans
@@ -297,22 +300,20 @@ bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1
   if (nt > (rpt ? kThreads : pass_max_threads(2, cimg, M))) return false;
   const bool lean = rpt == 0 && (nt > kThreads || (want_lean && pass_lean(2, cimg, M)));
   const int nch = mode == MODE_EUCLID ? 0 : (C == 1 ? 1 : kMaxChannels);
-  for (int s2 = wt ? std::max(2, std::min(S, 8)) : 2; s2 >= 2; s2 /= 2) {
-    for (int depth = max_pass_depth(nch, M); depth >= 2; depth /= 2) {
-      int B2, rowf, nown;
-      size_t sm;
-      if (rpt) {
-        const ClusterLayout ly = cluster_layout(cimg, M, wt ? s2 : 2, T1, N2, nt, rpt, depth, wt);
-        sm = (size_t)ly.bytes;
-        B2 = ly.B2;
-        rowf = ly.rowf;
-      } else {
-        sm = pass_smem_bytes(2, C, M, mode, wt, s2, T1, N2, &B2, &rowf, &nown, depth);
-      }
-      if (sm <= kSmemBudget) {
-        *out = Plan{T1, N2, 0, 0, G, 1, wt ? s2 : 8, nt, B2, rowf, depth, sm, lean, true, rpt};
-        return true;
-      }
+  for (int depth = max_pass_depth(nch, M); depth >= 2; depth /= 2) {
+    int B2, rowf, nown;
+    size_t sm;
+    if (rpt) {
+      const ClusterLayout ly = cluster_layout(cimg, M, T1, N2, nt, rpt, depth);
+      sm = (size_t)ly.bytes;
+      B2 = ly.B2;
+      rowf = ly.rowf;
+    } else {
+      sm = pass_smem_bytes(2, C, M, mode, false, 2, T1, N2, &B2, &rowf, &nown, depth);
+    }
+    if (sm <= kSmemBudget) {
+      *out = Plan{T1, N2, 0, 0, G, 1, 8, nt, B2, rowf, depth, sm, lean, true, rpt};
+      return true;
     }
   }
   return false;
@@ -1356,7 +1357,7 @@ int fg_batch3d_plan(const fg_batch3d_item *items, int n, int iterations, int clu
     PassArgs &a = j.a;
     bool fit = false;
     for (int P = 8; P >= 2 && !fit; P /= 2) {
-      const ClusterLayout ly = cluster_layout(cimg, M, 2, a.T1, a.N2, threads, 2, P, false);
+      const ClusterLayout ly = cluster_layout(cimg, M, a.T1, a.N2, threads, 2, P);
       if ((size_t)ly.bytes <= kSmemBudget) {
         a.S = 8;
         a.P = P;

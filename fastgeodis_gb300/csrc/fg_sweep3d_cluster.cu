@@ -5,27 +5,27 @@
 namespace fgi {
 namespace {
 
-template <int CT, int M, int MODE, bool WT, int RPT>
+template <int CT, int M, int MODE, int RPT>
 int launch_sweep(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
   static unsigned long long configured = 0;  // bit per device (set under the engine's launch lock)
   if (c.threads > kThreads) return set_error(FG_ERR_UNSUPPORTED, "a cluster sweep CTA has at most 512 threads");
-  return launch_one_cluster((const void *)fg_sweep_cluster_kernel<CT, M, MODE, WT, RPT>, configured, a, c, s);
+  return launch_one_cluster((const void *)fg_sweep_cluster_kernel<CT, M, MODE, RPT>, configured, a, c, s);
 }
 
-template <int CT, int M, int MODE, bool WT>
+template <int CT, int M, int MODE>
 int launch_rpt(const PassArgs &a, const LaunchCfg &c, cudaStream_t s) {
-  if (c.rpt == 2) return launch_sweep<CT, M, MODE, WT, 2>(a, c, s);
+  if (c.rpt == 2) return launch_sweep<CT, M, MODE, 2>(a, c, s);
   return set_error(FG_ERR_UNSUPPORTED, "a cluster sweep thread owns 2 runs");
 }
 
 // one image channel (or none read): images with more channels take the pass
 // kernel's cluster path (their channel rows would not fit the registers)
-template <int M, bool WT>
+template <int M>
 int launch_sweep_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStream_t s) {
-  if (mode == MODE_EUCLID) return launch_rpt<1, M, MODE_EUCLID, WT>(a, c, s);
+  if (mode == MODE_EUCLID) return launch_rpt<1, M, MODE_EUCLID>(a, c, s);
   if (a.C != 1) return set_error(FG_ERR_UNSUPPORTED, "the cluster sweep kernel reads one image channel");
-  if (mode == MODE_GEO) return launch_rpt<1, M, MODE_GEO, WT>(a, c, s);
-  return launch_rpt<1, M, MODE_GENERAL, WT>(a, c, s);
+  if (mode == MODE_GEO) return launch_rpt<1, M, MODE_GEO>(a, c, s);
+  return launch_rpt<1, M, MODE_GENERAL>(a, c, s);
 }
 
 }  // namespace
@@ -33,7 +33,7 @@ int launch_sweep_mode(const PassArgs &a, const LaunchCfg &c, int mode, cudaStrea
 // How many clusters of `size` CTAs (threads, smem each) of the cluster sweep
 // kernel the current device co-schedules (cudaOccupancyMaxActiveClusters).
 int cluster_capacity(int size, int threads, size_t smem, int *out) {
-  const void *fn = (const void *)fg_sweep_cluster_kernel<1, 1, MODE_GENERAL, false, 2>;
+  const void *fn = (const void *)fg_sweep_cluster_kernel<1, 1, MODE_GENERAL, 2>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
@@ -62,8 +62,8 @@ int cluster_capacity(int size, int threads, size_t smem, int *out) {
 // (the engine's pass generator): no variant here writes transposed.
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
   if (wt) return set_error(FG_ERR_UNSUPPORTED, "cluster plans do not write transposed");
-  if (M == 1) return launch_sweep_mode<1, false>(a, c, mode, s);
-  if (M == 2) return launch_sweep_mode<2, false>(a, c, mode, s);
+  if (M == 1) return launch_sweep_mode<1>(a, c, mode, s);
+  if (M == 2) return launch_sweep_mode<2>(a, c, mode, s);
   return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
 }
 

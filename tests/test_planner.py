@@ -23,12 +23,13 @@ def ring_pitch(f):
     return f + (36 - f % 32) % 32
 
 
-def cluster_smem(C, M, SR, T1, N2, NT, rpt, depth, wt):
-    """Shared-memory bytes of a cluster sweep CTA (the layout of ClusterLayout)."""
+def cluster_smem(C, M, T1, N2, NT, rpt, depth):
+    """Shared-memory bytes of a cluster sweep CTA (the layout of ClusterLayout:
+    two rows of each ring; the passes write in place)."""
     rpr = -(-N2 // 4)
     rowf = ring_pitch((T1 + 2) * (4 * rpr + 8))
     edgef = ring_pitch((T1 + 2) * (rpr + 2) * 2)
-    floats = (SR * M + 2 * C) * (rowf + edgef) + depth * (M + C) * rpt * NT * 4 + (2 * T1 * N2 if wt else 0)
+    floats = (2 * M + 2 * C) * (rowf + edgef) + depth * (M + C) * rpt * NT * 4
     return floats * 4 + 16
 
 
@@ -187,8 +188,7 @@ def test_cluster_sweep_plans(N1, N2, C, maps, mode, wt, rpt, flag):
     g = -(-N1 // T1)
     threads = T1 // rpt * -(-N2 // 4)
     nt = -(-threads // 32) * 32
-    fits = any(cluster_smem(cimg, maps, s2 if wt else 2, T1, N2, nt, rpt, 2, wt) <= 227 * 1024 - 1024
-               for s2 in (8, 4, 2))
+    fits = cluster_smem(cimg, maps, T1, N2, nt, rpt, 2) <= 227 * 1024 - 1024
     if cimg > 1 or g < 2 or threads > 512 or not fits:
         assert not p["lean"] & _lib.FG_PLAN_RUNS2  # the planner's own plan
         return
@@ -196,8 +196,8 @@ def test_cluster_sweep_plans(N1, N2, C, maps, mode, wt, rpt, flag):
     assert (p["tiles1"], p["tiles2"], p["T1"], p["T2"], p["K1"], p["K2"]) == (g, 1, T1, N2, 0, 0)
     assert threads <= p["threads"] <= 512 and p["threads"] % 32 == 0
     assert p["smem"] <= SMEM_LIMIT and p["depth"] in (2, 4, 8)
-    S = p["S"] if wt else 2
-    assert p["smem"] == cluster_smem(cimg, maps, S, T1, N2, p["threads"], rpt, p["depth"], wt)
+    # the layout-changing passes of a cluster plan write in place (a transpose follows): no flush rings
+    assert p["smem"] == cluster_smem(cimg, maps, T1, N2, p["threads"], rpt, p["depth"])
 
 
 def test_runs_flags_validation():
