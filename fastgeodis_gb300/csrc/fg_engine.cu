@@ -238,7 +238,7 @@ constexpr size_t kSmemPerSm = 228 * 1024;
 // step j, the runs whose cone distance is <= j (run_cone_dist in the kernel).
 double cone_avg_runs(int cross, int R1, int R2, int K1, int K2, int S) {
   const int rpr = (R2 + 3) / 4, nruns = R1 * rpr;
-  int count[9] = {0};  // runs by cone distance 0 .. S (S <= 8)
+  int count[33] = {0};  // runs by cone distance 0 .. S (S <= 32)
   for (int q = 0; q < nruns; q++) {
     const int r1 = q / rpr, u = q % rpr;
     const int d1 = (cross == 2 && K1 > 0) ? std::min(r1, R1 - 1 - r1) : S;
@@ -415,13 +415,15 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     const bool chunked = (ovLean & FG_PLAN_CHUNKED) != 0;
     if (chunked || (long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, (ovLean & FG_PLAN_LEAN) != 0, chunked);
   }
-  // Rows (2D passes) of more than 512 cells: tiles of 128 cells, S = 8.  The
-  // cost model prefers one tile, or one-warp tiles, there; measured on GB300
-  // (images of 640^2 to 4096^2, lamb 0.5, widths 64 to 2048 and S = 4 or 8)
-  // 128-cell tiles were the fastest for every size: 1.5-5% ahead of one tile
-  // below 1024 cells, 6-16% ahead of the model's pick from 1024 on.
+  // Rows (2D passes) of more than 512 cells: tiles of 128 cells with a hand-off
+  // every 32 steps (halos of 32 cells: a row's halo is only its two ends).
+  // The cost model prefers one tile, or one-warp tiles with S = 8, there;
+  // measured on GB300 (images of 600^2 to 8192^2, lamb 0.5, widths 64 to
+  // 2048, S = 4 to 32), 128-cell tiles were the fastest width for every size
+  // and S = 32 the fastest period: 11-20% ahead of S = 8 on the same tiles,
+  // 25-35% ahead of the model's pick (4096^2: 18.3 -> 13.0 ms).
   if (!found && cross == 1 && N2 > 512 && (N2 + 127) / 128 <= max_tiles)
-    consider(8, 1, 128, 1, (N2 + 127) / 128, false);
+    consider(32, 1, 128, 1, (N2 + 127) / 128, false);
   for (int S : {8, 4, 2, 1}) {
     if (found) break;  // an override that fits wins
     if (cross == 1) {
@@ -1066,7 +1068,8 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
   if (S == 0) {
     g_overrides.erase(key);
   } else {
-    if (S != 1 && S != 2 && S != 4 && S != 8) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be 1, 2, 4 or 8");
+    if (S < 1 || S > 32 || (S & (S - 1)))
+      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be a power of two up to 32");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
     const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_CHUNKED;
     if (lean < 0 || (lean & ~all)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");

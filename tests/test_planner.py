@@ -35,7 +35,7 @@ def cluster_smem(C, M, T1, N2, NT, rpt, depth):
 
 def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
     S, T1, T2, K1, K2, t1, t2, nt, depth, smem, lean = (p[k] for k in _lib.PLAN_FIELDS)
-    assert S in (1, 2, 4, 8) and depth in (2, 4, 8)
+    assert S in (1, 2, 4, 8, 16, 32) and depth in (2, 4, 8)
     assert t1 == -(-N1 // T1) and t2 == -(-N2 // T2)
     assert t1 * t2 <= sms, "all tiles must be co-resident"
     if cross == 1:
@@ -253,3 +253,15 @@ def test_chunked_override():
     finally:
         _lib.check(L.fg_plan_override(2, 64, 64, 0, 0, 0, 0))
     assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
+
+
+@pytest.mark.parametrize("N2", [513, 600, 1024, 2048, 8192, 19456])
+def test_long_rows_take_128_cell_tiles_with_32_step_chunks(N2):
+    """2D rows of more than 512 cells (up to one tile per SM): tiles of 128
+    cells, a hand-off every 32 steps (the measured optimum)."""
+    p = _lib.plan_describe(1, 1, N2)
+    assert (p["S"], p["T1"], p["T2"], p["K2"]) == (32, 1, 128, 32)
+    assert p["tiles2"] == -(-N2 // 128) and p["threads"] == 64
+    assert not p["lean"] & _lib.FG_PLAN_CHUNKED
+    # rows up to 512 cells and images wider than 152 such tiles keep the cost model's plan
+    assert _lib.plan_describe(1, 1, 512)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
