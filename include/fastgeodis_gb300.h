@@ -80,7 +80,7 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 /* Plan override (no counterpart in the reference): for passes whose
  * cross-section is N1 x N2 (cross = 1 for 2D images, N1 = 1; cross = 2 for
  * volumes), use tiles of T1 x T2 cells with S steps per halo hand-off
- * (S in {1,2,4,8}, halo S).  Flag FG_PLAN_LEAN asks for the 64-register
+ * (S a power of two up to 32, halo S).  Flag FG_PLAN_LEAN asks for the 64-register
  * kernel where the variant has one (volumes, one image channel or none, one
  * map: two CTAs of up to 512 threads per SM); without it the planner decides
  * (the 128-register kernel up to 512 threads).  Flag FG_PLAN_CLUSTER (volumes
