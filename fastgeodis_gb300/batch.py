@@ -103,26 +103,32 @@ def plan_jobs(shapes: Sequence[Tuple[int, int, int]], signed: Sequence[bool], it
     return jobs
 
 
-# A tiled strip's hand-off of its edges through L2, once per 8 steps, and the
-# CTAs per tiled image tried: on the uneven 2D batch (GB300) 11 images at 3
-# CTAs took 19.5 ms, at 4 CTAs 16.8, at 6 16.6 (the untiled rest then sets
-# the time); 3 CTAs per image imply about 5 us per hand-off of an image's
-# two maps.
+# A tiled strip's hand-off of its edges through L2, once per HANDOFF_STEPS
+# steps (its halo: HANDOFF_STEPS cells at each end of the strip), and the
+# CTAs per tiled image tried.  On the uneven 2D batch (GB300): with a hand-off
+# every 8 steps, 11 images at 3 CTAs took 19.5 ms, at 4 CTAs 16.8, at 6 16.6
+# (about 5 us per hand-off of an image's two maps); with one every 32 steps
+# 11 images at 6 CTAs 16.5 ms, 16 at 4 16.5, 22-26 at 4 15.4-15.5, 28 at 4
+# 16.0, and 32 at 4 (128 CTAs) or 24 at 5 22-24 ms: the persistent launch
+# then lacks SMs for the rest (MAX_TILED_SM_SHARE).
 HANDOFF_US = 5.0
+HANDOFF_STEPS = 32
 TILE_COUNTS = (4, 6, 8)
 MAX_TILED = 32  # images per tiled launch (fg_batch_geodesic2d_tiled)
+MAX_TILED_SM_SHARE = 0.7  # tiled CTAs per SM at most
 
 
-def tiled_width(n2: int, k: int, s: int = 8) -> int:
+def tiled_width(n2: int, k: int, s: int = HANDOFF_STEPS) -> int:
     """Strip width of a row of n2 cells over k CTAs (fg_batch_tiled.cu)."""
     return max(((n2 + k - 1) // k + 3) & ~3, s)
 
 
 def tiled_cost(C: int, H: int, W: int, maps: int, iterations: int, k: int) -> float:
     """Estimated microseconds of an image whose rows are split over k CTAs."""
-    h = HANDOFF_US / 8.0
-    return 2.0 * max(iterations, 1) * (H * (step_us(C, maps, tiled_width(W, k) + 16) + h) +
-                                       W * (step_us(C, maps, tiled_width(H, k) + 16) + h))
+    h = HANDOFF_US / HANDOFF_STEPS
+    halo = 2 * HANDOFF_STEPS
+    return 2.0 * max(iterations, 1) * (H * (step_us(C, maps, tiled_width(W, k) + halo) + h) +
+                                       W * (step_us(C, maps, tiled_width(H, k) + halo) + h))
 
 
 def _rest_bound(shapes, signed, iterations, sms) -> float:
@@ -133,7 +139,7 @@ def _rest_bound(shapes, signed, iterations, sms) -> float:
 
 
 def plan_tiles(shapes: Sequence[Tuple[int, int, int]], signed: Sequence[bool], iterations: int, sms: int,
-               max_images: int = 12) -> dict:
+               max_images: int = MAX_TILED) -> dict:
     """Images to run tiled beside the batch, ``{image: CTAs}``: the largest
     images, as many and as finely split as lowers the estimated time of the
     whole (the tiled images' longest against the rest of the batch on the
@@ -146,7 +152,7 @@ def plan_tiles(shapes: Sequence[Tuple[int, int, int]], signed: Sequence[bool], i
         top = order[:count]
         rest = [i for i in range(n) if i not in set(top)]
         for k in TILE_COUNTS:
-            if count * k > sms // 2:
+            if count * k > int(MAX_TILED_SM_SHARE * sms):
                 break
             t_tiled = max(tiled_cost(*shapes[i], 2 if signed[i] else 1, iterations, k) for i in top)
             t_rest = _rest_bound([shapes[i] for i in rest], [signed[i] for i in rest], iterations, sms - count * k)

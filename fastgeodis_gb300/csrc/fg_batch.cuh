@@ -53,6 +53,23 @@ __host__ __device__ inline bool batch_job_fit(int C, int M, int ext, size_t smem
   return false;
 }
 
+// The same for a strip of a tiled image, whose S is also its hand-off period
+// (halos of S cells): the longest period first, S = 32 down to 8 at the
+// natural depth, then as batch_job_fit.  A row's halo is only its two ends, so
+// a longer period costs little redundant work and saves hand-offs.
+__host__ __device__ inline bool tiled_job_fit(int C, int M, int ext, size_t smem, int *S, int *depth) {
+  const int nat = batch_natural_depth(C, M);
+  const int Ss[3] = {32, 16, 8};
+  for (int i = 0; i < 3; i++) {
+    if (batch_job_smem(C, M, ext, Ss[i], nat) <= smem) {
+      *S = Ss[i];
+      *depth = nat;
+      return true;
+    }
+  }
+  return batch_job_fit(C, M, ext, smem, S, depth);
+}
+
 // Transposed image copy (unless `transpose` is false) and the initial
 // distances of the job's maps: v*M for map 0, v*(1-M) for map 1.  A CTA that
 // is part `part` of `parts` CTAs sharing one image does that share.

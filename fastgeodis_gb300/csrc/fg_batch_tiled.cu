@@ -93,10 +93,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool wt = kk & 1;
       if (L <= 1 && !wt) continue;
       const int N2 = kk >= 2 ? H : W;
-      // flush steps and staging depth within the launch's shared memory,
-      // fitted at the widest region (halo 8)
+      // hand-off period (= flush steps) and staging depth within the launch's
+      // shared memory, fitted at this pass's region with the longest halo
       int S = 8, depth = 2;
-      batch_job_fit(it.C, M, tiled_width(N2, k, 8) + 16, smem, &S, &depth);
+      tiled_job_fit(it.C, M, tiled_width(N2, k, 32) + 64, smem, &S, &depth);
       const int T2 = tiled_width(N2, k, S), tiles = (N2 + T2 - 1) / T2;
       if (threadIdx.x == 0) {
         batch_pass_args(it, M, 0, kk, S, depth, r2, status, &s_args);
@@ -162,12 +162,12 @@ extern "C" FG_API int fg_batch_geodesic2d_tiled(const fg_batch2d_item *items, co
     kmin = std::min(kmin, tiles[i]);
   }
   const int grid = tab.start[n];
-  // the widest region of any pass at halo 8, for both map counts
-  const int R2 = tiled_width(max_extent, kmin, 8) + 16;
+  // the widest region of any pass at the longest halo (32), for both map counts
+  const int R2 = tiled_width(max_extent, kmin, 32) + 64;
   size_t smem = kBatchTransposeSmem;
   for (int M = 1; M <= 2; M++) {
     int S = 0, depth = 0;
-    if (!batch_job_fit(C, M, R2, kBatchSmemLimit, &S, &depth))
+    if (!tiled_job_fit(C, M, R2, kBatchSmemLimit, &S, &depth))
       return set_error(FG_ERR_UNSUPPORTED, "tiled batch: shared memory plan too large");
     smem = std::max(smem, batch_job_smem(C, M, R2, S, depth));
   }

@@ -59,7 +59,8 @@ def test_tiled_width():
     from fastgeodis_gb300.batch import tiled_width
 
     assert tiled_width(1968, 3) == 656 and tiled_width(1968, 3) % 4 == 0
-    assert tiled_width(30, 8) == 8  # at least the halo
+    assert tiled_width(30, 8) == 32  # at least the halo (a hand-off every 32 steps)
+    assert tiled_width(30, 8, 8) == 8
     assert tiled_width(2048, 2) == 1024
 
 
