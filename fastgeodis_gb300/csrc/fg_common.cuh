@@ -151,6 +151,11 @@ int launch_pass_cross2(const PassArgs &a, const LaunchCfg &c, int M, int mode, b
 int launch_pass_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int launch_sweep_cluster(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
 int cluster_capacity(int size, int threads, size_t smem, int *out);
+// 2D passes on row tiles (fg_rowtile2d.cu): c.tiles CTAs of a cooperative
+// launch, one thread per cell of a tile of a.T2 cells and its halos of a.K2 =
+// a.S cells; row_tile_smem: its shared memory for `cimg` image channels read.
+int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
+size_t row_tile_smem(int cimg, int M, int R, int S, bool wt);
 
 // A whole 2D transform (plain, or signed) of one image with both sides up to
 // kOneLaunchSide by one CTA in one launch (fg_row2d.cu, one thread per cell

@@ -215,6 +215,7 @@ struct Plan {
   bool cluster;  // one thread-block cluster of tiles1 strips of whole rows (fg_pass3d_cluster.cu)
   int rpt;       // cluster plans: runs per thread of the cluster sweep kernel (0: the pass kernel)
   bool chunked = false;  // one ordinary launch per chunk of S steps, any number of tiles
+  bool rowtile = false;  // 2D: the row-tile kernel (fg_rowtile2d.cu), one thread per cell of a tile and its halos
 };
 
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
@@ -402,6 +403,18 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (it == g_overrides.end()) it = g_overrides.find(std::make_tuple(cross, N1, N2, 0));
     if (it != g_overrides.end()) std::tie(ovS, ovT1, ovT2, ovLean) = it->second;
   }
+  // a 2D tile plan on the row-tile kernel: one thread per cell of the tile and
+  // its halos (at most 512), images of 1 to 4 channels read
+  auto to_row_tiles = [&](Plan &p) {
+    const int R = p.T2 + 2 * p.K2;
+    if (cross != 1 || p.tiles2 < 2 || p.chunked || C > kMaxChannels || R > 512) return false;
+    p.rowtile = true;
+    p.NT = (R + 31) / 32 * 32;
+    p.rowf = ring_pitch(R + 2);
+    p.smem = row_tile_smem(C, M, R, p.S, wt);
+    p.lean = false;
+    return true;
+  };
   if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
     Plan cp;
     const int rpt = (ovLean & FG_PLAN_RUNS2) ? 2 : 0;
@@ -414,16 +427,24 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     const int t1 = (N1 + T1 - 1) / T1, t2 = (N2 + T2 - 1) / T2;
     const bool chunked = (ovLean & FG_PLAN_CHUNKED) != 0;
     if (chunked || (long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, (ovLean & FG_PLAN_LEAN) != 0, chunked);
+    if (found && (ovLean & FG_PLAN_ROWS)) to_row_tiles(best);
   }
-  // Rows (2D passes) of more than 512 cells: tiles of 128 cells with a hand-off
-  // every 32 steps (halos of 32 cells: a row's halo is only its two ends).
-  // The cost model prefers one tile, or one-warp tiles with S = 8, there;
-  // measured on GB300 (images of 600^2 to 8192^2, lamb 0.5, widths 64 to
-  // 2048, S = 4 to 32), 128-cell tiles were the fastest width for every size
-  // and S = 32 the fastest period: 11-20% ahead of S = 8 on the same tiles,
-  // 25-35% ahead of the model's pick (4096^2: 18.3 -> 13.0 ms).
-  if (!found && cross == 1 && N2 > 512 && (N2 + 127) / 128 <= max_tiles)
-    consider(32, 1, 128, 1, (N2 + 127) / 128, false);
+  // Rows (2D passes) of more than 512 cells: row tiles (one thread per cell)
+  // with a hand-off every 32 steps (halos of 32 cells: a row's halo is only
+  // its two ends), the narrowest of 32, 64 or 128 cells that the SMs hold.
+  // Measured on GB300 (images of 600^2 to 8192^2, lamb 0.5): S = 32 was the
+  // fastest period (11-20% ahead of S = 8 on the pass kernel's tiles) and the
+  // row-tile kernel with narrow tiles the fastest form (4096^2: 18.3 ms on
+  // the cost model's plan, 13.0 on the pass kernel's 128-cell tiles, 7.85 on
+  // 32-cell row tiles).  Images of 1 to 4 channels; more take the pass kernel.
+  if (!found && cross == 1 && N2 > 512) {
+    for (int T2 : {32, 64, 128}) {
+      if ((N2 + T2 - 1) / T2 > max_tiles) continue;
+      consider(32, 1, T2, 1, (N2 + T2 - 1) / T2, false);
+      if (found && !to_row_tiles(best) && T2 < 128) found = false;  // narrow tiles only as row tiles
+      if (found) break;
+    }
+  }
   for (int S : {8, 4, 2, 1}) {
     if (found) break;  // an override that fits wins
     if (cross == 1) {
@@ -623,6 +644,7 @@ int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bo
   LaunchCfg c{p.tiles1 * p.tiles2, p.NT, p.smem, p.lean, p.rpt, p.chunked};
   return profiled_launch(s, (long long)a.L * a.N1 * a.N2 * M, a.L, [&] {
     if (p.cluster) return launch_pass_cluster(a, c, M, mode, wt, s);
+    if (p.rowtile) return launch_row_tiles(a, c, M, mode, wt, s);
     if (!p.chunked)
       return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
     // one ordinary launch per chunk of S steps, in stream order
@@ -1071,10 +1093,12 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
     if (S < 1 || S > 32 || (S & (S - 1)))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be a power of two up to 32");
     if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_CHUNKED;
+    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_CHUNKED | FG_PLAN_ROWS;
     if (lean < 0 || (lean & ~all)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
     if ((lean & FG_PLAN_CHUNKED) && (lean & FG_PLAN_CLUSTER))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: a chunked plan is a tile plan");
+    if ((lean & FG_PLAN_ROWS) && (cross != 1 || (lean & (FG_PLAN_CLUSTER | FG_PLAN_CHUNKED))))
+      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: row tiles are 2D tile plans");
     if ((lean & FG_PLAN_RUNS2) && !(lean & FG_PLAN_CLUSTER))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: runs per thread apply to cluster plans");
     if ((lean & FG_PLAN_CLUSTER) && (cross != 2 || S < 2))
@@ -1096,7 +1120,8 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
     return fail(FG_ERR_UNSUPPORTED, "no tiling for this cross-section");
   const int v[11] = {p.S,  p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem,
                      (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0) |
-                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0) | (p.chunked ? FG_PLAN_CHUNKED : 0)};
+                         (p.rpt == 2 ? FG_PLAN_RUNS2 : 0) | (p.chunked ? FG_PLAN_CHUNKED : 0) |
+                         (p.rowtile ? FG_PLAN_ROWS : 0)};
   for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }

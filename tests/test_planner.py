@@ -46,6 +46,11 @@ def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
     assert T1 >= K1 and T2 >= K2, "a halo reaches only the adjacent tiles"
     R1 = T1 + 2 * K1 if cross == 2 else 1
     R2 = T2 + 2 * K2
+    if lean == _lib.FG_PLAN_ROWS:
+        # row tiles: 2D, one thread per cell of a tile and its halos, at most 512
+        assert cross == 1 and t2 > 1 and C <= 4 and R2 <= nt <= 512 and nt % 32 == 0
+        assert smem <= SMEM_LIMIT
+        return
     runs = R1 * (-(-R2 // 4))
     mt = max_threads(cross, C, maps, mode)
     assert R1 * R2 <= 4 * mt and runs <= nt <= mt and nt % 32 == 0
@@ -255,13 +260,34 @@ def test_chunked_override():
     assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
 
 
-@pytest.mark.parametrize("N2", [513, 600, 1024, 2048, 8192, 19456])
-def test_long_rows_take_128_cell_tiles_with_32_step_chunks(N2):
-    """2D rows of more than 512 cells (up to one tile per SM): tiles of 128
-    cells, a hand-off every 32 steps (the measured optimum)."""
+@pytest.mark.parametrize("N2,T2", [(513, 32), (600, 32), (1024, 32), (4864, 32), (4865, 64), (8192, 64),
+                                   (9729, 128), (19456, 128)])
+def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
+    """2D rows of more than 512 cells: row tiles (one thread per cell of a
+    tile and its halos), the narrowest of 32, 64, 128 cells that fits the
+    SMs, a hand-off every 32 steps (the measured optimum)."""
     p = _lib.plan_describe(1, 1, N2)
-    assert (p["S"], p["T1"], p["T2"], p["K2"]) == (32, 1, 128, 32)
-    assert p["tiles2"] == -(-N2 // 128) and p["threads"] == 64
-    assert not p["lean"] & _lib.FG_PLAN_CHUNKED
+    assert (p["S"], p["T1"], p["T2"], p["K2"]) == (32, 1, T2, 32)
+    assert p["tiles2"] == -(-N2 // T2) <= 152 and p["threads"] == T2 + 64
+    assert p["lean"] == _lib.FG_PLAN_ROWS
+    # more than 4 channels take the pass kernel on 128-cell tiles
+    q = _lib.plan_describe(1, 1, N2, C=6)
+    assert not q["lean"] & _lib.FG_PLAN_ROWS and q["T2"] in (128, T2) or q["S"] <= 8
     # rows up to 512 cells and images wider than 152 such tiles keep the cost model's plan
     assert _lib.plan_describe(1, 1, 512)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
+
+
+def test_row_tile_override_validation():
+    L = _lib.load()
+    ROWS = _lib.FG_PLAN_ROWS
+    assert L.fg_plan_override(2, 64, 64, 8, 8, 8, ROWS) == _lib.FG_ERR_INVALID_ARGUMENT  # 2D only
+    assert L.fg_plan_override(1, 1, 300, 8, 1, 64, ROWS | _lib.FG_PLAN_CHUNKED) == _lib.FG_ERR_INVALID_ARGUMENT
+    try:
+        _lib.check(L.fg_plan_override(1, 1, 300, 8, 1, 64, ROWS))
+        p = _lib.plan_describe(1, 1, 300)
+        assert p["lean"] == ROWS and (p["S"], p["T2"], p["tiles2"], p["threads"]) == (8, 64, 5, 96)
+        # a region beyond 512 cells stays on the pass kernel
+        _lib.check(L.fg_plan_override(1, 1, 300, 8, 1, 496, ROWS))
+        assert not _lib.plan_describe(1, 1, 300)["lean"] & ROWS
+    finally:
+        _lib.check(L.fg_plan_override(1, 1, 300, 0, 0, 0, 0))

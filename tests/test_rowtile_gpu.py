@@ -1,0 +1,85 @@
+"""Row tiles: 2D passes whose rows are split into tiles of T2 cells, one CTA
+per tile and one thread per cell of the tile and its halos of S cells, with
+a hand-off of the halos through exchange words every S steps
+(fastgeodis_gb300/csrc/fg_rowtile2d.cu).  The planner takes them for rows of
+more than 512 cells; here they are also forced with fg_plan_override
+(FG_PLAN_ROWS) onto small images, through every variant (1 to 4 channels,
+one or two maps, the three arithmetic modes, both layouts, S from 1 to 32).
+The bar is the oracle's bits."""
+import numpy as np
+import pytest
+import torch
+
+import fastgeodis_gb300 as fg
+from fastgeodis_gb300 import _lib, tune
+from golden_cases import bits_equal
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+ROWS = _lib.FG_PLAN_ROWS
+
+
+def _case(shape, C, seed, soft=False):
+    rng = np.random.default_rng(seed)
+    img = (rng.random((C,) + tuple(shape)) * 80).astype(np.float32)
+    m = rng.random((1,) + tuple(shape)).astype(np.float32) if soft else np.ones((1,) + tuple(shape), np.float32)
+    for _ in range(3):
+        m[(0,) + tuple(int(rng.integers(0, n)) for n in shape)] = 0
+    return img, m
+
+
+def _pin(shape, S, T2):
+    tune.pin({k: (S, 1, T2, ROWS) for k in tune.pass_keys(shape)})
+    for k in tune.pass_keys(shape):
+        p = _lib.plan_describe(*k)
+        assert p["lean"] & ROWS and p["S"] == S and p["tiles2"] > 1, (k, p)
+
+
+@pytest.mark.parametrize("op,C,lamb,S,T2", [
+    ("plain", 1, 0.6, 8, 32),
+    ("plain", 1, 0.0, 4, 20),    # l_grad == 0: no image term
+    ("plain", 1, 1.0, 32, 64),   # l_eucl == 0, l_grad == 1
+    ("plain", 3, 0.5, 16, 48),
+    ("plain", 4, 0.3, 2, 12),
+    ("plain", 2, 0.8, 1, 8),     # a hand-off every step
+    ("signed", 1, 0.5, 32, 40),
+    ("signed", 3, 1.0, 8, 44),
+    ("gsf", 1, 0.7, 16, 36),
+])
+def test_forced_row_tiles(op, C, lamb, S, T2):
+    shape = (97, 211)  # the passes along H have rows of 211 cells, those along W rows of 97
+    img, m = _case(shape, C, 11 + C + S, soft=op == "gsf")
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    try:
+        _pin(shape, S, T2)
+        if op == "plain":
+            got = fg.generalised_geodesic2d(ti, tm, 1e10, lamb, 2)
+            want = oracle.geodesic2d(img, m, 1e10, lamb, 2)
+        elif op == "signed":
+            got = fg.signed_generalised_geodesic2d(ti, tm, 1e10, lamb, 2)
+            want = oracle.signed2d(img, m, 1e10, lamb, 2)
+        else:
+            got = fg.GSF2d(ti, tm, 0.4, 1e10, lamb, 1)
+            want = oracle.gsf2d(img, m, 0.4, 1e10, lamb, 1)
+        got = got[0].cpu().numpy()
+        assert bits_equal(got, want), float(np.nanmax(np.abs(got - want)))
+        fg.check_status()
+    finally:
+        tune.clear(shape)
+
+
+@pytest.mark.parametrize("shape,C", [((1500, 1300), 1), ((700, 2100), 3), ((3000, 600), 1)])
+def test_planner_row_tiles(shape, C):
+    """The planner's own plan for rows of more than 512 cells: 128-cell row
+    tiles with a hand-off every 32 steps."""
+    for k in tune.pass_keys(shape):
+        p = _lib.plan_describe(*k, C=C)
+        assert bool(p["lean"] & ROWS) == (k[2] > 512), (k, p)
+    img, m = _case(shape, C, 5 + C)
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    got = fg.generalised_geodesic2d(ti, tm, 1e10, 0.5, 2)[0].cpu().numpy()
+    assert bits_equal(got, oracle.geodesic2d(img, m, 1e10, 0.5, 2))
+    got = fg.signed_generalised_geodesic2d(ti, tm, 1e10, 1.0, 1)[0].cpu().numpy()
+    assert bits_equal(got, oracle.signed2d(img, m, 1e10, 1.0, 1))
+    fg.check_status()
