@@ -909,28 +909,48 @@ def run_reference_arm(args, w, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def _one_launch_side():
+def _one_launch(w):
+    """Whether the workload's transforms each run in one launch (a 2D image
+    the per-call path hands to the one-CTA kernel)."""
     from fastgeodis_gb300 import _lib
 
-    return _lib.FG_ONE_LAUNCH_SIDE
+    return w["dims"] == 2 and _lib.runs_in_one_launch(w["image"].shape[2:])
 
 
 def sweep_kernel_name(w, tuned):
     """The kernel of the workload's sweep passes: the pinned plans' kind."""
     if w.get("method") == "toivanen":
         return "fg_toivanen_kernel"
-    if w["dims"] == 2 and max(w["image"].shape[2:]) <= _one_launch_side():
+    if _one_launch(w):
         return "fg_row2d_kernel"
-    from fastgeodis_gb300 import _lib
+    from fastgeodis_gb300 import _lib, tune
 
+    plans = (tuned or {}).get("plans", {})
+    sms = torch_sms()
+    flags = []
+    for key in tune.pass_keys(w["image"].shape[2:]):
+        v = plans.get(",".join(map(str, key)))
+        # a pinned plan's flags, else the planner's plan for the pass
+        flags.append(int(v[3]) if v and int(v[0]) > 0 else
+                     _lib.plan_describe(*key, C=int(w["image"].shape[1]), sms=sms)["lean"])
+    flags += [int(v[3]) for k, v in plans.items() if k.count(",") == 3 and int(v[0]) > 0]  # per-mode plans
     names = []
-    for v in (tuned or {}).get("plans", {}).values() or [[0, 0, 0, 0]]:
-        f = int(v[3]) if int(v[0]) > 0 else 0
+    for f in flags:
         name = ("fg_sweep_cluster_kernel" if f & _lib.FG_PLAN_RUNS2 else
-                "fg_pass_cluster_kernel" if f & _lib.FG_PLAN_CLUSTER else "fg_pass_kernel")
+                "fg_pass_cluster_kernel" if f & _lib.FG_PLAN_CLUSTER else
+                "fg_row_tile_kernel" if f & _lib.FG_PLAN_ROWS else "fg_pass_kernel")
         if name not in names:
             names.append(name)
-    return " + ".join(names)  # the sweep kernels of the pinned plans (the passes of one transform)
+    return " + ".join(names)  # the sweep kernels of the transform's passes
+
+
+def torch_sms():
+    """SMs of the current device (152 without one: the planner's default)."""
+    import torch
+
+    if not torch.cuda.is_available():
+        return 152
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
 
 
 def metric_name(w):
@@ -1201,7 +1221,7 @@ def run_gpu_arm(args, w, rank, world):
         tuned = {"plans": {",".join(map(str, k)): [int(x) for x in v[:4]] for k, v in res.items()},
                  "note": f"loaded from {os.path.basename(args.plans)} (--plans)"}
     elif (args.tune and w.get("method") != "toivanen"
-          and not (w["dims"] == 2 and max(w["image"].shape[2:]) <= _lib.FG_ONE_LAUNCH_SIDE)):
+          and not _one_launch(w)):
         # untimed: plans of the step's transforms run together (small images
         # run in one launch and have no pass plans to tune)
         from fastgeodis_gb300 import tune
@@ -1369,7 +1389,7 @@ def run_gpu_arm(args, w, rank, world):
     # roofline below divides by the kernel's own duration (in the step above
     # three transforms share the SMs)
     alone = None
-    if w.get("method") != "toivanen" and not (w["dims"] == 2 and max(w["image"].shape[2:]) <= _one_launch_side()):
+    if w.get("method") != "toivanen" and not _one_launch(w):
         ka = len(w["lambs"]) // 2
         im_a, mk_a = d_in[ka]
         n_alone = max(3, min(args.steps, 10))

@@ -146,7 +146,16 @@ def profile_launch_times():
     return [(float(ms[i]), int(st[i])) for i in range(n.value)]
 
 
-FG_ONE_LAUNCH_SIDE = 512  # plain / signed 2D transforms of images up to this side run in one launch
+FG_ONE_LAUNCH_SIDE = 512  # the one-launch 2D kernel's largest side
+FG_ROW_TILE_MIN_ROW = 128  # 2D rows of at least this many cells run on row tiles
+
+
+def runs_in_one_launch(shape) -> bool:
+    """Whether the per-call path runs a plain or signed 2D transform of an
+    image of this (H, W) in one launch (no pinned plans or planner limits):
+    sides up to FG_ONE_LAUNCH_SIDE, one shorter than FG_ROW_TILE_MIN_ROW."""
+    H, W = (int(x) for x in shape)
+    return max(H, W) <= FG_ONE_LAUNCH_SIDE and min(H, W) < FG_ROW_TILE_MIN_ROW
 FG_PLAN_LEAN = 1      # plan flag: the 64-register kernel
 FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-section
 FG_PLAN_RUNS2 = 4     # plan flag: cluster sweep kernel, 2 runs of 4 cells per thread

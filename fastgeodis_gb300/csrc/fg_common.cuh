@@ -162,7 +162,10 @@ size_t row_tile_smem(int cimg, int M, int R, int S, bool wt);
 // of a row): initial distances, the image transpose, every pass and the
 // signed difference.
 int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, int *status, cudaStream_t s);
-constexpr int kOneLaunchSide = FG_ONE_LAUNCH_SIDE;  // images up to this side (measured faster than per-pass launches)
+constexpr int kOneLaunchSide = FG_ONE_LAUNCH_SIDE;  // the one-CTA kernel's largest side
+// 2D rows of at least this many cells are planned on row tiles; the per-call
+// path keeps the one-CTA launch for images with a side shorter than this
+constexpr int kRowTileMinRow = FG_ROW_TILE_MIN_ROW;
 
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
 // in place; spacing_sq = nullptr for images.  bar: 4 counters (16 bytes) of

@@ -321,8 +321,15 @@ bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1
 }
 std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older cache entries are stale
 
+// Measured on GB300 (square images, iterations 2, through the public call):
+// one CTA in one launch 0.28 / 0.55 / 0.87 / 1.23 ms at 128 / 256 / 384 / 512
+// per side, per-pass launches on 32-cell row tiles 0.27 / 0.47 / 0.68 / 0.88.
+// Images with a side shorter than kRowTileMinRow keep the one launch: their
+// passes along that side would not run on row tiles.
 bool one_launch_image(int H, int W) {
-  if (std::max(H, W) > kOneLaunchSide || g_tune_region.load() < kMaxRegion || g_tune_tiles.load() > 0) return false;
+  if (std::max(H, W) > kOneLaunchSide || std::min(H, W) >= kRowTileMinRow || g_tune_region.load() < kMaxRegion ||
+      g_tune_tiles.load() > 0)
+    return false;
   std::lock_guard<std::mutex> g(g_override_mu);
   return !has_override(1, 1, W) && !has_override(1, 1, H);
 }
@@ -429,15 +436,16 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (chunked || (long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, (ovLean & FG_PLAN_LEAN) != 0, chunked);
     if (found && (ovLean & FG_PLAN_ROWS)) to_row_tiles(best);
   }
-  // Rows (2D passes) of more than 512 cells: row tiles (one thread per cell)
-  // with a hand-off every 32 steps (halos of 32 cells: a row's halo is only
-  // its two ends), the narrowest of 32, 64 or 128 cells that the SMs hold.
-  // Measured on GB300 (images of 600^2 to 8192^2, lamb 0.5): S = 32 was the
-  // fastest period (11-20% ahead of S = 8 on the pass kernel's tiles) and the
-  // row-tile kernel with narrow tiles the fastest form (4096^2: 18.3 ms on
-  // the cost model's plan, 13.0 on the pass kernel's 128-cell tiles, 7.85 on
-  // 32-cell row tiles).  Images of 1 to 4 channels; more take the pass kernel.
-  if (!found && cross == 1 && N2 > 512) {
+  // Rows (2D passes) of kRowTileMinRow cells and more: row tiles (one thread
+  // per cell) with a hand-off every 32 steps (halos of 32 cells: a row's halo
+  // is only its two ends), the narrowest of 32, 64 or 128 cells that the SMs
+  // hold.  Measured on GB300 (images of 128^2 to 8192^2, lamb 0.5 and 1):
+  // S = 32 was the fastest period (11-20% ahead of S = 8 on the pass kernel's
+  // tiles) and the row-tile kernel with narrow tiles the fastest form (4096^2:
+  // 18.3 ms on the cost model's plan, 13.0 on the pass kernel's 128-cell
+  // tiles, 7.85 on 32-cell row tiles).  Images of 1 to 4 channels; more take
+  // the pass kernel.
+  if (!found && cross == 1 && N2 >= kRowTileMinRow) {
     for (int T2 : {32, 64, 128}) {
       if ((N2 + T2 - 1) / T2 > max_tiles) continue;
       consider(32, 1, T2, 1, (N2 + T2 - 1) / T2, false);

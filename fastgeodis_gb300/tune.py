@@ -127,6 +127,18 @@ def cluster_candidates(cross: int, N1: int, N2: int, lean_capable: bool = True, 
     return out
 
 
+def row_tile_candidates(cross: int, N2: int, sms: int, channels: int = 1,
+                        periods: Sequence[int] = (16, 32), widths: Sequence[int] = (32, 64, 128)
+                        ) -> List[Tuple[int, int, int, int]]:
+    """Row-tile plans of a 2D pass: (S, 1, T2, FG_PLAN_ROWS) for tiles of
+    `widths` cells narrower than the row, halos of S cells, at most 512
+    threads (T2 + 2 S) and every tile resident; images of 1 to 4 channels."""
+    if cross != 1 or channels > 4:
+        return []
+    return [(S, 1, T2, _lib.FG_PLAN_ROWS) for S in periods for T2 in widths
+            if T2 < N2 and T2 + 2 * S <= 512 and _ceil(N2, T2) <= sms]
+
+
 def pass_keys(shape: Sequence[int]) -> List[Key]:
     """Distinct (cross, N1, N2) cross-sections of a transform's passes."""
     if len(shape) == 2:
@@ -273,6 +285,8 @@ def autotune(shape: Sequence[int], channels: int = 1, lamb: float = 0.5, spacing
             # cluster plans (one thread-block cluster per transform): they pay
             # off when several transforms share the GPU
             trials += cluster_candidates(cross, N1, N2, lean_capable=lean, one_channel=channels <= 1)
+            # 2D rows: one thread per cell on row tiles
+            trials += row_tile_candidates(cross, N2, sms, channels)
             for c in trials:
                 _lib.check(L.fg_plan_override(cross, N1, N2, *c[:3], c[3] | mflag))
                 try:

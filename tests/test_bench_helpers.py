@@ -38,3 +38,20 @@ def test_spawned_ranks_report_the_world_size():
         assert len(lines) == 1, out.stdout
         assert lines[0]["n_gpus"] == 2 and lines[0]["max_over_ranks"] == 2.0
         assert lines[0].get("impl") == ("reference" if extra else None)
+
+
+def test_sweep_kernel_names_follow_the_plans():
+    """The bench line's kernel: the one-CTA kernel for a 2D image with a side
+    under 128, the planner's row tiles for 512 x 512, pinned plans' kinds."""
+    from fastgeodis_gb300 import _lib
+
+    w = bench.workload("c1")
+    assert bench.sweep_kernel_name(w, None) == "fg_row_tile_kernel"
+    small = dict(w, image=np.zeros((1, 1, 64, 300), np.float32))
+    assert bench.sweep_kernel_name(small, None) == "fg_row2d_kernel"
+    pinned = {"plans": {"1,1,512": [8, 1, 128, 0]}}
+    assert bench.sweep_kernel_name(w, pinned) == "fg_pass_kernel"
+    vol = dict(w, dims=3, image=np.zeros((1, 1, 16, 32, 32), np.float32))
+    pinned = {"plans": {"2,32,32": [8, 16, 32, _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2], "2,16,32": [0, 0, 0, 0]}}
+    names = bench.sweep_kernel_name(vol, pinned).split(" + ")
+    assert names[0] == "fg_sweep_cluster_kernel" and len(names) == 2

@@ -2,6 +2,9 @@
 returns respects the kernel's limits (region cells, threads, co-resident
 tiles, shared memory) and the tiling rules, for 2D rows and 3D planes, and
 honours plan overrides and tuning caps.  No kernel is launched."""
+import os
+import re
+
 import pytest
 
 from fastgeodis_gb300 import _lib
@@ -260,10 +263,10 @@ def test_chunked_override():
     assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
 
 
-@pytest.mark.parametrize("N2,T2", [(513, 32), (600, 32), (1024, 32), (4864, 32), (4865, 64), (8192, 64),
-                                   (9729, 128), (19456, 128)])
+@pytest.mark.parametrize("N2,T2", [(128, 32), (300, 32), (512, 32), (513, 32), (600, 32), (1024, 32), (4864, 32),
+                                   (4865, 64), (8192, 64), (9729, 128), (19456, 128)])
 def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
-    """2D rows of more than 512 cells: row tiles (one thread per cell of a
+    """2D rows of 128 cells and more: row tiles (one thread per cell of a
     tile and its halos), the narrowest of 32, 64, 128 cells that fits the
     SMs, a hand-off every 32 steps (the measured optimum)."""
     p = _lib.plan_describe(1, 1, N2)
@@ -273,8 +276,20 @@ def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
     # more than 4 channels take the pass kernel on 128-cell tiles
     q = _lib.plan_describe(1, 1, N2, C=6)
     assert not q["lean"] & _lib.FG_PLAN_ROWS and q["T2"] in (128, T2) or q["S"] <= 8
-    # rows up to 512 cells and images wider than 152 such tiles keep the cost model's plan
-    assert _lib.plan_describe(1, 1, 512)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
+    # rows shorter than 128 cells and images wider than 152 such tiles keep the cost model's plan
+    assert _lib.plan_describe(1, 1, 127)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
+
+
+def test_one_launch_rule():
+    """The per-call path's one-CTA launch: sides up to 512, one under 128."""
+    assert _lib.FG_ROW_TILE_MIN_ROW == 128 and _lib.FG_ONE_LAUNCH_SIDE == 512
+    assert _lib.runs_in_one_launch((64, 96)) and _lib.runs_in_one_launch((512, 127))
+    assert _lib.runs_in_one_launch((1, 5))
+    for shape in [(128, 128), (512, 512), (127, 513), (256, 300)]:
+        assert not _lib.runs_in_one_launch(shape), shape
+    header = open(os.path.join(os.path.dirname(__file__), "..", "include", "fastgeodis_gb300.h")).read()
+    for name in ("FG_ROW_TILE_MIN_ROW", "FG_ONE_LAUNCH_SIDE"):
+        assert re.search(rf"#define {name} (\d+)", header).group(1) == str(getattr(_lib, name))
 
 
 def test_row_tile_override_validation():

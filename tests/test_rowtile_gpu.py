@@ -2,7 +2,7 @@
 per tile and one thread per cell of the tile and its halos of S cells, with
 a hand-off of the halos through exchange words every S steps
 (fastgeodis_gb300/csrc/fg_rowtile2d.cu).  The planner takes them for rows of
-more than 512 cells; here they are also forced with fg_plan_override
+128 cells and more; here they are also forced with fg_plan_override
 (FG_PLAN_ROWS) onto small images, through every variant (1 to 4 channels,
 one or two maps, the three arithmetic modes, both layouts, S from 1 to 32).
 The bar is the oracle's bits."""
@@ -69,13 +69,16 @@ def test_forced_row_tiles(op, C, lamb, S, T2):
         tune.clear(shape)
 
 
-@pytest.mark.parametrize("shape,C", [((1500, 1300), 1), ((700, 2100), 3), ((3000, 600), 1)])
+@pytest.mark.parametrize("shape,C", [((1500, 1300), 1), ((700, 2100), 3), ((3000, 600), 1), ((512, 512), 1),
+                                     ((200, 384), 4), ((128, 130), 2), ((90, 700), 1)])
 def test_planner_row_tiles(shape, C):
-    """The planner's own plan for rows of more than 512 cells: 128-cell row
-    tiles with a hand-off every 32 steps."""
+    """The planner's own plan for rows of 128 cells and more: row tiles of
+    32 to 128 cells with a hand-off every 32 steps (shorter rows: the cost
+    model's plan on the pass kernel)."""
+    assert not _lib.runs_in_one_launch(shape)
     for k in tune.pass_keys(shape):
         p = _lib.plan_describe(*k, C=C)
-        assert bool(p["lean"] & ROWS) == (k[2] > 512), (k, p)
+        assert bool(p["lean"] & ROWS) == (k[2] >= _lib.FG_ROW_TILE_MIN_ROW), (k, p)
     img, m = _case(shape, C, 5 + C)
     ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
     got = fg.generalised_geodesic2d(ti, tm, 1e10, 0.5, 2)[0].cpu().numpy()

@@ -63,6 +63,24 @@ def test_cluster_candidates_fit_the_kernel(N1, N2):
         assert tune.cluster_candidates(2, N1, N2) == []
 
 
+@pytest.mark.parametrize("N2,C", [(128, 1), (300, 3), (512, 4), (5000, 1), (64, 1), (300, 5)])
+def test_row_tile_candidates_pin_row_tiles(N2, C):
+    """Each 2D row-tile candidate pins as a row-tile plan (T2 + 2 S threads
+    at most 512, narrower than the row); none for volumes or 5+ channels."""
+    L = _lib.load()
+    cands = tune.row_tile_candidates(1, N2, 152, C)
+    assert (cands == []) == (C > 4 or N2 <= 32)
+    try:
+        for S, T1, T2, flags in cands:
+            assert flags == _lib.FG_PLAN_ROWS and T1 == 1 and T2 < N2 and T2 + 2 * S <= 512
+            _lib.check(L.fg_plan_override(1, 1, N2, S, T1, T2, flags))
+            p = _lib.plan_describe(1, 1, N2, C=C)
+            assert p["lean"] == _lib.FG_PLAN_ROWS and (p["S"], p["T2"]) == (S, T2), (S, T2, p)
+    finally:
+        _lib.check(L.fg_plan_override(1, 1, N2, 0, 0, 0, 0))
+    assert tune.row_tile_candidates(2, 64, 64, 152) == []
+
+
 def test_pass_keys():
     assert tune.pass_keys((5, 7)) == [(1, 1, 7), (1, 1, 5)]
     assert tune.pass_keys((6, 6)) == [(1, 1, 6)]
@@ -121,6 +139,10 @@ def test_every_candidate_plan_gives_the_oracle_bits(shape, C):
                     _lib.check(L.fg_plan_override(*key, *c, lean))
                     got = run()[0].cpu().numpy()
                     assert bits_equal(got, want), (key, c, lean, np.abs(got - want).max())
+            for c in tune.row_tile_candidates(*key[::2], sms, C):  # 2D: row tiles
+                _lib.check(L.fg_plan_override(*key, *c))
+                got = run()[0].cpu().numpy()
+                assert bits_equal(got, want), (key, c, np.abs(got - want).max())
             _lib.check(L.fg_plan_override(*key, 0, 0, 0, 0))
         fg.check_status()
     finally:
