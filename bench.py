@@ -936,9 +936,9 @@ def sweep_kernel_name(w, tuned):
     flags += [int(v[3]) for k, v in plans.items() if k.count(",") == 3 and int(v[0]) > 0]  # per-mode plans
     names = []
     for f in flags:
-        name = ("fg_sweep_cluster_kernel" if f & _lib.FG_PLAN_RUNS2 else
-                "fg_pass_cluster_kernel" if f & _lib.FG_PLAN_CLUSTER else
-                "fg_row_tile_kernel" if f & _lib.FG_PLAN_ROWS else "fg_pass_kernel")
+        name = ("fg_row_tile_kernel" if f & _lib.FG_PLAN_ROWS else
+                "fg_sweep_cluster_kernel" if f & _lib.FG_PLAN_RUNS2 else
+                "fg_pass_cluster_kernel" if f & _lib.FG_PLAN_CLUSTER else "fg_pass_kernel")
         if name not in names:
             names.append(name)
     return " + ".join(names)  # the sweep kernels of the transform's passes

@@ -154,8 +154,10 @@ int cluster_capacity(int size, int threads, size_t smem, int *out);
 // 2D passes on row tiles (fg_rowtile2d.cu): c.tiles CTAs of a cooperative
 // launch, one thread per cell of a tile of a.T2 cells and its halos of a.K2 =
 // a.S cells; row_tile_smem: its shared memory for `cimg` image channels read.
-int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
-size_t row_tile_smem(int cimg, int M, int R, int S, bool wt);
+// clu: the tiles are one thread-block cluster and hand over through
+// distributed shared memory (2 to 16 tiles, halos of S <= T2 cells).
+int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, bool clu, cudaStream_t s);
+size_t row_tile_smem(int cimg, int M, int R, int S, bool wt, bool clu);
 
 // A whole 2D transform (plain, or signed) of one image with both sides up to
 // kOneLaunchSide by one CTA in one launch (fg_row2d.cu, one thread per cell

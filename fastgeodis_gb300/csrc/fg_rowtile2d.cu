@@ -20,6 +20,16 @@
 // layout keep S rows and flush them transposed at chunk ends (S consecutive
 // positions of a cell are contiguous there).  Arithmetic as every other
 // path: the same candidate expression in the reference's operation order.
+//
+// Cluster form (CLU, 2 to 16 tiles, halos no wider than a tile): the CTAs are
+// one thread-block cluster and the hand-off goes through distributed shared
+// memory instead: at a chunk's end each own cell within S of a tile boundary
+// is stored with st.async into the neighbour's receive rows (two parities,
+// one per side), completing on the neighbour's mbarrier of that parity; at
+// the next chunk's start the halo threads wait on it (bounded) and copy the
+// received row into the ring.  A neighbour cannot be two hand-offs ahead (it
+// needs this CTA's row of the hand-off between), so two parities suffice.
+#include "fg_pass.cuh"
 #include "fg_wait.cuh"
 
 namespace fgi {
@@ -29,7 +39,7 @@ __device__ __forceinline__ void st_word_rt(unsigned long long *p, unsigned long 
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
 }
 
-template <int C, int M, int MODE, bool WT>
+template <int C, int M, int MODE, bool WT, bool CLU>
 __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
   extern __shared__ __align__(16) float sm[];
   constexpr int CI = MODE == MODE_EUCLID ? 0 : C;  // image channels read
@@ -60,7 +70,34 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
   // exchange words of this cell: [2 parities][kMaxMaps][N2]
   unsigned long long *const xw = a.xch + g2;
   const long long xpar = (long long)kMaxMaps * N2;
+  // cluster form: receive rows [2 parities][2 sides][M][K] after the rings,
+  // then two mbarriers (one per parity)
+  float *const rbuf = irow + 2 * CI * RP;
+  const int nq = (L + S - 1) / S - 1;  // hand-offs of the pass
+  const int xo = tid - K;              // this thread's cell within the tile (own cells: 0 .. T2-1)
+  unsigned cbar = 0, rbl = 0, rbr = 0, barl = 0, barr = 0, cl_bytes = 0;
+  bool pushl = false, pushr = false, dead = false;
+  if (CLU) {
+    const int tiles = a.tiles2;
+    const unsigned rb = smem_u32(rbuf);
+    cbar = rb + 4u * (unsigned)(4 * M * K);
+    const int nl = ti > 0 ? K : 0, nr = ti < tiles - 1 ? min(K, N2 - (ti + 1) * T2) : 0;
+    cl_bytes = (unsigned)((nl + nr) * M * 4);
+    // own cells within K of a boundary go to that neighbour's halo of this side
+    pushl = own && ti > 0 && xo < K;
+    pushr = own && ti < tiles - 1 && xo >= T2 - K;
+    if (pushl) rbl = cl_map(rb, (unsigned)(ti - 1)), barl = cl_map(cbar, (unsigned)(ti - 1));
+    if (pushr) rbr = cl_map(rb, (unsigned)(ti + 1)), barr = cl_map(cbar, (unsigned)(ti + 1));
+    if (tid == 0) {
+      mbar_init(cbar, 1);
+      mbar_init(cbar + 8, 1);
+      mbar_fence_init();
+      if (nq >= 1) mbar_expect(cbar, cl_bytes);      // hand-off 0
+      if (nq >= 2) mbar_expect(cbar + 8, cl_bytes);  // hand-off 1
+    }
+  }
   __syncthreads();
+  if (CLU) cl_sync();  // rings filled and mbarriers armed in every CTA before the first store
 
   // steps of own inputs held in registers, loaded through L2 ahead of their
   // use: deep enough to cover DRAM latency for images beyond L2 (on 4096^2
@@ -86,7 +123,21 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
 #pragma unroll
     for (int c = 0; c < CI; c++) ic[c] = ni[set][c];
     if (valid && t + PF < L) load(set);
-    if (t > 0 && (t & (S - 1)) == 0) {
+    if (CLU && t > 0 && (t & (S - 1)) == 0) {
+      // the halo's previous row from the neighbours' stores of hand-off q
+      const int q = (t >> lgS) - 1;
+      const unsigned bar = cbar + (unsigned)(q & 1) * 8u;
+      if ((halo || tid == 0) && !dead) {
+        if (!wait_phase(bar, (unsigned)(q >> 1) & 1u, a.status, kClusterSpinLimit)) dead = true;  // results void
+        if (tid == 0 && !dead && q + 2 < nq) mbar_expect(bar, cl_bytes);  // the same parity's next hand-off
+      }
+      if (halo) {
+        const float *src = rbuf + (q & 1) * 2 * M * K + (tid < K ? tid : M * K + tid - K - T2);
+#pragma unroll
+        for (int m = 0; m < M; m++) drow[((t - 1) & (SR - 1)) * M * RP + m * RP + tid + 1] = src[m * K];
+      }
+      __syncthreads();
+    } else if (t > 0 && (t & (S - 1)) == 0) {
       // the halo's previous row from the owners' words of the chunk just ended
       if (halo) {
         const unsigned want = a.epoch_base + (unsigned)(t >> lgS);
@@ -145,7 +196,20 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
 #pragma unroll
           for (int m = 0; m < M; m++) a.ddst[m][woff] = best[m];
         }
-        if (((t + 1) & (S - 1)) == 0 && t + 1 < L) {
+        if (CLU && ((t + 1) & (S - 1)) == 0 && t + 1 < L) {
+          // last step of a chunk: this cell into the neighbours' receive rows
+          const int q = ((t + 1) >> lgS) - 1;
+          const unsigned po = (unsigned)((q & 1) * 2 * M * K), bo = (unsigned)(q & 1) * 8u;
+          if (pushl) {  // the left neighbour's right halo, cell xo
+#pragma unroll
+            for (int m = 0; m < M; m++) st_async1(rbl + 4u * (po + (unsigned)(M * K + m * K + xo)), best[m], barl + bo);
+          }
+          if (pushr) {  // the right neighbour's left halo, cell xo - (T2 - K)
+#pragma unroll
+            for (int m = 0; m < M; m++)
+              st_async1(rbr + 4u * (po + (unsigned)(m * K + xo - (T2 - K))), best[m], barr + bo);
+          }
+        } else if (((t + 1) & (S - 1)) == 0 && t + 1 < L) {
           // last step of a chunk: publish this cell for the neighbours' halos
           const unsigned long long ep = (unsigned long long)(a.epoch_base + (unsigned)((t + 1) >> lgS)) << 32;
           unsigned long long *w = xw + (long long)(((t + 1) >> lgS) & 1) * xpar;
@@ -178,11 +242,25 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
     for (int k = 0; k < PF; k++)
       if (t + k < L) step(t + k, k);
   }
+  if (CLU) {
+    cl_sync();  // no CTA leaves while a neighbour may still store into its shared memory
+    if (tid == 0) {
+      mbar_inval(cbar);
+      mbar_inval(cbar + 8);
+    }
+  }
 }
 
 template <int C, int M, int MODE>
-int launch_rt(const PassArgs &a, const LaunchCfg &c, bool wt, cudaStream_t s) {
-  void (*fn)(const PassArgs) = wt ? fg_row_tile_kernel<C, M, MODE, true> : fg_row_tile_kernel<C, M, MODE, false>;
+int launch_rt(const PassArgs &a, const LaunchCfg &c, bool wt, bool clu, cudaStream_t s) {
+  if (clu) {
+    static unsigned long long configured_cl[2] = {0, 0};  // bit per device (set under the engine's launch lock)
+    void (*fc)(const PassArgs) =
+        wt ? fg_row_tile_kernel<C, M, MODE, true, true> : fg_row_tile_kernel<C, M, MODE, false, true>;
+    return launch_one_cluster((const void *)fc, configured_cl[wt], a, c, s);
+  }
+  void (*fn)(const PassArgs) =
+      wt ? fg_row_tile_kernel<C, M, MODE, true, false> : fg_row_tile_kernel<C, M, MODE, false, false>;
   static unsigned long long configured[2] = {0, 0};  // bit per device (set under the engine's launch lock)
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -202,34 +280,38 @@ int launch_rt(const PassArgs &a, const LaunchCfg &c, bool wt, cudaStream_t s) {
 }
 
 template <int M, int MODE>
-int launch_rt_c(const PassArgs &a, const LaunchCfg &c, bool wt, cudaStream_t s) {
+int launch_rt_c(const PassArgs &a, const LaunchCfg &c, bool wt, bool clu, cudaStream_t s) {
   switch (a.C) {
-    case 1: return launch_rt<1, M, MODE>(a, c, wt, s);
-    case 2: return launch_rt<2, M, MODE>(a, c, wt, s);
-    case 3: return launch_rt<3, M, MODE>(a, c, wt, s);
-    case 4: return launch_rt<4, M, MODE>(a, c, wt, s);
+    case 1: return launch_rt<1, M, MODE>(a, c, wt, clu, s);
+    case 2: return launch_rt<2, M, MODE>(a, c, wt, clu, s);
+    case 3: return launch_rt<3, M, MODE>(a, c, wt, clu, s);
+    case 4: return launch_rt<4, M, MODE>(a, c, wt, clu, s);
     default: return set_error(FG_ERR_UNSUPPORTED, "row tiles read 1 to 4 image channels");
   }
 }
 
 template <int M>
-int launch_rt_mode(const PassArgs &a, const LaunchCfg &c, int mode, bool wt, cudaStream_t s) {
-  if (mode == MODE_EUCLID) return launch_rt<1, M, MODE_EUCLID>(a, c, wt, s);
-  if (mode == MODE_GEO) return launch_rt_c<M, MODE_GEO>(a, c, wt, s);
-  return launch_rt_c<M, MODE_GENERAL>(a, c, wt, s);
+int launch_rt_mode(const PassArgs &a, const LaunchCfg &c, int mode, bool wt, bool clu, cudaStream_t s) {
+  if (mode == MODE_EUCLID) return launch_rt<1, M, MODE_EUCLID>(a, c, wt, clu, s);
+  if (mode == MODE_GEO) return launch_rt_c<M, MODE_GEO>(a, c, wt, clu, s);
+  return launch_rt_c<M, MODE_GENERAL>(a, c, wt, clu, s);
 }
 
 }  // namespace
 
-size_t row_tile_smem(int cimg, int M, int R, int S, bool wt) {
-  return (size_t)((wt ? S : 2) * M + 2 * cimg) * ring_pitch(R + 2) * 4;
+size_t row_tile_smem(int cimg, int M, int R, int S, bool wt, bool clu) {
+  // the cluster form adds its receive rows (2 parities, 2 sides, K = S cells
+  // per map) and two mbarriers
+  return (size_t)((wt ? S : 2) * M + 2 * cimg) * ring_pitch(R + 2) * 4 + (clu ? (size_t)(4 * M * S + 4) * 4 : 0);
 }
 
-int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s) {
+int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, bool clu, cudaStream_t s) {
   if (c.threads > 512 || c.threads < a.T2 + 2 * a.K2)
     return set_error(FG_ERR_UNSUPPORTED, "row tiles: one thread per cell of a tile and its halos, at most 512");
-  if (M == 1) return launch_rt_mode<1>(a, c, mode, wt, s);
-  if (M == 2) return launch_rt_mode<2>(a, c, mode, wt, s);
+  if (clu && (c.tiles != a.tiles2 || c.tiles < 2 || c.tiles > kMaxCluster || a.K2 != a.S || a.K2 > a.T2))
+    return set_error(FG_ERR_UNSUPPORTED, "row tiles in a cluster: 2 to 16 tiles, halos of S cells at most a tile wide");
+  if (M == 1) return launch_rt_mode<1>(a, c, mode, wt, clu, s);
+  if (M == 2) return launch_rt_mode<2>(a, c, mode, wt, clu, s);
   return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
 }
 

@@ -132,11 +132,19 @@ def row_tile_candidates(cross: int, N2: int, sms: int, channels: int = 1,
                         ) -> List[Tuple[int, int, int, int]]:
     """Row-tile plans of a 2D pass: (S, 1, T2, FG_PLAN_ROWS) for tiles of
     `widths` cells narrower than the row, halos of S cells, at most 512
-    threads (T2 + 2 S) and every tile resident; images of 1 to 4 channels."""
+    threads (T2 + 2 S) and every tile resident; images of 1 to 4 channels.
+    Where the tiles can form one thread-block cluster (2 to 16 tiles, S <=
+    T2) the clustered form (| FG_PLAN_CLUSTER) follows each."""
     if cross != 1 or channels > 4:
         return []
-    return [(S, 1, T2, _lib.FG_PLAN_ROWS) for S in periods for T2 in widths
-            if T2 < N2 and T2 + 2 * S <= 512 and _ceil(N2, T2) <= sms]
+    out = []
+    for S in periods:
+        for T2 in widths:
+            if T2 < N2 and T2 + 2 * S <= 512 and _ceil(N2, T2) <= sms:
+                out.append((S, 1, T2, _lib.FG_PLAN_ROWS))
+                if _ceil(N2, T2) <= 16 and S <= T2:
+                    out.append((S, 1, T2, _lib.FG_PLAN_ROWS | _lib.FG_PLAN_CLUSTER))
+    return out
 
 
 def pass_keys(shape: Sequence[int]) -> List[Key]:

@@ -67,7 +67,8 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 
 /* Plan flags (fg_plan_override's `lean` argument, fg_plan_describe's last field). */
 #define FG_PLAN_LEAN 1    /* the 64-register kernel */
-#define FG_PLAN_CLUSTER 2 /* a cluster plan: one thread-block cluster owns the cross-section */
+#define FG_PLAN_CLUSTER 2 /* a cluster plan: one thread-block cluster owns the cross-section (with
+                           * FG_PLAN_ROWS: row tiles forming one cluster) */
 #define FG_PLAN_RUNS2 4   /* cluster plan on the cluster sweep kernel, 2 runs of 4 cells per thread */
 #define FG_PLAN_CHUNKED 8 /* a tile plan run as one ordinary launch per chunk of S steps */
 #define FG_PLAN_ROWS 64   /* a 2D tile plan on the row-tile kernel: one thread per cell of a tile and its halos */
@@ -98,7 +99,14 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * its tiles need not all be resident at once: each launch's CTAs start from
  * the previous row that the launch before published.  The planner takes a
  * chunked plan by itself only for cross-sections whose tiles cannot all be
- * resident (volumes with slices beyond about 600 thousand cells).
+ * resident (volumes with slices beyond about 600 thousand cells).  With
+ * FG_PLAN_ROWS (2D only) a tile plan of 1 to 4 image channels and at most
+ * 512 cells per tile and halos runs on the row-tile kernel, one thread per
+ * cell; adding FG_PLAN_CLUSTER makes its tiles one thread-block cluster that
+ * hands the halos over through distributed shared memory (2 to 16 tiles;
+ * otherwise the hand-off goes through global memory as without the flag).
+ * The planner takes row tiles for rows of FG_ROW_TILE_MIN_ROW cells and
+ * more, clustered for rows of up to 1024 cells.
  * FG_PLAN_MODE(m) restricts the plan to passes
  * of one arithmetic mode (several transforms of one shape with different
  * weights, e.g. the lambdas of one image, may then get different plans).
@@ -121,7 +129,8 @@ FG_API int fg_cluster_capacity(int cluster_size, int threads, size_t smem, int *
  * general, 1 l_grad == 0, 2 l_eucl == 0 and l_grad == 1), transposed write
  * or not, on a GPU of `sms` SMs.  Writes 11 ints to `plan`: S, T1, T2, K1,
  * K2, tiles1, tiles2, threads, staging depth, shared-memory bytes, flags
- * (FG_PLAN_LEAN, FG_PLAN_CLUSTER, FG_PLAN_RUNS2, FG_PLAN_CHUNKED).  Needs
+ * (FG_PLAN_LEAN, FG_PLAN_CLUSTER, FG_PLAN_RUNS2, FG_PLAN_CHUNKED,
+ * FG_PLAN_ROWS).  Needs
  * no GPU; honours fg_set_tuning and fg_plan_override. */
 FG_API int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int transposed_write, int sms,
                             int *plan);

@@ -49,9 +49,13 @@ def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
     assert T1 >= K1 and T2 >= K2, "a halo reaches only the adjacent tiles"
     R1 = T1 + 2 * K1 if cross == 2 else 1
     R2 = T2 + 2 * K2
-    if lean == _lib.FG_PLAN_ROWS:
-        # row tiles: 2D, one thread per cell of a tile and its halos, at most 512
+    if lean & _lib.FG_PLAN_ROWS:
+        # row tiles: 2D, one thread per cell of a tile and its halos, at most
+        # 512; as one thread-block cluster: 2 to 16 tiles, halos within a tile
+        assert lean in (_lib.FG_PLAN_ROWS, _lib.FG_PLAN_ROWS | _lib.FG_PLAN_CLUSTER)
         assert cross == 1 and t2 > 1 and C <= 4 and R2 <= nt <= 512 and nt % 32 == 0
+        if lean & _lib.FG_PLAN_CLUSTER:
+            assert t2 <= 16 and K2 == S <= T2
         assert smem <= SMEM_LIMIT
         return
     runs = R1 * (-(-R2 // 4))
@@ -263,16 +267,19 @@ def test_chunked_override():
     assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
 
 
-@pytest.mark.parametrize("N2,T2", [(128, 32), (300, 32), (512, 32), (513, 32), (600, 32), (1024, 32), (4864, 32),
-                                   (4865, 64), (8192, 64), (9729, 128), (19456, 128)])
+@pytest.mark.parametrize("N2,T2", [(128, 32), (300, 32), (512, 32), (513, 64), (600, 64), (1024, 64), (1025, 32),
+                                   (4864, 32), (4865, 64), (8192, 64), (9729, 128), (19456, 128)])
 def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
     """2D rows of 128 cells and more: row tiles (one thread per cell of a
-    tile and its halos), the narrowest of 32, 64, 128 cells that fits the
-    SMs, a hand-off every 32 steps (the measured optimum)."""
+    tile and its halos), a hand-off every 32 steps (the measured optimum).
+    Rows up to 1024 cells: one thread-block cluster of at most 16 tiles (32
+    cells up to 512, else 64); longer rows: the narrowest of 32, 64, 128
+    cells that fits the SMs, handing over through global memory."""
     p = _lib.plan_describe(1, 1, N2)
     assert (p["S"], p["T1"], p["T2"], p["K2"]) == (32, 1, T2, 32)
     assert p["tiles2"] == -(-N2 // T2) <= 152 and p["threads"] == T2 + 64
-    assert p["lean"] == _lib.FG_PLAN_ROWS
+    clu = _lib.FG_PLAN_CLUSTER if N2 <= 1024 else 0
+    assert p["lean"] == _lib.FG_PLAN_ROWS | clu and (not clu or p["tiles2"] <= 16)
     # more than 4 channels take the pass kernel on 128-cell tiles
     q = _lib.plan_describe(1, 1, N2, C=6)
     assert not q["lean"] & _lib.FG_PLAN_ROWS and q["T2"] in (128, T2) or q["S"] <= 8
@@ -306,3 +313,37 @@ def test_row_tile_override_validation():
         assert not _lib.plan_describe(1, 1, 300)["lean"] & ROWS
     finally:
         _lib.check(L.fg_plan_override(1, 1, 300, 0, 0, 0, 0))
+
+
+@pytest.mark.parametrize("N2,S,T2,clu", [(512, 32, 32, True), (211, 4, 20, True), (1024, 32, 64, True),
+                                         (1024, 32, 32, False), (492, 32, 32, True), (300, 8, 16, False),
+                                         (300, 8, 300, False)])
+def test_cluster_row_tile_overrides(N2, S, T2, clu):
+    """FG_PLAN_ROWS | FG_PLAN_CLUSTER: row tiles as one thread-block cluster
+    when there are 2 to 16 tiles with halos no wider than a tile; otherwise
+    the same row tiles with the hand-off through global memory (or the
+    planner's plan for one tile).  The cluster form adds its receive rows and
+    two mbarriers to the shared memory."""
+    L = _lib.load()
+    ROWS, CLU = _lib.FG_PLAN_ROWS, _lib.FG_PLAN_CLUSTER
+    try:
+        for maps, wt in ((1, False), (2, True)):
+            _lib.check(L.fg_plan_override(1, 1, N2, S, 1, T2, ROWS | CLU))
+            p = _lib.plan_describe(1, 1, N2, maps=maps, transposed_write=wt)
+            _lib.check(L.fg_plan_override(1, 1, N2, S, 1, T2, ROWS))
+            q = _lib.plan_describe(1, 1, N2, maps=maps, transposed_write=wt)
+            if T2 >= N2:
+                assert not p["lean"] & ROWS
+                continue
+            assert p["lean"] == (ROWS | CLU if clu else ROWS) and q["lean"] == ROWS
+            assert (p["tiles2"], p["threads"]) == (q["tiles2"], q["threads"])
+            assert p["smem"] - q["smem"] == ((4 * maps * S + 4) * 4 if clu else 0)
+            if clu:
+                assert 2 <= p["tiles2"] <= 16 and S <= T2
+    finally:
+        _lib.check(L.fg_plan_override(1, 1, N2, 0, 0, 0, 0))
+    # no runs per thread or chunks with row tiles; a cluster flag alone stays a volume plan
+    assert L.fg_plan_override(1, 1, 300, 8, 1, 64, ROWS | CLU | _lib.FG_PLAN_RUNS2) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_plan_override(1, 1, 300, 8, 1, 64, ROWS | CLU | _lib.FG_PLAN_CHUNKED) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_plan_override(1, 1, 300, 8, 1, 64, CLU) == _lib.FG_ERR_INVALID_ARGUMENT
+    assert L.fg_plan_override(2, 64, 64, 8, 8, 8, ROWS | CLU) == _lib.FG_ERR_INVALID_ARGUMENT

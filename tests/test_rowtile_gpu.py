@@ -18,6 +18,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 ROWS = _lib.FG_PLAN_ROWS
+CLU = _lib.FG_PLAN_CLUSTER
 
 
 def _case(shape, C, seed, soft=False):
@@ -29,11 +30,11 @@ def _case(shape, C, seed, soft=False):
     return img, m
 
 
-def _pin(shape, S, T2):
-    tune.pin({k: (S, 1, T2, ROWS) for k in tune.pass_keys(shape)})
+def _pin(shape, S, T2, flags=ROWS):
+    tune.pin({k: (S, 1, T2, flags) for k in tune.pass_keys(shape)})
     for k in tune.pass_keys(shape):
         p = _lib.plan_describe(*k)
-        assert p["lean"] & ROWS and p["S"] == S and p["tiles2"] > 1, (k, p)
+        assert p["lean"] == flags and p["S"] == S and p["tiles2"] > 1, (k, p)
 
 
 @pytest.mark.parametrize("op,C,lamb,S,T2", [
@@ -48,11 +49,15 @@ def _pin(shape, S, T2):
     ("gsf", 1, 0.7, 16, 36),
 ])
 def test_forced_row_tiles(op, C, lamb, S, T2):
+    _forced(op, C, lamb, S, T2, ROWS)
+
+
+def _forced(op, C, lamb, S, T2, flags):
     shape = (97, 211)  # the passes along H have rows of 211 cells, those along W rows of 97
     img, m = _case(shape, C, 11 + C + S, soft=op == "gsf")
     ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
     try:
-        _pin(shape, S, T2)
+        _pin(shape, S, T2, flags)
         if op == "plain":
             got = fg.generalised_geodesic2d(ti, tm, 1e10, lamb, 2)
             want = oracle.geodesic2d(img, m, 1e10, lamb, 2)
@@ -64,6 +69,42 @@ def test_forced_row_tiles(op, C, lamb, S, T2):
             want = oracle.gsf2d(img, m, 0.4, 1e10, lamb, 1)
         got = got[0].cpu().numpy()
         assert bits_equal(got, want), float(np.nanmax(np.abs(got - want)))
+        fg.check_status()
+    finally:
+        tune.clear(shape)
+
+
+@pytest.mark.parametrize("op,C,lamb,S,T2", [
+    ("plain", 1, 0.6, 8, 32),
+    ("plain", 1, 0.0, 4, 20),
+    ("plain", 1, 1.0, 32, 64),
+    ("plain", 3, 0.5, 16, 48),
+    ("plain", 4, 0.3, 2, 16),
+    ("plain", 2, 0.8, 1, 16),    # a hand-off every step
+    ("signed", 1, 0.5, 32, 40),
+    ("signed", 3, 1.0, 8, 44),
+    ("gsf", 1, 0.7, 16, 36),
+])
+def test_forced_cluster_row_tiles(op, C, lamb, S, T2):
+    """Row tiles as one thread-block cluster (FG_PLAN_ROWS | FG_PLAN_CLUSTER):
+    the halos handed over through distributed shared memory."""
+    _forced(op, C, lamb, S, T2, ROWS | CLU)
+
+
+@pytest.mark.parametrize("shape,S", [((150, 492), 32), ((492, 150), 16), ((40, 512), 32)])
+def test_cluster_row_tiles_with_a_short_last_tile(shape, S):
+    """16 tiles of 32 cells whose last tile holds fewer cells than a halo
+    (492 = 15 x 32 + 12), and 5 tiles of a 150-cell row: the cluster form
+    expects only the cells that exist."""
+    img, m = _case(shape, 1, 41 + S)
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    try:
+        _pin(shape, S, 32, ROWS | CLU)
+        for lamb in (0.4, 1.0):
+            got = fg.generalised_geodesic2d(ti, tm, 1e10, lamb, 2)[0].cpu().numpy()
+            assert bits_equal(got, oracle.geodesic2d(img, m, 1e10, lamb, 2)), lamb
+        got = fg.signed_generalised_geodesic2d(ti, tm, 1e10, 0.6, 1)[0].cpu().numpy()
+        assert bits_equal(got, oracle.signed2d(img, m, 1e10, 0.6, 1))
         fg.check_status()
     finally:
         tune.clear(shape)

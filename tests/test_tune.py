@@ -72,10 +72,14 @@ def test_row_tile_candidates_pin_row_tiles(N2, C):
     assert (cands == []) == (C > 4 or N2 <= 32)
     try:
         for S, T1, T2, flags in cands:
-            assert flags == _lib.FG_PLAN_ROWS and T1 == 1 and T2 < N2 and T2 + 2 * S <= 512
+            clu = -(-N2 // T2) <= 16 and S <= T2
+            assert flags in (_lib.FG_PLAN_ROWS, _lib.FG_PLAN_ROWS | _lib.FG_PLAN_CLUSTER)
+            assert T1 == 1 and T2 < N2 and T2 + 2 * S <= 512 and (clu or flags == _lib.FG_PLAN_ROWS)
             _lib.check(L.fg_plan_override(1, 1, N2, S, T1, T2, flags))
             p = _lib.plan_describe(1, 1, N2, C=C)
-            assert p["lean"] == _lib.FG_PLAN_ROWS and (p["S"], p["T2"]) == (S, T2), (S, T2, p)
+            assert p["lean"] == flags and (p["S"], p["T2"]) == (S, T2), (S, T2, p)
+        assert sum(f != _lib.FG_PLAN_ROWS for *_, f in cands) == sum(
+            -(-N2 // T2) <= 16 and S <= T2 for S, _, T2, f in cands if f == _lib.FG_PLAN_ROWS)
     finally:
         _lib.check(L.fg_plan_override(1, 1, N2, 0, 0, 0, 0))
     assert tune.row_tile_candidates(2, 64, 64, 152) == []
