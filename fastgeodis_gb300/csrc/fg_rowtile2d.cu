@@ -18,8 +18,11 @@
 // previous row's distances and image values are shared-memory rows with a
 // NaN apron (cells outside the image never win a min).  Passes that change
 // layout keep S rows and flush them transposed at chunk ends (S consecutive
-// positions of a cell are contiguous there).  Arithmetic as every other
-// path: the same candidate expression in the reference's operation order.
+// positions of a cell are contiguous there); the others write each step's
+// own cells in place (measured: holding a chunk's rows and writing them at
+// its end cost 7-13%, the burst of stores stalling the next step).
+// Arithmetic as every other path: the same candidate expression in the
+// reference's operation order.
 //
 // Cluster form (CLU, 2 to 16 tiles, halos no wider than a tile): the CTAs are
 // one thread-block cluster and the hand-off goes through distributed shared
@@ -47,7 +50,9 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
   const int L = a.L, S = a.S, lgS = __ffs(S) - 1, N2 = a.N2;
   const int ti = blockIdx.x, T2 = a.T2, K = a.K2;
   const int R = T2 + 2 * K, RP = a.rowf;  // region cells, floats per shared row (apron + R + apron)
-  const int SR = WT ? S : 2;
+  // distance rows kept: two, or a chunk's for the transposed flush (two at
+  // least: a step reads one row while it writes the next)
+  const int SR = WT && S > 2 ? S : 2;
   const int g2 = ti * T2 - K + tid;       // this thread's cell of the row
   const bool valid = tid < R && g2 >= 0 && g2 < N2;
   const bool own = valid && tid >= K && tid < K + T2;
@@ -226,7 +231,7 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
       const int cpw = 32 / S, j = lane & (S - 1);
       if (j < Sn) {
         const int so = (a.dir > 0 ? t0 + j : L - 1 - t0 - j) * (int)a.ws_str;
-        const float *src = drow + j * M * RP;
+        const float *src = drow + ((t0 + j) & (SR - 1)) * M * RP;
         const int own0 = K, nown = min(T2, N2 - ti * T2);
         for (int x = warp * cpw + (lane >> lgS); x < nown; x += nwarps * cpw) {
           const int gx = ti * T2 + x;
@@ -302,7 +307,8 @@ int launch_rt_mode(const PassArgs &a, const LaunchCfg &c, int mode, bool wt, boo
 size_t row_tile_smem(int cimg, int M, int R, int S, bool wt, bool clu) {
   // the cluster form adds its receive rows (2 parities, 2 sides, K = S cells
   // per map) and two mbarriers
-  return (size_t)((wt ? S : 2) * M + 2 * cimg) * ring_pitch(R + 2) * 4 + (clu ? (size_t)(4 * M * S + 4) * 4 : 0);
+  const size_t rings = (size_t)((wt && S > 2 ? S : 2) * M + 2 * cimg) * ring_pitch(R + 2) * 4;
+  return rings + (clu ? (size_t)(4 * M * S + 4) * 4 : 0);
 }
 
 int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, bool clu, cudaStream_t s) {

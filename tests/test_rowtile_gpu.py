@@ -44,6 +44,8 @@ def _pin(shape, S, T2, flags=ROWS):
     ("plain", 3, 0.5, 16, 48),
     ("plain", 4, 0.3, 2, 12),
     ("plain", 2, 0.8, 1, 8),     # a hand-off every step
+    ("plain", 1, 0.6, 1, 64),    # a hand-off every step, 3 warps per tile: two ring rows at least
+    ("signed", 2, 0.7, 1, 40),
     ("signed", 1, 0.5, 32, 40),
     ("signed", 3, 1.0, 8, 44),
     ("gsf", 1, 0.7, 16, 36),
@@ -81,6 +83,7 @@ def _forced(op, C, lamb, S, T2, flags):
     ("plain", 3, 0.5, 16, 48),
     ("plain", 4, 0.3, 2, 16),
     ("plain", 2, 0.8, 1, 16),    # a hand-off every step
+    ("plain", 1, 0.6, 1, 64),
     ("signed", 1, 0.5, 32, 40),
     ("signed", 3, 1.0, 8, 44),
     ("gsf", 1, 0.7, 16, 36),
