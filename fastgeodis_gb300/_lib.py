@@ -147,15 +147,16 @@ def profile_launch_times():
 
 
 FG_ONE_LAUNCH_SIDE = 512  # the one-launch 2D kernel's largest side
-FG_ROW_TILE_MIN_ROW = 128  # 2D rows of at least this many cells run on row tiles
+FG_ONE_LAUNCH_CELLS = 16384  # the per-call path runs images of fewer cells in one launch
+FG_ROW_TILE_MIN_ROW = 64  # 2D rows of at least this many cells run on row tiles
 
 
 def runs_in_one_launch(shape) -> bool:
     """Whether the per-call path runs a plain or signed 2D transform of an
     image of this (H, W) in one launch (no pinned plans or planner limits):
-    sides up to FG_ONE_LAUNCH_SIDE, one shorter than FG_ROW_TILE_MIN_ROW."""
+    fewer than FG_ONE_LAUNCH_CELLS cells, sides up to FG_ONE_LAUNCH_SIDE."""
     H, W = (int(x) for x in shape)
-    return max(H, W) <= FG_ONE_LAUNCH_SIDE and min(H, W) < FG_ROW_TILE_MIN_ROW
+    return max(H, W) <= FG_ONE_LAUNCH_SIDE and H * W < FG_ONE_LAUNCH_CELLS
 FG_PLAN_LEAN = 1      # plan flag: the 64-register kernel
 FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-section
 FG_PLAN_RUNS2 = 4     # plan flag: cluster sweep kernel, 2 runs of 4 cells per thread

@@ -155,9 +155,10 @@ int cluster_capacity(int size, int threads, size_t smem, int *out);
 // launch, one thread per cell of a tile of a.T2 cells and its halos of a.K2 =
 // a.S cells; row_tile_smem: its shared memory for `cimg` image channels read.
 // clu: the tiles are one thread-block cluster and hand over through
-// distributed shared memory (2 to 16 tiles, halos of S <= T2 cells).
+// distributed shared memory (2 to 16 tiles, halos of S <= T2 cells).  Row
+// tiles write in place (wt is refused: a transpose follows such a pass).
 int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, bool clu, cudaStream_t s);
-size_t row_tile_smem(int cimg, int M, int R, int S, bool wt, bool clu);
+size_t row_tile_smem(int cimg, int M, int R, int S, bool clu);
 
 // A whole 2D transform (plain, or signed) of one image with both sides up to
 // kOneLaunchSide by one CTA in one launch (fg_row2d.cu, one thread per cell
@@ -165,8 +166,9 @@ size_t row_tile_smem(int cimg, int M, int R, int S, bool wt, bool clu);
 // signed difference.
 int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, int *status, cudaStream_t s);
 constexpr int kOneLaunchSide = FG_ONE_LAUNCH_SIDE;  // the one-CTA kernel's largest side
-// 2D rows of at least this many cells are planned on row tiles; the per-call
-// path keeps the one-CTA launch for images with a side shorter than this
+// the per-call path's one-CTA launch: images of fewer cells than this
+constexpr long long kOneLaunchCells = FG_ONE_LAUNCH_CELLS;
+// 2D rows of at least this many cells are planned on row tiles
 constexpr int kRowTileMinRow = FG_ROW_TILE_MIN_ROW;
 
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept

@@ -322,13 +322,15 @@ bool cluster_plan(int N1, int N2, int C, int M, int mode, bool wt, int S, int T1
 }
 std::atomic<unsigned> g_plan_epoch{0};  // bumped when overrides change: older cache entries are stale
 
-// Measured on GB300 (square images, iterations 2, through the public call):
-// one CTA in one launch 0.28 / 0.55 / 0.87 / 1.23 ms at 128 / 256 / 384 / 512
-// per side, per-pass launches on 32-cell row tiles 0.27 / 0.47 / 0.68 / 0.88.
-// Images with a side shorter than kRowTileMinRow keep the one launch: their
-// passes along that side would not run on row tiles.
+// Measured on GB300 (iterations 2, lamb 1, through the public call): one
+// CTA in one launch 0.28 / 0.55 / 0.87 / 1.23 ms at 128 / 256 / 384 / 512
+// per side, per-pass launches on 32-cell row tiles 0.27 / 0.47 / 0.68 / 0.88
+// (global hand-offs, layout changes written by the passes); with clustered
+// row tiles the one launch still won on 64^2 (0.158 against 0.170 ms), 96^2
+// (0.215 / 0.217) and 64 x 200 (0.261 / 0.269), and lost on 120 x 300 (0.425
+// / 0.396), 64 x 512 (0.522 / 0.478) and 100 x 512 (0.664 / 0.528).
 bool one_launch_image(int H, int W) {
-  if (std::max(H, W) > kOneLaunchSide || std::min(H, W) >= kRowTileMinRow || g_tune_region.load() < kMaxRegion ||
+  if (std::max(H, W) > kOneLaunchSide || (long long)H * W >= kOneLaunchCells || g_tune_region.load() < kMaxRegion ||
       g_tune_tiles.load() > 0)
     return false;
   std::lock_guard<std::mutex> g(g_override_mu);
@@ -420,7 +422,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     p.rowcl = clu && p.tiles2 <= kMaxCluster && p.K2 == p.S && p.K2 <= p.T2;
     p.NT = (R + 31) / 32 * 32;
     p.rowf = ring_pitch(R + 2);
-    p.smem = row_tile_smem(C, M, R, p.S, wt, p.rowcl);
+    p.smem = row_tile_smem(C, M, R, p.S, p.rowcl);
     p.lean = false;
     return true;
   };
@@ -441,7 +443,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   // Rows (2D passes) of kRowTileMinRow cells and more: row tiles (one thread
   // per cell) with a hand-off every 32 steps (halos of 32 cells: a row's halo
   // is only its two ends), the narrowest of 32, 64 or 128 cells that the SMs
-  // hold.  Measured on GB300 (images of 128^2 to 8192^2, lamb 0.5 and 1):
+  // hold.  Measured on GB300 (images of 64 x 512 to 8192^2, lamb 0.5 and 1):
   // S = 32 was the fastest period (11-20% ahead of S = 8 on the pass kernel's
   // tiles) and the row-tile kernel with narrow tiles the fastest form (4096^2:
   // 18.3 ms on the cost model's plan, 13.0 on the pass kernel's 128-cell
@@ -750,10 +752,11 @@ void axes_for(const Geometry &g, Axis *ax, int *nax) {
 // A pass that changes layout on a cluster plan (a strip of whole rows per
 // SM, thousands of own cells) would write S-element segments of every own
 // cell at each flush, one memory transaction each: measured, that doubles
-// the pass.  With `emit_t` such a pass writes in place and
+// the pass; on row tiles the transposed flush at chunk ends cost 5-7% of a
+// 2D transform.  With `emit_t` such a pass writes in place and
 // `emit_t(src, dst, rows, cols)` then transposes each map (a rows x cols
 // matrix) into the other layout at full-line width.  Without it (nullptr)
-// every pass writes its own layout change.
+// every pass writes its own layout change (row tiles then refuse the pass).
 template <typename PlanFn, typename Emit, typename EmitT>
 int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, const MapSet &ms, int iterations,
                   PlanFn plan_fn, Emit emit, EmitT *emit_t) {
@@ -780,7 +783,7 @@ int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, con
           Plan p;
           int rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, wt, &p);
           if (rc != FG_OK) return rc;
-          const bool split = wt && emit_t != nullptr && p.cluster;  // in place, then a transpose
+          const bool split = wt && emit_t != nullptr && (p.cluster || p.rowtile);  // in place, then a transpose
           if (split) {
             rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, false, &p);
             if (rc != FG_OK) return rc;

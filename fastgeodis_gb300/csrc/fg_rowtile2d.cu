@@ -16,11 +16,12 @@
 // next hand-off, so every cell computes every step.  Each thread keeps its
 // cell's old distance and image values 4-8 steps ahead in registers; the
 // previous row's distances and image values are shared-memory rows with a
-// NaN apron (cells outside the image never win a min).  Passes that change
-// layout keep S rows and flush them transposed at chunk ends (S consecutive
-// positions of a cell are contiguous there); the others write each step's
-// own cells in place (measured: holding a chunk's rows and writing them at
-// its end cost 7-13%, the burst of stores stalling the next step).
+// NaN apron (cells outside the image never win a min).  Each step's own
+// cells are written in place (measured: holding a chunk's rows and writing
+// them at its end cost 7-13%, the burst of stores stalling the next step);
+// a pass that changes layout runs in place and a tiled transpose then moves
+// the map (5-7% faster than writing the chunk's rows transposed from shared
+// memory at its end).
 // Arithmetic as every other path: the same candidate expression in the
 // reference's operation order.
 //
@@ -42,17 +43,15 @@ __device__ __forceinline__ void st_word_rt(unsigned long long *p, unsigned long 
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
 }
 
-template <int C, int M, int MODE, bool WT, bool CLU>
+template <int C, int M, int MODE, bool CLU>
 __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
   extern __shared__ __align__(16) float sm[];
   constexpr int CI = MODE == MODE_EUCLID ? 0 : C;  // image channels read
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int tid = threadIdx.x;
   const int L = a.L, S = a.S, lgS = __ffs(S) - 1, N2 = a.N2;
   const int ti = blockIdx.x, T2 = a.T2, K = a.K2;
   const int R = T2 + 2 * K, RP = a.rowf;  // region cells, floats per shared row (apron + R + apron)
-  // distance rows kept: two, or a chunk's for the transposed flush (two at
-  // least: a step reads one row while it writes the next)
-  const int SR = WT && S > 2 ? S : 2;
+  constexpr int SR = 2;  // distance rows kept: a step reads one while it writes the other
   const int g2 = ti * T2 - K + tid;       // this thread's cell of the row
   const bool valid = tid < R && g2 >= 0 && g2 < N2;
   const bool own = valid && tid >= K && tid < K + T2;
@@ -197,7 +196,7 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
 #pragma unroll
       for (int c = 0; c < CI; c++) icw[c * RP] = ic[c];
       if (own) {
-        if (!WT && t > 0) {
+        if (t > 0) {
 #pragma unroll
           for (int m = 0; m < M; m++) a.ddst[m][woff] = best[m];
         }
@@ -225,22 +224,6 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
     }
     woff += wstep;
     __syncthreads();
-    if (WT && (((t + 1) & (S - 1)) == 0 || t == L - 1)) {
-      // the chunk's own cells, transposed: lanes take S consecutive steps of 32 / S cells
-      const int t0 = t & ~(S - 1), Sn = t - t0 + 1;
-      const int cpw = 32 / S, j = lane & (S - 1);
-      if (j < Sn) {
-        const int so = (a.dir > 0 ? t0 + j : L - 1 - t0 - j) * (int)a.ws_str;
-        const float *src = drow + ((t0 + j) & (SR - 1)) * M * RP;
-        const int own0 = K, nown = min(T2, N2 - ti * T2);
-        for (int x = warp * cpw + (lane >> lgS); x < nown; x += nwarps * cpw) {
-          const int gx = ti * T2 + x;
-#pragma unroll
-          for (int m = 0; m < M; m++) a.ddst[m][so + gx * (int)a.wst2] = src[m * RP + own0 + x + 1];
-        }
-      }
-      __syncthreads();
-    }
   };
   for (int t = 0; t < L; t += PF) {
 #pragma unroll
@@ -257,23 +240,20 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
 }
 
 template <int C, int M, int MODE>
-int launch_rt(const PassArgs &a, const LaunchCfg &c, bool wt, bool clu, cudaStream_t s) {
+int launch_rt(const PassArgs &a, const LaunchCfg &c, bool clu, cudaStream_t s) {
   if (clu) {
-    static unsigned long long configured_cl[2] = {0, 0};  // bit per device (set under the engine's launch lock)
-    void (*fc)(const PassArgs) =
-        wt ? fg_row_tile_kernel<C, M, MODE, true, true> : fg_row_tile_kernel<C, M, MODE, false, true>;
-    return launch_one_cluster((const void *)fc, configured_cl[wt], a, c, s);
+    static unsigned long long configured_cl = 0;  // bit per device (set under the engine's launch lock)
+    return launch_one_cluster((const void *)fg_row_tile_kernel<C, M, MODE, true>, configured_cl, a, c, s);
   }
-  void (*fn)(const PassArgs) =
-      wt ? fg_row_tile_kernel<C, M, MODE, true, false> : fg_row_tile_kernel<C, M, MODE, false, false>;
-  static unsigned long long configured[2] = {0, 0};  // bit per device (set under the engine's launch lock)
+  void (*fn)(const PassArgs) = fg_row_tile_kernel<C, M, MODE, false>;
+  static unsigned long long configured = 0;  // bit per device (set under the engine's launch lock)
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 64 && !(configured[wt] & (1ull << dev))) {
+  if (dev < 64 && !(configured & (1ull << dev))) {
     e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return set_error(FG_ERR_CUDA, cudaGetErrorString(e));
-    configured[wt] |= 1ull << dev;
+    configured |= 1ull << dev;
   }
   void *args[] = {const_cast<PassArgs *>(&a)};
   if (c.tiles > 1)
@@ -285,39 +265,40 @@ int launch_rt(const PassArgs &a, const LaunchCfg &c, bool wt, bool clu, cudaStre
 }
 
 template <int M, int MODE>
-int launch_rt_c(const PassArgs &a, const LaunchCfg &c, bool wt, bool clu, cudaStream_t s) {
+int launch_rt_c(const PassArgs &a, const LaunchCfg &c, bool clu, cudaStream_t s) {
   switch (a.C) {
-    case 1: return launch_rt<1, M, MODE>(a, c, wt, clu, s);
-    case 2: return launch_rt<2, M, MODE>(a, c, wt, clu, s);
-    case 3: return launch_rt<3, M, MODE>(a, c, wt, clu, s);
-    case 4: return launch_rt<4, M, MODE>(a, c, wt, clu, s);
+    case 1: return launch_rt<1, M, MODE>(a, c, clu, s);
+    case 2: return launch_rt<2, M, MODE>(a, c, clu, s);
+    case 3: return launch_rt<3, M, MODE>(a, c, clu, s);
+    case 4: return launch_rt<4, M, MODE>(a, c, clu, s);
     default: return set_error(FG_ERR_UNSUPPORTED, "row tiles read 1 to 4 image channels");
   }
 }
 
 template <int M>
-int launch_rt_mode(const PassArgs &a, const LaunchCfg &c, int mode, bool wt, bool clu, cudaStream_t s) {
-  if (mode == MODE_EUCLID) return launch_rt<1, M, MODE_EUCLID>(a, c, wt, clu, s);
-  if (mode == MODE_GEO) return launch_rt_c<M, MODE_GEO>(a, c, wt, clu, s);
-  return launch_rt_c<M, MODE_GENERAL>(a, c, wt, clu, s);
+int launch_rt_mode(const PassArgs &a, const LaunchCfg &c, int mode, bool clu, cudaStream_t s) {
+  if (mode == MODE_EUCLID) return launch_rt<1, M, MODE_EUCLID>(a, c, clu, s);
+  if (mode == MODE_GEO) return launch_rt_c<M, MODE_GEO>(a, c, clu, s);
+  return launch_rt_c<M, MODE_GENERAL>(a, c, clu, s);
 }
 
 }  // namespace
 
-size_t row_tile_smem(int cimg, int M, int R, int S, bool wt, bool clu) {
-  // the cluster form adds its receive rows (2 parities, 2 sides, K = S cells
-  // per map) and two mbarriers
-  const size_t rings = (size_t)((wt && S > 2 ? S : 2) * M + 2 * cimg) * ring_pitch(R + 2) * 4;
+size_t row_tile_smem(int cimg, int M, int R, int S, bool clu) {
+  // two rows of distances and of image values; the cluster form adds its
+  // receive rows (2 parities, 2 sides, K = S cells per map) and two mbarriers
+  const size_t rings = (size_t)(2 * M + 2 * cimg) * ring_pitch(R + 2) * 4;
   return rings + (clu ? (size_t)(4 * M * S + 4) * 4 : 0);
 }
 
 int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, bool clu, cudaStream_t s) {
+  if (wt) return set_error(FG_ERR_UNSUPPORTED, "row tiles write in place (a transpose moves the map)");
   if (c.threads > 512 || c.threads < a.T2 + 2 * a.K2)
     return set_error(FG_ERR_UNSUPPORTED, "row tiles: one thread per cell of a tile and its halos, at most 512");
   if (clu && (c.tiles != a.tiles2 || c.tiles < 2 || c.tiles > kMaxCluster || a.K2 != a.S || a.K2 > a.T2))
     return set_error(FG_ERR_UNSUPPORTED, "row tiles in a cluster: 2 to 16 tiles, halos of S cells at most a tile wide");
-  if (M == 1) return launch_rt_mode<1>(a, c, mode, wt, clu, s);
-  if (M == 2) return launch_rt_mode<2>(a, c, mode, wt, clu, s);
+  if (M == 1) return launch_rt_mode<1>(a, c, mode, clu, s);
+  if (M == 2) return launch_rt_mode<2>(a, c, mode, clu, s);
   return set_error(FG_ERR_UNSUPPORTED, "a pass updates one or two distance maps");
 }
 

@@ -165,16 +165,18 @@ FG_API int fg_workspace_status(void *workspace, void *stream);
  * context stays usable.  Uses the first 256 bytes of the workspace. */
 FG_API int fg_selftest_wait(int kind, void *workspace, size_t workspace_bytes, void *stream);
 
-/* Images whose sides are all at most FG_ONE_LAUNCH_SIDE, one of them shorter
- * than FG_ROW_TILE_MIN_ROW, run their whole plain or signed transform in one
+/* Images of fewer than FG_ONE_LAUNCH_CELLS cells, with sides of at most
+ * FG_ONE_LAUNCH_SIDE, run their whole plain or signed transform in one
  * launch (one CTA: initial distances, transpose, every pass); the others, and
  * any image whose passes have a pinned plan (fg_plan_override) or planner
  * limits (fg_set_tuning), run one launch per pass on the planned tiles.  A 2D
  * pass over rows of at least FG_ROW_TILE_MIN_ROW cells is planned on row
  * tiles (FG_PLAN_ROWS), which measured faster than the one-CTA launch from
- * 128 x 128 up (512 x 512: 0.88 against 1.23 ms, iterations 2). */
+ * 128 x 128 and 64 x 512 up (512 x 512: 0.79 against 1.23 ms, iterations 2;
+ * 64 x 64: 0.17 against 0.16). */
 #define FG_ONE_LAUNCH_SIDE 512
-#define FG_ROW_TILE_MIN_ROW 128
+#define FG_ONE_LAUNCH_CELLS 16384
+#define FG_ROW_TILE_MIN_ROW 64
 
 /* Replaces FastGeodis.generalised_geodesic2d
  * (reference: FastGeodis/__init__.py:37-65 -> FastGeodis/fastgeodis.cpp:44-90

@@ -41,13 +41,14 @@ def test_spawned_ranks_report_the_world_size():
 
 
 def test_sweep_kernel_names_follow_the_plans():
-    """The bench line's kernel: the one-CTA kernel for a 2D image with a side
-    under 128, the planner's row tiles for 512 x 512, pinned plans' kinds."""
+    """The bench line's kernel: the one-CTA kernel for a 2D image of fewer
+    than 16384 cells, the planner's row tiles for 512 x 512, pinned plans'
+    kinds."""
     from fastgeodis_gb300 import _lib
 
     w = bench.workload("c1")
     assert bench.sweep_kernel_name(w, None) == "fg_row_tile_kernel"
-    small = dict(w, image=np.zeros((1, 1, 64, 300), np.float32))
+    small = dict(w, image=np.zeros((1, 1, 64, 200), np.float32))
     assert bench.sweep_kernel_name(small, None) == "fg_row2d_kernel"
     pinned = {"plans": {"1,1,512": [8, 1, 128, 0]}}
     assert bench.sweep_kernel_name(w, pinned) == "fg_pass_kernel"

@@ -102,13 +102,13 @@ def test_2d_vs_oracle(shape, C):
         assert bits_equal(got, want), (shape, C, lamb, it, np.abs(got - want).max())
 
 
-@pytest.mark.parametrize("shape", [(1, 5), (31, 33), (96, 200), (512, 100), (120, 512)])
+@pytest.mark.parametrize("shape", [(1, 5), (31, 33), (96, 150), (512, 30), (31, 512), (127, 128)])
 @pytest.mark.parametrize("C", [1, 2, 3, 4])
 def test_one_launch_forms_vs_oracle(shape, C):
-    """Images up to 512 per side with a side under 128 run in one launch (one
-    thread per cell of a row), compiled per channel count and lamb form (0: no
-    image term, 1: no spatial term, else general): plain and signed against
-    the oracle."""
+    """Images of fewer than 16384 cells, up to 512 per side, run in one launch
+    (one thread per cell of a row), compiled per channel count and lamb form
+    (0: no image term, 1: no spatial term, else general): plain and signed
+    against the oracle."""
     assert _lib.runs_in_one_launch(shape)
     rng = np.random.default_rng(hash((shape, C, "one")) % 2**32)
     img, m = rand_case(rng, shape, C)

@@ -267,10 +267,11 @@ def test_chunked_override():
     assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
 
 
-@pytest.mark.parametrize("N2,T2", [(128, 32), (300, 32), (512, 32), (513, 64), (600, 64), (1024, 64), (1025, 32),
+@pytest.mark.parametrize("N2,T2", [(64, 32), (100, 32), (128, 32), (300, 32), (512, 32), (513, 64), (600, 64),
+                                   (1024, 64), (1025, 32),
                                    (4864, 32), (4865, 64), (8192, 64), (9729, 128), (19456, 128)])
 def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
-    """2D rows of 128 cells and more: row tiles (one thread per cell of a
+    """2D rows of 64 cells and more: row tiles (one thread per cell of a
     tile and its halos), a hand-off every 32 steps (the measured optimum).
     Rows up to 1024 cells: one thread-block cluster of at most 16 tiles (32
     cells up to 512, else 64); longer rows: the narrowest of 32, 64, 128
@@ -283,19 +284,21 @@ def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
     # more than 4 channels take the pass kernel on 128-cell tiles
     q = _lib.plan_describe(1, 1, N2, C=6)
     assert not q["lean"] & _lib.FG_PLAN_ROWS and q["T2"] in (128, T2) or q["S"] <= 8
-    # rows shorter than 128 cells and images wider than 152 such tiles keep the cost model's plan
-    assert _lib.plan_describe(1, 1, 127)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
+    # rows shorter than 64 cells and images wider than 152 such tiles keep the cost model's plan
+    assert _lib.plan_describe(1, 1, 63)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
 
 
 def test_one_launch_rule():
-    """The per-call path's one-CTA launch: sides up to 512, one under 128."""
-    assert _lib.FG_ROW_TILE_MIN_ROW == 128 and _lib.FG_ONE_LAUNCH_SIDE == 512
-    assert _lib.runs_in_one_launch((64, 96)) and _lib.runs_in_one_launch((512, 127))
-    assert _lib.runs_in_one_launch((1, 5))
-    for shape in [(128, 128), (512, 512), (127, 513), (256, 300)]:
+    """The per-call path's one-CTA launch: fewer than 16384 cells, sides up
+    to 512."""
+    assert _lib.FG_ROW_TILE_MIN_ROW == 64 and _lib.FG_ONE_LAUNCH_SIDE == 512
+    assert _lib.FG_ONE_LAUNCH_CELLS == 16384
+    assert _lib.runs_in_one_launch((64, 96)) and _lib.runs_in_one_launch((512, 31))
+    assert _lib.runs_in_one_launch((1, 5)) and _lib.runs_in_one_launch((127, 128))
+    for shape in [(128, 128), (512, 512), (127, 513), (256, 300), (64, 512), (20, 600)]:
         assert not _lib.runs_in_one_launch(shape), shape
     header = open(os.path.join(os.path.dirname(__file__), "..", "include", "fastgeodis_gb300.h")).read()
-    for name in ("FG_ROW_TILE_MIN_ROW", "FG_ONE_LAUNCH_SIDE"):
+    for name in ("FG_ROW_TILE_MIN_ROW", "FG_ONE_LAUNCH_SIDE", "FG_ONE_LAUNCH_CELLS"):
         assert re.search(rf"#define {name} (\d+)", header).group(1) == str(getattr(_lib, name))
 
 

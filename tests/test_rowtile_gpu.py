@@ -2,7 +2,7 @@
 per tile and one thread per cell of the tile and its halos of S cells, with
 a hand-off of the halos through exchange words every S steps
 (fastgeodis_gb300/csrc/fg_rowtile2d.cu).  The planner takes them for rows of
-128 cells and more; here they are also forced with fg_plan_override
+64 cells and more; here they are also forced with fg_plan_override
 (FG_PLAN_ROWS) onto small images, through every variant (1 to 4 channels,
 one or two maps, the three arithmetic modes, both layouts, S from 1 to 32).
 The bar is the oracle's bits."""
@@ -114,9 +114,10 @@ def test_cluster_row_tiles_with_a_short_last_tile(shape, S):
 
 
 @pytest.mark.parametrize("shape,C", [((1500, 1300), 1), ((700, 2100), 3), ((3000, 600), 1), ((512, 512), 1),
-                                     ((200, 384), 4), ((128, 130), 2), ((90, 700), 1)])
+                                     ((200, 384), 4), ((128, 130), 2), ((90, 700), 1), ((64, 512), 1),
+                                     ((40, 900), 2), ((100, 200), 1)])
 def test_planner_row_tiles(shape, C):
-    """The planner's own plan for rows of 128 cells and more: row tiles of
+    """The planner's own plan for rows of 64 cells and more: row tiles of
     32 to 128 cells with a hand-off every 32 steps (shorter rows: the cost
     model's plan on the pass kernel)."""
     assert not _lib.runs_in_one_launch(shape)
