@@ -148,7 +148,6 @@ def profile_launch_times():
 
 FG_ONE_LAUNCH_SIDE = 512  # the one-launch 2D kernel's largest side
 FG_ONE_LAUNCH_CELLS = 16384  # the per-call path runs images of fewer cells in one launch
-FG_ROW_TILE_MIN_ROW = 64  # 2D rows of at least this many cells run on row tiles
 
 
 def runs_in_one_launch(shape) -> bool:

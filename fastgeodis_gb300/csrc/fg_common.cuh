@@ -168,8 +168,6 @@ int launch_image_one(const fg_batch2d_item &it, bool is_signed, int iterations, 
 constexpr int kOneLaunchSide = FG_ONE_LAUNCH_SIDE;  // the one-CTA kernel's largest side
 // the per-call path's one-CTA launch: images of fewer cells than this
 constexpr long long kOneLaunchCells = FG_ONE_LAUNCH_CELLS;
-// 2D rows of at least this many cells are planned on row tiles
-constexpr int kRowTileMinRow = FG_ROW_TILE_MIN_ROW;
 
 // Toivanen's raster scan (fg_toivanen.cu): `nmaps` (1-4) distance maps swept
 // in place; spacing_sq = nullptr for images.  bar: 4 counters (16 bytes) of

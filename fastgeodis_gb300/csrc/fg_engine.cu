@@ -417,7 +417,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   // its halos (at most 512), images of 1 to 4 channels read
   auto to_row_tiles = [&](Plan &p, bool clu) {
     const int R = p.T2 + 2 * p.K2;
-    if (cross != 1 || p.tiles2 < 2 || p.chunked || C > kMaxChannels || R > 512) return false;
+    if (cross != 1 || p.chunked || C > kMaxChannels || R > 512) return false;  // one tile: no halos, no hand-off
     p.rowtile = true;
     p.rowcl = clu && p.tiles2 <= kMaxCluster && p.K2 == p.S && p.K2 <= p.T2;
     p.NT = (R + 31) / 32 * 32;
@@ -440,29 +440,38 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     if (chunked || (long long)t1 * t2 <= max_tiles) consider(ovS, T1, T2, t1, t2, (ovLean & FG_PLAN_LEAN) != 0, chunked);
     if (found && (ovLean & FG_PLAN_ROWS)) to_row_tiles(best, (ovLean & FG_PLAN_CLUSTER) != 0);
   }
-  // Rows (2D passes) of kRowTileMinRow cells and more: row tiles (one thread
-  // per cell) with a hand-off every 32 steps (halos of 32 cells: a row's halo
-  // is only its two ends), the narrowest of 32, 64 or 128 cells that the SMs
-  // hold.  Measured on GB300 (images of 64 x 512 to 8192^2, lamb 0.5 and 1):
-  // S = 32 was the fastest period (11-20% ahead of S = 8 on the pass kernel's
-  // tiles) and the row-tile kernel with narrow tiles the fastest form (4096^2:
-  // 18.3 ms on the cost model's plan, 13.0 on the pass kernel's 128-cell
-  // tiles, 7.85 on 32-cell row tiles).  Images of 1 to 4 channels; more take
-  // the pass kernel.  Rows of up to 1024 cells run as one thread-block
-  // cluster of at most 16 tiles (32 cells up to 512, else 64) handing over
-  // through distributed shared memory: measured 5-7% faster than the same
-  // tiles handing over through global memory (512^2: 0.877 -> 0.826 ms plain,
-  // 1.015 -> 0.946 signed; 1024^2: 1.710 ms on 32 tiles of 32 -> 1.638 on a
-  // cluster of 16 tiles of 64), and slower beyond (2048^2 on 16 tiles of 128:
-  // 3.458 ms against 3.356 on 64 tiles of 32).
-  if (!found && cross == 1 && N2 >= kRowTileMinRow && N2 <= 2 * 32 * kMaxCluster) {
+  // 2D passes of 1 to 4 image channels run on row tiles: one thread per cell
+  // and a hand-off every 32 steps (halos of 32 cells: a row's halo is only
+  // its two ends).  Measured on GB300 (images of 64 x 512 to 8192^2, lamb 0.5
+  // and 1): S = 32 was the fastest period (11-20% ahead of S = 8 on the pass
+  // kernel's tiles) and the row-tile kernel with narrow tiles the fastest
+  // form (4096^2: 18.3 ms on the cost model's plan, 13.0 on the pass
+  // kernel's 128-cell tiles, 7.85 on 32-cell row tiles); on rows of 16 to 256
+  // cells (3000 steps, iterations 2) the pass kernel's plan took 4.0-4.8 ms
+  // and row tiles 2.1-2.4.
+  //   * Rows of up to 32 cells: one tile of the whole row (no hand-off).
+  //   * Up to 1024 cells: one thread-block cluster of at most 16 tiles (32
+  //     cells up to 512, else 64) handing over through distributed shared
+  //     memory: 5-7% faster than the same tiles handing over through global
+  //     memory (512^2: 0.877 -> 0.826 ms plain, 1.015 -> 0.946 signed;
+  //     1024^2: 1.710 ms on 32 tiles of 32 -> 1.638 on 16 tiles of 64).
+  //   * Longer rows: the narrowest of 32, 64 or 128 cells that the SMs hold,
+  //     handing over through global memory (2048^2 on a cluster of 16 tiles
+  //     of 128 took 3.458 ms against 3.356 on 64 tiles of 32).
+  // Images of more than 4 channels take the pass kernel (on 128-cell tiles
+  // for rows of more than 512 cells).
+  if (!found && cross == 1 && N2 <= 32) {
+    consider(32, 1, N2, 1, 1, false);
+    if (found && !to_row_tiles(best, false)) found = false;
+  }
+  if (!found && cross == 1 && N2 > 32 && N2 <= 2 * 32 * kMaxCluster) {
     const int T2 = N2 <= 32 * kMaxCluster ? 32 : 64, t2 = (N2 + T2 - 1) / T2;
     if (t2 <= max_tiles) {
       consider(32, 1, T2, 1, t2, false);
       if (found && !(to_row_tiles(best, true) && best.rowcl)) found = false;
     }
   }
-  if (!found && cross == 1 && N2 >= kRowTileMinRow) {
+  if (!found && cross == 1 && N2 > 32 && (C <= kMaxChannels || N2 > 512)) {
     for (int T2 : {32, 64, 128}) {
       if ((N2 + T2 - 1) / T2 > max_tiles) continue;
       consider(32, 1, T2, 1, (N2 + T2 - 1) / T2, false);

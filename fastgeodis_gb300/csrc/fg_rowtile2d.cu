@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
             for (int m = 0; m < M; m++)
               st_async1(rbr + 4u * (po + (unsigned)(m * K + xo - (T2 - K))), best[m], barr + bo);
           }
-        } else if (((t + 1) & (S - 1)) == 0 && t + 1 < L) {
+        } else if (((t + 1) & (S - 1)) == 0 && t + 1 < L && a.tiles2 > 1) {
           // last step of a chunk: publish this cell for the neighbours' halos
           const unsigned long long ep = (unsigned long long)(a.epoch_base + (unsigned)((t + 1) >> lgS)) << 32;
           unsigned long long *w = xw + (long long)(((t + 1) >> lgS) & 1) * xpar;

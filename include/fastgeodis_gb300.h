@@ -105,8 +105,10 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
  * cell; adding FG_PLAN_CLUSTER makes its tiles one thread-block cluster that
  * hands the halos over through distributed shared memory (2 to 16 tiles;
  * otherwise the hand-off goes through global memory as without the flag).
- * The planner takes row tiles for rows of FG_ROW_TILE_MIN_ROW cells and
- * more, clustered for rows of up to 1024 cells.
+ * The planner takes row tiles for every 2D pass of 1 to 4 image channels:
+ * one tile for rows of up to 32 cells, a cluster of up to 16 tiles for rows
+ * of up to 1024 cells, tiles of 32 to 128 cells handing over through global
+ * memory beyond.
  * FG_PLAN_MODE(m) restricts the plan to passes
  * of one arithmetic mode (several transforms of one shape with different
  * weights, e.g. the lambdas of one image, may then get different plans).
@@ -169,14 +171,12 @@ FG_API int fg_selftest_wait(int kind, void *workspace, size_t workspace_bytes, v
  * FG_ONE_LAUNCH_SIDE, run their whole plain or signed transform in one
  * launch (one CTA: initial distances, transpose, every pass); the others, and
  * any image whose passes have a pinned plan (fg_plan_override) or planner
- * limits (fg_set_tuning), run one launch per pass on the planned tiles.  A 2D
- * pass over rows of at least FG_ROW_TILE_MIN_ROW cells is planned on row
- * tiles (FG_PLAN_ROWS), which measured faster than the one-CTA launch from
- * 128 x 128 and 64 x 512 up (512 x 512: 0.79 against 1.23 ms, iterations 2;
- * 64 x 64: 0.17 against 0.16). */
+ * limits (fg_set_tuning), run one launch per pass on the planned tiles: row
+ * tiles (FG_PLAN_ROWS) for 1 to 4 image channels, which measured faster than
+ * the one-CTA launch from 128 x 128 and 64 x 512 up (512 x 512: 0.79 against
+ * 1.23 ms, iterations 2; 64 x 64: 0.17 against 0.16). */
 #define FG_ONE_LAUNCH_SIDE 512
 #define FG_ONE_LAUNCH_CELLS 16384
-#define FG_ROW_TILE_MIN_ROW 64
 
 /* Replaces FastGeodis.generalised_geodesic2d
  * (reference: FastGeodis/__init__.py:37-65 -> FastGeodis/fastgeodis.cpp:44-90

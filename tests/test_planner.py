@@ -53,7 +53,7 @@ def check_plan(cross, N1, N2, p, sms, C=1, maps=1, mode=0):
         # row tiles: 2D, one thread per cell of a tile and its halos, at most
         # 512; as one thread-block cluster: 2 to 16 tiles, halos within a tile
         assert lean in (_lib.FG_PLAN_ROWS, _lib.FG_PLAN_ROWS | _lib.FG_PLAN_CLUSTER)
-        assert cross == 1 and t2 > 1 and C <= 4 and R2 <= nt <= 512 and nt % 32 == 0
+        assert cross == 1 and C <= 4 and R2 <= nt <= 512 and nt % 32 == 0
         if lean & _lib.FG_PLAN_CLUSTER:
             assert t2 <= 16 and K2 == S <= T2
         assert smem <= SMEM_LIMIT
@@ -267,11 +267,11 @@ def test_chunked_override():
     assert not _lib.plan_describe(2, 64, 64)["lean"] & CH
 
 
-@pytest.mark.parametrize("N2,T2", [(64, 32), (100, 32), (128, 32), (300, 32), (512, 32), (513, 64), (600, 64),
-                                   (1024, 64), (1025, 32),
+@pytest.mark.parametrize("N2,T2", [(33, 32), (40, 32), (64, 32), (100, 32), (128, 32), (300, 32), (512, 32), (513, 64),
+                                   (600, 64), (1024, 64), (1025, 32),
                                    (4864, 32), (4865, 64), (8192, 64), (9729, 128), (19456, 128)])
 def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
-    """2D rows of 64 cells and more: row tiles (one thread per cell of a
+    """2D rows of more than 32 cells: row tiles (one thread per cell of a
     tile and its halos), a hand-off every 32 steps (the measured optimum).
     Rows up to 1024 cells: one thread-block cluster of at most 16 tiles (32
     cells up to 512, else 64); longer rows: the narrowest of 32, 64, 128
@@ -284,21 +284,31 @@ def test_long_rows_take_row_tiles_with_32_step_chunks(N2, T2):
     # more than 4 channels take the pass kernel on 128-cell tiles
     q = _lib.plan_describe(1, 1, N2, C=6)
     assert not q["lean"] & _lib.FG_PLAN_ROWS and q["T2"] in (128, T2) or q["S"] <= 8
-    # rows shorter than 64 cells and images wider than 152 such tiles keep the cost model's plan
-    assert _lib.plan_describe(1, 1, 63)["S"] <= 8 and _lib.plan_describe(1, 1, 19457)["S"] <= 8
+    # rows wider than 152 tiles of 128 keep the cost model's plan
+    assert _lib.plan_describe(1, 1, 19457)["S"] <= 8
+
+
+@pytest.mark.parametrize("N2", [1, 2, 5, 17, 32])
+def test_short_rows_take_one_row_tile(N2):
+    """Rows of up to 32 cells: one row tile of the whole row, one warp, no
+    halos and no hand-off (images of 1 to 4 channels)."""
+    for C, maps in ((1, 1), (4, 2)):
+        p = _lib.plan_describe(1, 1, N2, C=C, maps=maps)
+        assert p["lean"] == _lib.FG_PLAN_ROWS and (p["T2"], p["K2"], p["tiles2"], p["threads"]) == (N2, 0, 1, 32)
+    assert not _lib.plan_describe(1, 1, N2, C=5)["lean"] & _lib.FG_PLAN_ROWS
 
 
 def test_one_launch_rule():
     """The per-call path's one-CTA launch: fewer than 16384 cells, sides up
     to 512."""
-    assert _lib.FG_ROW_TILE_MIN_ROW == 64 and _lib.FG_ONE_LAUNCH_SIDE == 512
+    assert _lib.FG_ONE_LAUNCH_SIDE == 512
     assert _lib.FG_ONE_LAUNCH_CELLS == 16384
     assert _lib.runs_in_one_launch((64, 96)) and _lib.runs_in_one_launch((512, 31))
     assert _lib.runs_in_one_launch((1, 5)) and _lib.runs_in_one_launch((127, 128))
     for shape in [(128, 128), (512, 512), (127, 513), (256, 300), (64, 512), (20, 600)]:
         assert not _lib.runs_in_one_launch(shape), shape
     header = open(os.path.join(os.path.dirname(__file__), "..", "include", "fastgeodis_gb300.h")).read()
-    for name in ("FG_ROW_TILE_MIN_ROW", "FG_ONE_LAUNCH_SIDE", "FG_ONE_LAUNCH_CELLS"):
+    for name in ("FG_ONE_LAUNCH_SIDE", "FG_ONE_LAUNCH_CELLS"):
         assert re.search(rf"#define {name} (\d+)", header).group(1) == str(getattr(_lib, name))
 
 
@@ -311,11 +321,16 @@ def test_row_tile_override_validation():
         _lib.check(L.fg_plan_override(1, 1, 300, 8, 1, 64, ROWS))
         p = _lib.plan_describe(1, 1, 300)
         assert p["lean"] == ROWS and (p["S"], p["T2"], p["tiles2"], p["threads"]) == (8, 64, 5, 96)
-        # a region beyond 512 cells stays on the pass kernel
+        # one tile of the whole row: no halos and no hand-off
         _lib.check(L.fg_plan_override(1, 1, 300, 8, 1, 496, ROWS))
-        assert not _lib.plan_describe(1, 1, 300)["lean"] & ROWS
+        p = _lib.plan_describe(1, 1, 300)
+        assert p["lean"] == ROWS and (p["T2"], p["K2"], p["tiles2"], p["threads"]) == (300, 0, 1, 320)
+        # a region beyond 512 cells stays on the pass kernel
+        _lib.check(L.fg_plan_override(1, 1, 600, 8, 1, 600, ROWS))
+        assert not _lib.plan_describe(1, 1, 600)["lean"] & ROWS
     finally:
         _lib.check(L.fg_plan_override(1, 1, 300, 0, 0, 0, 0))
+        _lib.check(L.fg_plan_override(1, 1, 600, 0, 0, 0, 0))
 
 
 @pytest.mark.parametrize("N2,S,T2,clu", [(512, 32, 32, True), (211, 4, 20, True), (1024, 32, 64, True),
@@ -335,8 +350,8 @@ def test_cluster_row_tile_overrides(N2, S, T2, clu):
             p = _lib.plan_describe(1, 1, N2, maps=maps, transposed_write=wt)
             _lib.check(L.fg_plan_override(1, 1, N2, S, 1, T2, ROWS))
             q = _lib.plan_describe(1, 1, N2, maps=maps, transposed_write=wt)
-            if T2 >= N2:
-                assert not p["lean"] & ROWS
+            if T2 >= N2:  # one tile of the whole row: no halos, no cluster
+                assert p["lean"] == q["lean"] == ROWS and p["tiles2"] == 1 and p["K2"] == 0
                 continue
             assert p["lean"] == (ROWS | CLU if clu else ROWS) and q["lean"] == ROWS
             assert (p["tiles2"], p["threads"]) == (q["tiles2"], q["threads"])

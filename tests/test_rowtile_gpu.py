@@ -1,11 +1,13 @@
 """Row tiles: 2D passes whose rows are split into tiles of T2 cells, one CTA
 per tile and one thread per cell of the tile and its halos of S cells, with
 a hand-off of the halos through exchange words every S steps
-(fastgeodis_gb300/csrc/fg_rowtile2d.cu).  The planner takes them for rows of
-64 cells and more; here they are also forced with fg_plan_override
+(fastgeodis_gb300/csrc/fg_rowtile2d.cu).  The planner takes them for every
+2D pass of 1 to 4 image channels; here they are also forced with fg_plan_override
 (FG_PLAN_ROWS) onto small images, through every variant (1 to 4 channels,
-one or two maps, the three arithmetic modes, both layouts, S from 1 to 32).
-The bar is the oracle's bits."""
+one or two maps, the three arithmetic modes, S from 1 to 32, hand-offs
+through global memory or within a thread-block cluster; the passes that
+change layout run in place and a transpose follows).  The bar is the
+oracle's bits."""
 import numpy as np
 import pytest
 import torch
@@ -94,6 +96,30 @@ def test_forced_cluster_row_tiles(op, C, lamb, S, T2):
     _forced(op, C, lamb, S, T2, ROWS | CLU)
 
 
+@pytest.mark.parametrize("op,C,lamb", [("plain", 1, 0.6), ("plain", 3, 1.0), ("signed", 2, 0.4), ("gsf", 1, 0.8)])
+def test_single_tile_row_tiles(op, C, lamb):
+    """A row-tile plan of one tile (T2 >= the row): the whole row on one CTA,
+    one thread per cell, no halos and no hand-off."""
+    shape = (97, 211)
+    img, m = _case(shape, C, 61 + C, soft=op == "gsf")
+    ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
+    try:
+        tune.pin({k: (32, 1, 512, ROWS) for k in tune.pass_keys(shape)})
+        for k in tune.pass_keys(shape):
+            p = _lib.plan_describe(*k)
+            assert p["lean"] == ROWS and p["tiles2"] == 1 and p["K2"] == 0, (k, p)
+        if op == "plain":
+            got, want = fg.generalised_geodesic2d(ti, tm, 1e10, lamb, 2), oracle.geodesic2d(img, m, 1e10, lamb, 2)
+        elif op == "signed":
+            got, want = fg.signed_generalised_geodesic2d(ti, tm, 1e10, lamb, 2), oracle.signed2d(img, m, 1e10, lamb, 2)
+        else:
+            got, want = fg.GSF2d(ti, tm, 0.4, 1e10, lamb, 1), oracle.gsf2d(img, m, 0.4, 1e10, lamb, 1)
+        assert bits_equal(got[0].cpu().numpy(), want)
+        fg.check_status()
+    finally:
+        tune.clear(shape)
+
+
 @pytest.mark.parametrize("shape,S", [((150, 492), 32), ((492, 150), 16), ((40, 512), 32)])
 def test_cluster_row_tiles_with_a_short_last_tile(shape, S):
     """16 tiles of 32 cells whose last tile holds fewer cells than a halo
@@ -115,15 +141,16 @@ def test_cluster_row_tiles_with_a_short_last_tile(shape, S):
 
 @pytest.mark.parametrize("shape,C", [((1500, 1300), 1), ((700, 2100), 3), ((3000, 600), 1), ((512, 512), 1),
                                      ((200, 384), 4), ((128, 130), 2), ((90, 700), 1), ((64, 512), 1),
-                                     ((40, 900), 2), ((100, 200), 1)])
+                                     ((40, 900), 2), ((100, 200), 1), ((3000, 20), 3), ((7, 4000), 1)])
 def test_planner_row_tiles(shape, C):
-    """The planner's own plan for rows of 64 cells and more: row tiles of
-    32 to 128 cells with a hand-off every 32 steps (shorter rows: the cost
-    model's plan on the pass kernel)."""
+    """The planner's own plan for every 2D pass: row tiles with a hand-off
+    every 32 steps (one tile for rows of up to 32 cells, a cluster of up to
+    16 tiles for rows of up to 1024)."""
     assert not _lib.runs_in_one_launch(shape)
     for k in tune.pass_keys(shape):
         p = _lib.plan_describe(*k, C=C)
-        assert bool(p["lean"] & ROWS) == (k[2] >= _lib.FG_ROW_TILE_MIN_ROW), (k, p)
+        assert p["lean"] & ROWS and (p["tiles2"] == 1) == (k[2] <= 32), (k, p)
+        assert bool(p["lean"] & CLU) == (32 < k[2] <= 1024), (k, p)
     img, m = _case(shape, C, 5 + C)
     ti, tm = (torch.from_numpy(a)[None].cuda() for a in (img, m))
     got = fg.generalised_geodesic2d(ti, tm, 1e10, 0.5, 2)[0].cpu().numpy()
