@@ -13,7 +13,8 @@
 // waits: FG_ERR_TIMEOUT).  A row's halo is only its two ends, so a long
 // period is cheap: cells within j of a halo's outer end are stale at chunk
 // step j, but an own cell (at least S from it) never reads one before the
-// next hand-off, so every cell computes every step.  Each thread keeps its
+// next hand-off, so every cell computes every step (a plan of one tile,
+// for rows of up to 32 cells, has no halos and no hand-off).  Each thread keeps its
 // cell's old distance and image values 4-8 steps ahead in registers; the
 // previous row's distances and image values are shared-memory rows with a
 // NaN apron (cells outside the image never win a min).  Each step's own
