@@ -229,8 +229,8 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
               const int n = r * 3 + (d2 + 1);  // neighbour number (d1 = r - 1)
 #pragma unroll
               for (int i = 0; i < 4; i++) {
-                // one image channel: d = I(x) - I(y); the reference's l_grad * |d| equals
-                // |l_grad * d| bit for bit (round to nearest is symmetric in sign)
+                // one image channel: d = I(x) - I(y), the image term l_grad * |d| as
+                // the reference forms it (any sign of l_grad)
                 float d = 0.0f, l1 = 0.0f;
                 if (USE_IMG) {
                   if (CT == 1) {
@@ -246,7 +246,7 @@ __device__ __forceinline__ void cluster_body(const PassArgs &a, float *sm) {
                 for (int m = 0; m < M; m++) {
                   float cand;
                   if (MODE == MODE_GENERAL && CT == 1)
-                    cand = __fadd_rn(__fadd_rn(wd[j][m][i + 1 + d2], a.e[m][n]), fabsf(__fmul_rn(a.lg[m], d)));
+                    cand = __fadd_rn(__fadd_rn(wd[j][m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], fabsf(d)));
                   else if (MODE == MODE_GENERAL)
                     cand = __fadd_rn(__fadd_rn(wd[j][m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], l1));
                   else if (MODE == MODE_EUCLID)

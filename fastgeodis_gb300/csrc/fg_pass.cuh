@@ -529,8 +529,8 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
             const int k = r * 3 + (d2 + 1);  // candidate number 0 .. 3 * NR - 1
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-              // one image channel: d = I(x) - I(y); the reference's l_grad * |d|
-              // equals |l_grad * d| bit for bit (round to nearest is symmetric in sign)
+              // one image channel: d = I(x) - I(y), the image term l_grad * |d|
+              // as the reference forms it (any sign of l_grad)
               float d = 0.0f, l1 = 0.0f;
               if (WIDE) {
                 l1 = l1w[d2 + 1][i];
@@ -548,7 +548,7 @@ __device__ __forceinline__ void pass_body(const PassArgs &ar, const int tile, fl
               for (int m = 0; m < M; m++) {
                 float cand;
                 if (MODE == MODE_GENERAL && CT == 1)
-                  cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), fabsf(__fmul_rn(a.lg[m], d)));
+                  cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], fabsf(d)));
                 else if (MODE == MODE_GENERAL)
                   cand = __fadd_rn(__fadd_rn(dp[m][i + 1 + d2], a.e[m][n]), __fmul_rn(a.lg[m], l1));
                 else if (MODE == MODE_EUCLID)

@@ -107,8 +107,8 @@ __device__ __forceinline__ void row_pass(const PassArgs &ar, float *sm) {
               v = __fadd_rn(dq, e[m][o + 1]);
             else if (MODE == MODE_GEO)
               v = __fadd_rn(dq, l1);
-            else if (C == 1)  // the reference's l_grad * |d| equals |l_grad * d| bit for bit
-              v = __fadd_rn(__fadd_rn(dq, e[m][o + 1]), fabsf(__fmul_rn(lg[m], d)));
+            else if (C == 1)  // the reference's l_grad * |d| (any sign of l_grad)
+              v = __fadd_rn(__fadd_rn(dq, e[m][o + 1]), __fmul_rn(lg[m], fabsf(d)));
             else
               v = __fadd_rn(__fadd_rn(dq, e[m][o + 1]), __fmul_rn(lg[m], l1));
             best[m] = fminf(best[m], v);

@@ -182,8 +182,8 @@ __global__ void __launch_bounds__(512, 1) fg_row_tile_kernel(const PassArgs a) {
               v = __fadd_rn(dq, e[m][o + 1]);
             else if (MODE == MODE_GEO)
               v = __fadd_rn(dq, l1);
-            else if (C == 1)  // the reference's l_grad * |d| equals |l_grad * d| bit for bit
-              v = __fadd_rn(__fadd_rn(dq, e[m][o + 1]), fabsf(__fmul_rn(lg[m], d)));
+            else if (C == 1)  // the reference's l_grad * |d| (any sign of l_grad)
+              v = __fadd_rn(__fadd_rn(dq, e[m][o + 1]), __fmul_rn(lg[m], fabsf(d)));
             else
               v = __fadd_rn(__fadd_rn(dq, e[m][o + 1]), __fmul_rn(lg[m], l1));
             best[m] = fminf(best[m], v);  // a NaN neighbour (outside the image) never wins

@@ -140,6 +140,20 @@ def cases(rng):
                     spacing=[1.0, 1.0, 1.0]))
     out.append(dict(name="s3d_c8", op="signed3d", image=img, mask=m, v=1e10, lamb=0.7, iter=2,
                     spacing=[2.0, 0.5, 0.5]))
+    # lamb outside [0, 1] (the reference does not restrict it): a negative
+    # image weight, and a negative step-length weight
+    img = smooth_noise(rng, (47, 53), 2.0, 0.0, 255.0)[None]
+    m = disks(rng, (47, 53), 3, 2)[None]
+    out.append(dict(name="g2d_lneg", op="geodesic2d", image=img, mask=m, v=1e10, lamb=-0.4, iter=2))
+    out.append(dict(name="g2d_l1.5", op="geodesic2d", image=img, mask=m, v=1e10, lamb=1.5, iter=2))
+    out.append(dict(name="s2d_lneg", op="signed2d", image=img, mask=m, v=1e10, lamb=-0.25, iter=2))
+    img3 = (rng.random((3, 29, 31)) * 255).astype(np.float32)
+    out.append(dict(name="g2d_c3_lneg", op="geodesic2d", image=img3, mask=disks(rng, (29, 31), 2, 2)[None],
+                    v=1e10, lamb=-0.3, iter=2))
+    img = rng.random((1, 11, 13, 12)).astype(np.float32)
+    m = disks(rng, (11, 13, 12), 2, 1)[None]
+    out.append(dict(name="g3d_lneg", op="geodesic3d", image=img, mask=m, v=1e10, lamb=-0.3, iter=2,
+                    spacing=[1.5, 0.8, 1.1]))
     return out
 
 

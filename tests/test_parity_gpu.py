@@ -347,3 +347,34 @@ def test_3d_wide_channels_vs_oracle(shape, C, region, tuning):
     got = fg.GSF3d(t(img), t(m), 0.5, sp, 1e10, 0.6, 1)[0].cpu().numpy()
     assert bits_equal(got, oracle.gsf3d(img, m, 0.5, sp, 1e10, 0.6, 1)), (shape, C, region, "gsf")
     fg.check_status()
+
+
+@pytest.mark.parametrize("lamb", [-0.4, 1.5])
+def test_lamb_outside_the_unit_interval(lamb):
+    """The reference does not restrict lamb to [0, 1]: with a negative image
+    weight (lamb < 0) the image term l_grad * |d| is negative, and with lamb
+    > 1 the step-length term is.  Every sweep form gives the oracle's bits:
+    the one-CTA launch, row tiles (clustered and through global memory),
+    volume tile plans and the cluster sweep kernel."""
+    from fastgeodis_gb300 import tune
+
+    rng = np.random.default_rng(91)
+    for shape, C in (((60, 70), 1), ((300, 400), 1), ((150, 1100), 3)):
+        img, m = rand_case(rng, shape, C)
+        got = fg.generalised_geodesic2d(t(img), t(m), 1e10, lamb, 2)[0].cpu().numpy()
+        assert bits_equal(got, oracle.geodesic2d(img, m, 1e10, lamb, 2)), (shape, C)
+        got = fg.signed_generalised_geodesic2d(t(img), t(m), 1e10, lamb, 1)[0].cpu().numpy()
+        assert bits_equal(got, oracle.signed2d(img, m, 1e10, lamb, 1)), (shape, C, "signed")
+    shape = (20, 48, 40)
+    img, m = rand_case(rng, shape, 1)
+    sp = [1.5, 0.8, 1.1]
+    want = oracle.geodesic3d(img, m, sp, 1e10, lamb, 2)
+    got = fg.generalised_geodesic3d(t(img), t(m), sp, 1e10, lamb, 2)[0].cpu().numpy()
+    assert bits_equal(got, want), "tile plans"
+    try:
+        tune.pin({k: (8, -(-k[1] // 4), k[2], _lib.FG_PLAN_CLUSTER | _lib.FG_PLAN_RUNS2) for k in tune.pass_keys(shape)})
+        got = fg.generalised_geodesic3d(t(img), t(m), sp, 1e10, lamb, 2)[0].cpu().numpy()
+        assert bits_equal(got, want), "cluster plans"
+    finally:
+        tune.clear(shape)
+    fg.check_status()
