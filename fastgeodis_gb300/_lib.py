@@ -161,7 +161,6 @@ FG_PLAN_CLUSTER = 2   # plan flag: one thread-block cluster owns the cross-secti
 FG_PLAN_RUNS2 = 4     # plan flag: cluster sweep kernel, 2 runs of 4 cells per thread
 FG_PLAN_CHUNKED = 8   # plan flag: one ordinary launch per chunk of S steps (tiles need not all be resident)
 FG_PLAN_ROWS = 64     # plan flag: 2D tiles on the row-tile kernel (one thread per cell)
-FG_PLAN_WARPS = 128   # plan flag: 2D pass on warp tiles (one CTA, a warp per strip, 4 cells per lane)
 
 
 def FG_PLAN_MODE(m: int) -> int:

@@ -160,16 +160,6 @@ int cluster_capacity(int size, int threads, size_t smem, int *out);
 int launch_row_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, bool clu, cudaStream_t s);
 size_t row_tile_smem(int cimg, int M, int R, int S, bool clu);
 
-// 2D passes on warp tiles (fg_warptile2d.cu): one CTA of c.threads / 32
-// warps, each owning a.T2 = kWarpCells - 2 a.K2 cells of the row with halos
-// of a.K2 = a.S cells (one warp and no halo for rows of up to kWarpCells);
-// one image channel read or none, one or two maps, in place (wt refused).
-constexpr int kWarpCells = 128;          // region cells of a warp: 4 per lane
-constexpr int kWarpTileMaxRow = 1024;    // longest row on warp tiles
-constexpr int kWarpTileMaxThreads = 512; // 16 warps: a 1024-cell row with halos of 32
-int launch_warp_tiles(const PassArgs &a, const LaunchCfg &c, int M, int mode, bool wt, cudaStream_t s);
-size_t warp_tile_smem(int M, int N2, int K);
-
 // A whole 2D transform (plain, or signed) of one image with both sides up to
 // kOneLaunchSide by one CTA in one launch (fg_row2d.cu, one thread per cell
 // of a row): initial distances, the image transpose, every pass and the

@@ -217,7 +217,6 @@ struct Plan {
   bool chunked = false;  // one ordinary launch per chunk of S steps, any number of tiles
   bool rowtile = false;  // 2D: the row-tile kernel (fg_rowtile2d.cu), one thread per cell of a tile and its halos
   bool rowcl = false;    // row tiles of one thread-block cluster, handing over through distributed shared memory
-  bool warptile = false;  // 2D: one CTA of warp tiles (fg_warptile2d.cu), 4 cells per lane
 };
 
 std::atomic<int> g_tune_region{kMaxRegion};  // largest per-CTA region (cells) the planner may use
@@ -427,25 +426,7 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
     p.lean = false;
     return true;
   };
-  // a 2D pass on warp tiles: halos of K = S cells (T2 = kWarpCells - 2K),
-  // or one warp with no halo for rows of up to kWarpCells cells
-  auto warp_tiles = [&](int S) {
-    if (cross != 1 || C > 1 || M > kMaxMaps || N2 > kWarpTileMaxRow) return false;
-    Plan p{};
-    const int K = N2 <= kWarpCells ? 0 : S, T2 = K ? kWarpCells - 2 * K : N2, nw = (N2 + T2 - 1) / T2;
-    if (32 * nw > kWarpTileMaxThreads) return false;
-    p.T1 = 1, p.T2 = T2, p.K1 = 0, p.K2 = K, p.tiles1 = 1, p.tiles2 = 1, p.S = S;
-    p.NT = 32 * nw, p.B2 = 0, p.rowf = 0, p.P = 8;
-    p.smem = warp_tile_smem(M, N2, K);
-    p.lean = false, p.cluster = false, p.rpt = 0;
-    p.warptile = true;
-    best = p;
-    found = true;
-    return true;
-  };
-  if (ovS > 0 && (ovLean & FG_PLAN_WARPS)) {
-    warp_tiles(ovS);
-  } else if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
+  if (ovS > 0 && (ovLean & FG_PLAN_CLUSTER) && cross == 2) {
     Plan cp;
     const int rpt = (ovLean & FG_PLAN_RUNS2) ? 2 : 0;
     if (cluster_plan(N1, N2, C, M, mode, wt, ovS, ovT1, rpt, (ovLean & FG_PLAN_LEAN) != 0, &cp)) {
@@ -479,9 +460,6 @@ bool make_plan(int cross, int N1, int N2, int C, int M, int mode, bool wt, int m
   //     of 128 took 3.458 ms against 3.356 on 64 tiles of 32).
   // Images of more than 4 channels take the pass kernel (on 128-cell tiles
   // for rows of more than 512 cells).
-  // Rows of up to kWarpTileMaxRow cells with one image channel read (or
-  // none): one CTA of warp tiles, halos of 16 cells handed over every 16 steps.
-  if (!found) warp_tiles(16);
   if (!found && cross == 1 && N2 <= 32) {
     consider(32, 1, N2, 1, 1, false);
     if (found && !to_row_tiles(best, false)) found = false;
@@ -701,7 +679,6 @@ int launch_pass(const PassArgs &a, const Plan &p, int cross, int M, int mode, bo
   return profiled_launch(s, (long long)a.L * a.N1 * a.N2 * M, a.L, [&] {
     if (p.cluster) return launch_pass_cluster(a, c, M, mode, wt, s);
     if (p.rowtile) return launch_row_tiles(a, c, M, mode, wt, p.rowcl, s);
-    if (p.warptile) return launch_warp_tiles(a, c, M, mode, wt, s);
     if (!p.chunked)
       return cross == 2 ? launch_pass_cross2(a, c, M, mode, wt, s) : launch_pass_cross1(a, c, M, mode, wt, s);
     // one ordinary launch per chunk of S steps, in stream order
@@ -817,7 +794,7 @@ int for_each_pass(const Geometry &g, const float *img_r, const float *img_t, con
           Plan p;
           int rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, wt, &p);
           if (rc != FG_OK) return rc;
-          const bool split = wt && emit_t != nullptr && (p.cluster || p.rowtile || p.warptile);  // in place, then a transpose
+          const bool split = wt && emit_t != nullptr && (p.cluster || p.rowtile);  // in place, then a transpose
           if (split) {
             rc = plan_fn(cross, A.N1, A.N2, Cimg, M, mode, false, &p);
             if (rc != FG_OK) return rc;
@@ -1152,16 +1129,13 @@ int fg_plan_override(int cross, int N1, int N2, int S, int T1, int T2, int lean)
   } else {
     if (S < 1 || S > 32 || (S & (S - 1)))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: S must be a power of two up to 32");
-    if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4 && !(lean & FG_PLAN_WARPS)))  // warp tiles: T2 follows from S
-      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
-    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_CHUNKED | FG_PLAN_ROWS | FG_PLAN_WARPS;
+    if (T1 < 1 || T2 < 1 || (T2 < N2 && T2 % 4)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad tile extents");
+    const int all = FG_PLAN_LEAN | FG_PLAN_CLUSTER | FG_PLAN_RUNS2 | FG_PLAN_CHUNKED | FG_PLAN_ROWS;
     if (lean < 0 || (lean & ~all)) return fail(FG_ERR_INVALID_ARGUMENT, "plan override: bad flags");
     if ((lean & FG_PLAN_CHUNKED) && (lean & FG_PLAN_CLUSTER))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: a chunked plan is a tile plan");
     if ((lean & FG_PLAN_ROWS) && (cross != 1 || (lean & (FG_PLAN_CHUNKED | FG_PLAN_RUNS2))))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: row tiles are 2D tile plans");
-    if ((lean & FG_PLAN_WARPS) && (cross != 1 || S < 4 || (lean & ~FG_PLAN_WARPS)))
-      return fail(FG_ERR_INVALID_ARGUMENT, "plan override: warp tiles are 2D plans with S from 4 to 32");
     if ((lean & FG_PLAN_RUNS2) && !(lean & FG_PLAN_CLUSTER))
       return fail(FG_ERR_INVALID_ARGUMENT, "plan override: runs per thread apply to cluster plans");
     if ((lean & FG_PLAN_CLUSTER) && !(lean & FG_PLAN_ROWS) && (cross != 2 || S < 2))
@@ -1184,8 +1158,7 @@ int fg_plan_describe(int cross, int N1, int N2, int C, int maps, int mode, int t
   const int v[11] = {p.S,  p.T1, p.T2, p.K1, p.K2, p.tiles1, p.tiles2, p.NT, p.P, (int)p.smem,
                      (p.lean ? FG_PLAN_LEAN : 0) | (p.cluster ? FG_PLAN_CLUSTER : 0) |
                          (p.rpt == 2 ? FG_PLAN_RUNS2 : 0) | (p.chunked ? FG_PLAN_CHUNKED : 0) |
-                         (p.rowtile ? FG_PLAN_ROWS : 0) | (p.rowcl ? FG_PLAN_CLUSTER : 0) |
-                         (p.warptile ? FG_PLAN_WARPS : 0)};
+                         (p.rowtile ? FG_PLAN_ROWS : 0) | (p.rowcl ? FG_PLAN_CLUSTER : 0)};
   for (int i = 0; i < 11; i++) plan[i] = v[i];
   return FG_OK;
 }

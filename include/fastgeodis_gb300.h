@@ -72,7 +72,6 @@ FG_API int fg_set_tuning(int max_region_cells, int max_tiles);
 #define FG_PLAN_RUNS2 4   /* cluster plan on the cluster sweep kernel, 2 runs of 4 cells per thread */
 #define FG_PLAN_CHUNKED 8 /* a tile plan run as one ordinary launch per chunk of S steps */
 #define FG_PLAN_ROWS 64   /* a 2D tile plan on the row-tile kernel: one thread per cell of a tile and its halos */
-#define FG_PLAN_WARPS 128 /* a 2D pass on warp tiles: one CTA, a warp per strip of the row, 4 cells per lane */
 /* fg_plan_override only: the plan applies to passes of arithmetic mode m
  * alone (0: general, 1: l_grad == 0, 2: l_eucl == 0 and l_grad == 1), and
  * wins over a plan without this flag; without it a plan applies to every
