@@ -848,6 +848,40 @@ def signed_gsf_record(FG, repeats=3):
                     "thread beside the first, two OpenMP teams on the same cores"}
 
 
+def signed_gsf_gpu_record(fg, repeats=5):
+    """This engine's plain, signed and GSF transforms of the 2D workload's
+    512^2 image on the device (CUDA events, median of `repeats` after
+    warm-up): the counterpart of the reference arm's signed_gsf_cpu record.
+    A signed transform sweeps both maps in each pass; GSF is a signed
+    transform, thresholds and a second signed transform."""
+    import torch
+
+    w = workload("c1")
+    img, m = (torch.from_numpy(a).cuda() for a in (w["image"], w["mask"]))
+    lamb, it, v = 1.0, 2, 1e10
+
+    def med(fn):
+        fn()
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(repeats):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    t_plain = med(lambda: fg.generalised_geodesic2d(img, m, v, lamb, it))
+    t_signed = med(lambda: fg.signed_generalised_geodesic2d(img, m, v, lamb, it))
+    t_gsf = med(lambda: fg.GSF2d(img, m, 0.5, v, lamb, it))
+    return {"image": "1x1x512x512 (the 2D workload), lamb 1.0, iterations 2, theta 0.5 for GSF", "repeats": repeats,
+            "plain2d_ms": round(t_plain, 4), "signed2d_ms": round(t_signed, 4), "GSF2d_ms": round(t_gsf, 4),
+            "note": "median device milliseconds through the public API, inputs resident"}
+
+
 def run_reference_arm(args, w, rank, world):
     """The reference's own implementation on the workload, on all host cores:
     its installed package (OpenMP CPU path) where it could be built here,
@@ -1408,6 +1442,7 @@ def run_gpu_arm(args, w, rank, world):
         a_ms, a_launches, a_vp = _lib.profile_end()
         alone = {"lamb": w["lambs"][ka], "transforms": n_alone, "pass_ms": a_ms, "launches": a_launches, "vp": a_vp}
     extra = {}
+    sg = signed_gsf_gpu_record(fg) if w["name"] in ("c1", "c2") and not args.kernels_only else None
     if w["name"] == "c2" and not args.no_extras:
         # the batch targets, measured in the same run (outside the timed steps)
         extra["b256"] = b256_record(args, dev, rank, world, dist)
@@ -1492,6 +1527,7 @@ def run_gpu_arm(args, w, rank, world):
         "clocks": clk,
         "gpu_launches": int((pass_launches + aux_launches + init_launches) / args.steps),
         **({"batch_targets": extra} if extra else {}),
+        **({"signed_gsf_gpu": sg} if sg else {}),
     }
     print(json.dumps(line), flush=True)
     if dist:
