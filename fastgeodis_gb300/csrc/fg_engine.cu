@@ -555,6 +555,7 @@ struct Workspace {
   int *status;
   unsigned long long *xch;  // halo exchange words (PassArgs::xch)
   size_t xch_bytes;
+  unsigned long long *xch2;  // GSF: the words of its second map group, swept beside the first
   char *base;
   size_t map_stride;  // floats between maps
 };
@@ -579,9 +580,14 @@ size_t xch_bytes(int D, int H, int W) {
 int extra_maps(int op) { return op == FG_OP_PLAIN ? 0 : (op == FG_OP_SIGNED ? 1 : 4); }
 int t_maps(int op) { return op == FG_OP_PLAIN ? 1 : (op == FG_OP_SIGNED ? 2 : 4); }
 
+// exchange-word regions: GSF sweeps its four second-stage maps as two groups
+// of two at once, each with its own words
+int xch_regions(int op) { return op == FG_OP_GSF ? 2 : 1; }
+
 size_t workspace_bytes(int op, int C, int D, int H, int W) {
   const long long P = (long long)D * H * W;
-  return kWsHeader + xch_bytes(D, H, W) + (size_t)(extra_maps(op) + t_maps(op)) * map_bytes(P) + map_bytes(P * C);
+  return kWsHeader + xch_regions(op) * xch_bytes(D, H, W) + (size_t)(extra_maps(op) + t_maps(op)) * map_bytes(P) +
+         map_bytes(P * C);
 }
 
 int bind_workspace(void *ws, size_t bytes, int op, int C, int D, int H, int W, Workspace *w) {
@@ -595,7 +601,8 @@ int bind_workspace(void *ws, size_t bytes, int op, int C, int D, int H, int W, W
   w->status = reinterpret_cast<int *>(base);
   w->xch = reinterpret_cast<unsigned long long *>(base + kWsHeader);
   w->xch_bytes = xch_bytes(D, H, W);
-  w->base = base + kWsHeader + w->xch_bytes;
+  w->xch2 = xch_regions(op) > 1 ? reinterpret_cast<unsigned long long *>(base + kWsHeader + w->xch_bytes) : nullptr;
+  w->base = base + kWsHeader + xch_regions(op) * w->xch_bytes;
   w->map_stride = map_bytes(P) / 4;
   return FG_OK;
 }
@@ -921,6 +928,30 @@ int check_common(const float *image, int C, int D, int H, int W, const float *ma
 // fastgeodis_cpu.cpp (toivanen = false) or Toivanen's scan of
 // geodis_toivanen.cpp (toivanen = true); the compositions are the same
 // (FastGeodis/fastgeodis.cpp:241-258, 319-343 and :260-277, 345-369).
+// A side stream of the calling host thread for work that runs beside the
+// caller's stream `s` (same device and priority, non-blocking; created once
+// per thread), or nullptr while `s` is being captured into a graph (the work
+// then stays on `s`) or if none can be made.
+cudaStream_t side_stream(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  int dev = 0, prio = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaStreamGetPriority(s, &prio) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  thread_local std::map<std::pair<int, int>, cudaStream_t> streams;
+  cudaStream_t &st = streams[std::make_pair(dev, prio)];
+  if (st == nullptr && cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio) != cudaSuccess) {
+    (void)cudaGetLastError();
+    st = nullptr;
+  }
+  return st;
+}
+
 int run_op(int op, const Geometry &g, const float *image, const float *mask, int Cm, float *out, float v, float lg,
            float le, float theta, int iterations, void *ws, size_t ws_bytes, void *stream, bool toivanen = false) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -939,6 +970,7 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   float *img_t = tb + t_maps(op) * ms_;
   // epoch 0 is never wanted; earlier calls' words must not match this call's epochs
   if (!toivanen) FG_CUDA(cudaMemsetAsync(w.xch, 0, w.xch_bytes, s));
+  if (!toivanen && w.xch2) FG_CUDA(cudaMemsetAsync(w.xch2, 0, w.xch_bytes, s));
   unsigned counter = 0;
   // Toivanen's group barriers: 4 counters in the spare bytes of the header
   unsigned *toiv_bar = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(w.status) + 64);
@@ -1008,7 +1040,36 @@ int run_op(int op, const Geometry &g, const float *image, const float *mask, int
   // Ds = xr0 - xr1; the four initial maps go to out, xr1, xr2, xr3
   fg_gsf_mid_kernel<<<ew_grid(P), 256, 0, s>>>(xr[0], xr[1], out, xr[1], xr[2], xr[3], P, v, theta);
   FG_CUDA(cudaGetLastError());
-  {
+  cudaStream_t side = toivanen ? nullptr : side_stream(s);
+  if (side) {
+    // the two signed transforms of stage two at once: maps (out, xr1) on the
+    // caller's stream, (xr2, xr3) on a side stream with their own exchange
+    // words (a pass of a 2D image or a volume slab fills few SMs)
+    MapSet ma{2, {out, xr[1]}, {xt[0], xt[1]}, lg, le};
+    MapSet mb{2, {xr[2], xr[3]}, {xt[2], xt[3]}, lg, le};
+    Workspace w2 = w;
+    w2.xch = w.xch2;
+    unsigned counter2 = 0;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    FG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    if (cudaEventCreateWithFlags(&join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventDestroy(fork);
+      return fail(FG_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    }
+    cudaError_t e = cudaEventRecord(fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
+    if (e == cudaSuccess) {
+      rc = run_transform(g, image, img_t, ma, iterations, w, &counter, s);
+      const int rc2 = run_transform(g, image, img_t, mb, iterations, w2, &counter2, side);
+      if (rc == FG_OK) rc = rc2;
+      e = cudaEventRecord(join, side);  // the caller's stream waits for the side stream's work either way
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    }
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
+    if (rc != FG_OK) return rc;
+  } else {
     MapSet ms{4, {out, xr[1], xr[2], xr[3]}, {xt[0], xt[1], xt[2], xt[3]}, lg, le};
     rc = sweep(ms);
     if (rc != FG_OK) return rc;
