@@ -378,3 +378,44 @@ def test_lamb_outside_the_unit_interval(lamb):
     finally:
         tune.clear(shape)
     fg.check_status()
+
+
+def test_gsf_side_stream_eager_threads_and_graph():
+    """GSF runs the two signed transforms of its second stage at once, the
+    second on a side stream of the calling thread: the oracle's bits from
+    two host threads on their own streams, and from a CUDA graph (captured
+    calls keep both on the captured stream)."""
+    import threading
+
+    rng = np.random.default_rng(77)
+    cases = [rand_case(rng, (150, 300), 1), rand_case(rng, (12, 40, 36), 1)]
+    wants = [oracle.gsf2d(*cases[0], 0.5, 1e10, 0.8, 2), oracle.gsf3d(*cases[1], 0.5, [1.2, 0.9, 1.0], 1e10, 0.8, 2)]
+    outs = [None, None]
+
+    def run(k):
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            img, m = (t(a) for a in cases[k])
+            r = fg.GSF2d(img, m, 0.5, 1e10, 0.8, 2) if k == 0 else fg.GSF3d(img, m, 0.5, [1.2, 0.9, 1.0], 1e10, 0.8, 2)
+            outs[k] = r[0].cpu().numpy()
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for k in range(2):
+        assert bits_equal(outs[k], wants[k]), k
+    img, m = (t(a) for a in cases[0])
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        fg.GSF2d(img, m, 0.5, 1e10, 0.8, 2)  # plans, attributes and workspace set up before capture
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = fg.GSF2d(img, m, 0.5, 1e10, 0.8, 2)
+    g.replay()
+    torch.cuda.synchronize()
+    assert bits_equal(out[0].cpu().numpy(), wants[0])
+    fg.check_status()
