@@ -158,3 +158,30 @@ def test_tiled_batch_arguments_without_launch():
     assert L.fg_batch_geodesic2d_tiled(p, tiles, 2, 1, 1000, 2, p, need - 8, p, None) == _lib.FG_ERR_WORKSPACE
     bad = (ctypes.c_int * 2)(4, 1)
     assert L.fg_batch_geodesic2d_tiled(p, bad, 2, 1, 1000, 2, p, need, p, None) == _lib.FG_ERR_INVALID_ARGUMENT
+
+
+def test_header_constants_match_the_binding():
+    """Every integer constant of the C header that the Python binding also
+    names (status codes, operations, plan flags, one-launch limits, batch
+    flags) has the same value on both sides."""
+    header = open(os.path.join(ROOT, "include", "fastgeodis_gb300.h")).read()
+    defines = {name: int(val, 0) for name, val in re.findall(r"#define (FG_\w+) (0x[0-9a-fA-F]+|\d+)\b", header)}
+    named = {n: v for n, v in defines.items() if hasattr(_lib, n)}
+    assert {"FG_OK", "FG_ERR_TIMEOUT", "FG_OP_GSF", "FG_PLAN_ROWS", "FG_PLAN_CHUNKED", "FG_ONE_LAUNCH_CELLS"} <= set(named)
+    for name, value in named.items():
+        assert getattr(_lib, name) == value, name
+    for name in defines:  # every status code, operation and plan flag is bound
+        if name.startswith(("FG_ERR_", "FG_OP_", "FG_PLAN_")) and name != "FG_PLAN_MODE_MASK":
+            assert hasattr(_lib, name), name
+    for m in range(3):
+        assert _lib.FG_PLAN_MODE(m) == (m + 1) << 4
+
+
+def test_batch_flags_match_the_header():
+    from fastgeodis_gb300 import batch, batch3d
+
+    header = open(os.path.join(ROOT, "include", "fastgeodis_gb300.h")).read()
+    defines = dict((n, int(v)) for n, v in re.findall(r"#define (FG_BATCH_\w+) (\d+)\b", header))
+    assert defines == {"FG_BATCH_SIGNED": batch.FG_BATCH_SIGNED, "FG_BATCH_SPLIT": batch.FG_BATCH_SPLIT,
+                       "FG_BATCH_SECOND": batch.FG_BATCH_SECOND}
+    assert batch3d.FG_BATCH_SIGNED == defines["FG_BATCH_SIGNED"]
