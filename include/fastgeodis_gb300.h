@@ -216,7 +216,12 @@ FG_API int fg_signed_generalised_geodesic3d(const float *image, int C, int D, in
 
 /* Replaces FastGeodis.GSF2d (reference: FastGeodis/__init__.py:526-553 ->
  * FastGeodis/fastgeodis.cpp:319-330).  lambda as float; 1 - lambda is formed
- * in float inside, as the reference does. */
+ * in float inside, as the reference does.  The two signed transforms of the
+ * second stage run at once: the second on a side stream of the calling host
+ * thread (same device and priority), forked from and joined back to `stream`
+ * with events, so the call stays ordered on `stream` as usual; while `stream`
+ * is being captured into a CUDA graph both run on it.  The same holds for
+ * fg_GSF3d. */
 FG_API int fg_GSF2d(const float *image, int C, int H, int W, const float *mask,
              int Cm, float theta, float v, float lambda, int iterations,
              float *out, void *workspace, size_t workspace_bytes, void *stream);
